@@ -1,0 +1,145 @@
+/*
+ * libjurassic_gb300 -- C ABI of the GB300 JURASSIC forward model.
+ *
+ * Plain C: opaque context handle, plain pointers and sizes, int status
+ * codes (JGB_OK == 0) instead of the reference's exit() on error
+ * (ERRMSG, jurassic.h:237-241).  All array arguments are host pointers
+ * unless a function name ends in _dev (device pointers, inputs already
+ * resident in GPU memory).
+ *
+ * Array layouts follow the reference structs with runtime sizes:
+ *   channel-major results rad/tau [nd][nray] (obs_t, jurassic.h:766-772),
+ *   emitter-major volume mixing ratios q [ng][nlev] (atm_t, jurassic.h:518).
+ *
+ * Threading: a context owns one CUDA stream; calls on one context must not
+ * overlap (use one context per host thread).  Contexts are independent.
+ */
+#ifndef JURASSIC_GB300_H
+#define JURASSIC_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define JGB_OK 0
+#define JGB_ERR_ARG 1          /* invalid argument or size */
+#define JGB_ERR_CUDA 2         /* CUDA runtime failure */
+#define JGB_ERR_STATE 3        /* tables or source function not set */
+#define JGB_ERR_LOS 4          /* too many LOS points (jurassic.c:4335) */
+#define JGB_ERR_SURFACE 5      /* observer below surface (jurassic.c:4238) */
+#define JGB_ERR_UNSUPPORTED 6  /* option outside the device path (e.g. RFM) */
+#define JGB_ERR_IO 7           /* file could not be read */
+#define JGB_ERR_NUMERIC 8      /* matrix not positive definite */
+
+#define JGB_FP64 0   /* plain FP64: rounding-level agreement with the reference */
+#define JGB_MIXED 1  /* FP32 path loop with compensated sums (<= 10 mK BT) */
+
+typedef struct jgb_ctx jgb_ctx;
+
+/* Forward-model control parameters: the fields of ctl_t (jurassic.h:541-675)
+   that the forward model, Jacobian and retrieval read. */
+typedef struct {
+  int ng;                        /* emitters */
+  const char *const *emitter;    /* [ng] names; "CO2"/"H2O" enable continua */
+  int nd;                        /* channels */
+  const double *nu;              /* [nd] centroid wavenumbers [cm^-1] */
+  int nw;                        /* spectral windows */
+  const int *window;             /* [nd] window of each channel */
+  int ncl;                       /* cloud spectral grid points */
+  const double *clnu;            /* [ncl] */
+  int nsf;                       /* surface spectral grid points */
+  const double *sfnu;            /* [nsf] */
+  int sftype;                    /* 0 none, 1 emission, 2 +downward, 3 +solar */
+  double sfsza;                  /* solar zenith angle, <0 = computed */
+  double hydz;                   /* hydrostatic reference height, <0 = off */
+  int ctm_co2, ctm_h2o, ctm_n2, ctm_o2;  /* continua switches */
+  int refrac;                    /* refraction on/off */
+  double rayds, raydz;           /* ray-tracing step controls [km] */
+  int formod;                    /* 0 = CGA, 1 = EGA */
+  int write_bbt;                 /* 1 = results as brightness temperature */
+  double retp_zmin, retp_zmax;   /* state-vector windows (atm2x) */
+  double rett_zmin, rett_zmax;
+  const double *retq_zmin, *retq_zmax;  /* [ng] */
+  const double *retk_zmin, *retk_zmax;  /* [nw] */
+  int ret_clz, ret_cldz, ret_clk, ret_sfz, ret_sfp, ret_sft, ret_sfeps;
+  int nlos_max;                  /* LOS points per ray (reference NLOS); 0 = 4096 */
+} jgb_ctl;
+
+/* A batch of independent observations, each with its own atmosphere
+   (levels lev_off[i]..lev_off[i+1]-1) and rays (ray_off[i]..ray_off[i+1]-1).
+   One observation is the reference's (atm_t, obs_t) pair of formod(). */
+typedef struct {
+  int nobs;
+  const int *lev_off;            /* [nobs+1] */
+  const double *time, *z, *lon, *lat;  /* [nlev] */
+  double *p;                     /* [nlev]; rewritten when hydz >= 0 */
+  const double *t;               /* [nlev] */
+  const double *q;               /* [ng][nlev] */
+  const double *k;               /* [nw][nlev] */
+  const double *scal;            /* [nobs][5+ncl+nsf]: clz cldz clk[] sfz sfp sft sfeps[] */
+  const int *ray_off;            /* [nobs+1] */
+  const double *geo;             /* [7][nray]: time obsz obslon obslat vpz vplon vplat */
+  double *rad;                   /* [nd][nray] in: NaN = masked channel; out: radiance/BT */
+  double *tau;                   /* [nd][nray] out: path transmittance */
+  double *tp;                    /* [3][nray] out: tangent point z lon lat */
+} jgb_batch;
+
+/* Device times [ms] of the last forward call, measured with CUDA events on
+   the context stream. */
+typedef struct {
+  double h2d_ms, hydro_ms, trace_ms, pack_ms, path_ms, d2h_ms, total_ms;
+  long long los_points;          /* LOS points of the batch */
+  int path_launches;             /* kernels launched by the last call */
+} jgb_stats;
+
+/* Context: replaces the process-global table state initialised by the first
+   formod_pencil call (jurassic.c:3202-3217). */
+int jgb_create(const jgb_ctl *ctl, int device, jgb_ctx **out);
+void jgb_destroy(jgb_ctx *ctx);
+const char *jgb_last_error(const jgb_ctx *ctx);
+
+/* Emissivity tables (tbl_t, jurassic.h:778-807; read_tbl, jurassic.c:4949).
+   jgb_tables_init fixes the capacities; jgb_set_table uploads one
+   (channel, emitter) table whose arrays have the layout of tbl_t rows:
+   p[np], nt[np], t[np][tt_cap], nu[np][tt_cap], u/eps[np][tt_cap][tu_cap]. */
+int jgb_tables_init(jgb_ctx *ctx, int tp, int tt, int tu);
+int jgb_set_table(jgb_ctx *ctx, int id, int ig, int np, const double *p, const int *nt,
+                  const double *t, const int *nu, const float *u, const float *eps,
+                  int tt_cap, int tu_cap);
+
+/* Source function of channel id from its filter function
+   (init_srcfunc, jurassic.c:3631-3681), computed on the device. */
+int jgb_set_filter(jgb_ctx *ctx, int id, int n, const double *fnu, const double *f);
+/* Upload / read back a source-function table sr[1200][nd]. */
+int jgb_set_srcfunc(jgb_ctx *ctx, const double *sr);
+int jgb_get_srcfunc(jgb_ctx *ctx, double *st, double *sr);
+
+/* Forward model of one observation (formod, jurassic.c:3026-3071):
+   atmosphere arrays of np levels, nr rays; same layouts as jgb_batch. */
+int jgb_formod(jgb_ctx *ctx, int np, const double *time, const double *z, const double *lon,
+               const double *lat, double *p, const double *t, const double *q,
+               const double *k, const double *scal, int nr, const double *geo, double *rad,
+               double *tau, double *tp, int precision);
+
+/* Batched forward model of many observations: the seam of the reference's
+   external GPU library, jur_unified_formod_multiple_packages (formod.c:72-73).
+   Host buffers; copies are part of the call. */
+int jgb_formod_batch(jgb_ctx *ctx, const jgb_batch *b, int precision);
+/* Same with every jgb_batch pointer a device pointer. */
+int jgb_formod_batch_dev(jgb_ctx *ctx, const jgb_batch *b, int precision);
+
+int jgb_get_stats(const jgb_ctx *ctx, jgb_stats *out);
+
+/* Page-locked host memory for fast transfers (cudaHostAlloc). */
+void *jgb_host_alloc(unsigned long long bytes);
+void jgb_host_free(void *p);
+/* Device memory for callers that stage inputs themselves. */
+void *jgb_dev_alloc(unsigned long long bytes);
+void jgb_dev_free(void *p);
+int jgb_memcpy_h2d(void *dst, const void *src, unsigned long long bytes);
+int jgb_memcpy_d2h(void *dst, const void *src, unsigned long long bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,822 @@
+// Host side of libjurassic_gb300: context, table and source-function
+// upload, the batched forward-model driver and the C ABI.
+//
+// A context replaces the reference's process-global state (the static
+// tables of formod_pencil, jurassic.c:3202-3217, and the emitter indices
+// cached in formod_continua, 3081) with explicit, device-resident data:
+// one context serves one control set, any number of contexts coexist.
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/jurassic_gb300.h"
+#include "jgb_common.cuh"
+#include "jgb_internal.h"
+
+extern "C" const double jgb_continua_blob[];
+extern "C" const long jgb_continua_count;
+
+using namespace jgb;
+
+namespace {
+
+// Grow-only device buffer.
+struct DevBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  cudaError_t reserve(size_t bytes) {
+    if (bytes <= n) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    const size_t want = bytes + bytes / 8;  // headroom for slightly larger batches
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) n = want;
+    return e;
+  }
+  template <typename T>
+  T* as() const { return static_cast<T*>(p); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+// Offsets of the continuum tables inside the blob (order of continua.bin).
+enum { CT_CO2_296 = 0, CT_CO2_260 = 2001, CT_CO2_230 = 4002, CT_H2O_296 = 6003,
+       CT_H2O_260 = 8004, CT_H2O_FRN = 10005, CT_XFCREV = 12006, CT_N2_B = 12021,
+       CT_N2_BETA = 12119, CT_N2_NU = 12217, CT_O2_B = 12315, CT_O2_BETA = 12405,
+       CT_O2_NU = 12495, CT_TOTAL = 12585 };
+
+// Wavenumber-only factors of ctmco2/ctmh2o/ctmn2/ctmo2
+// (jurassic.c:1718-1741, 2762-2790, 2846-2857, 2906-2916), evaluated once
+// per channel with the reference's operation order.
+void ctm_coefficients(double nu, double* out) {
+  const double* B = jgb_continua_blob;
+  for (int i = 0; i < kCtmStride; i++) out[i] = 0;
+  {
+    const double xw = nu / 2 + 1;
+    if (xw >= 1 && xw < 2001) {
+      const int iw = (int)xw;
+      const double dw = xw - iw, ew = 1 - dw;
+      out[0] = 1;
+      out[1] = ew * B[CT_CO2_296 + iw - 1] + dw * B[CT_CO2_296 + iw];
+      out[2] = ew * B[CT_CO2_260 + iw - 1] + dw * B[CT_CO2_260 + iw];
+      out[3] = ew * B[CT_CO2_230 + iw - 1] + dw * B[CT_CO2_230 + iw];
+    }
+  }
+  {
+    const double xw = nu / 10 + 1;
+    if (xw >= 1 && xw < 2001) {
+      const int iw = (int)xw;
+      const double dw = xw - iw, ew = 1 - dw;
+      const double c296 = ew * B[CT_H2O_296 + iw - 1] + dw * B[CT_H2O_296 + iw];
+      const double c260 = ew * B[CT_H2O_260 + iw - 1] + dw * B[CT_H2O_260 + iw];
+      const double cfrn = ew * B[CT_H2O_FRN + iw - 1] + dw * B[CT_H2O_FRN + iw];
+      double sfac = 1;
+      if (!(nu <= 820 || nu >= 960)) {
+        const double xx = (nu - 820) / 10;
+        const int ix = (int)xx;
+        const double dx = xx - ix;
+        sfac = (1 - dx) * B[CT_XFCREV + ix] + dx * B[CT_XFCREV + ix + 1];
+      }
+      const double vf2 = (nu - 370) * (nu - 370), vf6 = vf2 * vf2 * vf2;
+      const double fscal = 36100 / (vf2 + vf6 * 1e-8 + 36100) * -.25 + 1;
+      out[4] = 1;
+      out[5] = sfac * c296;
+      out[6] = c260 / c296;
+      out[7] = cfrn * fscal;
+    }
+  }
+  auto cia = [&](int ob, int obeta, int onu, int n, double* o) {
+    const double* nua = B + onu;
+    if (nu < nua[0] || nu > nua[n - 1]) return;
+    int i = (int)((nu - nua[0]) / (nua[1] - nua[0]));
+    i = i < 0 ? 0 : (i > n - 2 ? n - 2 : i);
+    o[0] = 1;
+    o[1] = lin(nua[i], B[ob + i], nua[i + 1], B[ob + i + 1], nu);
+    o[2] = lin(nua[i], B[obeta + i], nua[i + 1], B[obeta + i + 1], nu);
+  };
+  cia(CT_N2_B, CT_N2_BETA, CT_N2_NU, 98, out + 8);
+  cia(CT_O2_B, CT_O2_BETA, CT_O2_NU, 90, out + 11);
+}
+
+}  // namespace
+
+struct jgb_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  CtlDev c{};
+  std::vector<std::string> emitter;
+  std::vector<double> nu, clnu, sfnu, retq_zmin, retq_zmax, retk_zmin, retk_zmax;
+  std::vector<int> window;
+  double retp_zmin = 0, retp_zmax = 0, rett_zmin = 0, rett_zmax = 0;
+  int ret_flags[7] = {0, 0, 0, 0, 0, 0, 0};
+  // device constants
+  DevBuf d_nu, d_window, d_clnu, d_sfnu, d_ctm;
+  // tables
+  int tp = 0, tt = 0, tu = 0;
+  bool tables_init = false;
+  std::vector<int> h_np;
+  DevBuf t_np, t_p, t_nt, t_t, t_nu, t_u, t_eps, t_pf, t_tf;
+  // source function
+  DevBuf s_st, s_sr, s_srf;
+  std::vector<char> src_set;
+  bool srf_stale = true;
+  // per-call scratch
+  DevBuf b_levoff, b_rayoff, b_rayobs, b_lev, b_scal, b_geo, b_rad, b_tau, b_tp, b_mask, b_p;
+  DevBuf los_off, los_cnt, los_cnt64, los_sft, los_ends, los_planes, scan_tmp, err_word;
+  DevBuf tiles_perm, tiles_keys, tiles_keys2, tiles_vals, tiles_off, tiles_len, tiles_data;
+  DevBuf refl;
+  cudaEvent_t ev[8] = {};
+  jgb_stats stats{};
+  std::string err;
+};
+
+namespace {
+
+int fail(jgb_ctx* x, int code, const std::string& msg) {
+  if (x) x->err = msg;
+  return code;
+}
+
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(x, JGB_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+bool iequal(const std::string& a, const char* b) {
+  if (a.size() != strlen(b)) return false;
+  for (size_t i = 0; i < a.size(); i++)
+    if (std::tolower((unsigned char)a[i]) != std::tolower((unsigned char)b[i])) return false;
+  return true;
+}
+
+TblDev tbl_view(const jgb_ctx* x) {
+  TblDev T;
+  T.tp = x->tp;
+  T.tt = x->tt;
+  T.tu = x->tu;
+  T.np = x->t_np.as<int>();
+  T.p = x->t_p.as<double>();
+  T.nt = x->t_nt.as<int>();
+  T.t = x->t_t.as<double>();
+  T.nu = x->t_nu.as<int>();
+  T.u = x->t_u.as<float>();
+  T.eps = x->t_eps.as<float>();
+  T.pf = x->t_pf.as<float>();
+  T.tf = x->t_tf.as<float>();
+  T.sr = x->s_sr.as<double>();
+  T.srf = x->s_srf.as<float>();
+  T.st = x->s_st.as<double>();
+  return T;
+}
+
+ChanDev chan_view(const jgb_ctx* x) {
+  ChanDev ch;
+  ch.nu = x->d_nu.as<double>();
+  ch.window = x->d_window.as<int>();
+  ch.clnu = x->d_clnu.as<double>();
+  ch.sfnu = x->d_sfnu.as<double>();
+  ch.ctm = x->d_ctm.as<double>();
+  return ch;
+}
+
+__global__ void k_mask(long long n, const double* rad, unsigned char* mask) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) mask[i] = !isfinite(rad[i]);
+}
+
+__global__ void k_ray_obs(int nobs, const int* ray_off, int* ray_obs) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= nobs) return;
+  for (int r = ray_off[o]; r < ray_off[o + 1]; r++) ray_obs[r] = o;
+}
+
+__global__ void k_widen(int n, const int* a, long long* b) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = a[i];
+}
+
+__global__ void k_iota(int n, int* v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = i;
+}
+
+// tile plan from rays sorted by LOS length (descending)
+__global__ void k_tiles(int nray, int ntile, const int* sorted_cnt, const int* sorted_ray,
+                        int* perm, int* tlen, long long* tpts) {
+  const int tile = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tile >= ntile) return;
+  int mx = 0;
+  for (int l = 0; l < 32; l++) {
+    const int k = tile * 32 + l;
+    perm[tile * 32 + l] = k < nray ? sorted_ray[k] : -1;
+    if (k < nray) mx = sorted_cnt[k] > mx ? sorted_cnt[k] : mx;
+  }
+  tlen[tile] = mx;
+  tpts[tile] = mx;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+// Forward model of a device-resident batch (BatchDev pointers on device).
+int run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
+  cudaStream_t s = x->stream;
+  const CtlDev& c = x->c;
+  const int nray = b.nray;
+  CK(x->err_word.reserve(sizeof(unsigned)));
+  unsigned* d_err = x->err_word.as<unsigned>();
+  CK(cudaMemsetAsync(d_err, 0, sizeof(unsigned), s));
+  if (!timed_h2d) CK(cudaEventRecord(x->ev[1], s));
+
+  // hydrostatic equilibrium (rewrites p in place)
+  if (c.hydz >= 0) launch_hydrostatic(c, b, const_cast<double*>(b.p), s);
+  CK(cudaEventRecord(x->ev[2], s));
+
+  // ray tracing: count, scan, fill
+  CK(x->los_cnt.reserve(sizeof(int) * (size_t)std::max(nray, 1)));
+  CK(x->los_cnt64.reserve(sizeof(long long) * (size_t)std::max(nray, 1)));
+  CK(x->los_off.reserve(sizeof(long long) * (size_t)(nray + 1)));
+  CK(x->los_sft.reserve(sizeof(double) * (size_t)std::max(nray, 1)));
+  CK(x->los_ends.reserve(6 * sizeof(double) * (size_t)std::max(nray, 1)));
+  LosDev L{};
+  L.count = x->los_cnt.as<int>();
+  L.off = x->los_off.as<long long>();
+  L.sft = x->los_sft.as<double>();
+  L.ends = x->los_ends.as<double>();
+  L.ng = c.ng;
+  L.nw = c.nw;
+  L.cga = c.formod == 0;
+  ChanDev ch = chan_view(x);
+  launch_trace_count(c, ch, b, L, d_err, s);
+  CK(cudaGetLastError());
+  long long* cnt64 = x->los_cnt64.as<long long>();
+  k_widen<<<(nray + 255) / 256, 256, 0, s>>>(nray, L.count, cnt64);
+  CK(cudaMemsetAsync(L.off, 0, sizeof(long long), s));
+  size_t tmp_bytes = 0;
+  cub::DeviceScan::InclusiveSum(nullptr, tmp_bytes, cnt64, L.off + 1, nray, s);
+  CK(x->scan_tmp.reserve(tmp_bytes + 16));
+  cub::DeviceScan::InclusiveSum(x->scan_tmp.p, tmp_bytes, cnt64, L.off + 1, nray, s);
+  long long total = 0;
+  unsigned h_err = 0;
+  CK(cudaMemcpyAsync(&total, L.off + nray, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&h_err, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (h_err & kErrObserverBelowSurface) return fail(x, JGB_ERR_SURFACE, "Observer below surface!");
+  if (h_err & kErrLosOverflow) return fail(x, JGB_ERR_LOS, "Too many LOS points!");
+  const long long cap = std::max(total, 1LL);
+  const int nplanes = 8 + c.ng + c.nw + (c.formod == 0 ? 3 * c.ng : 0);
+  CK(x->los_planes.reserve(sizeof(double) * (size_t)cap * nplanes));
+  double* P = x->los_planes.as<double>();
+  L.cap = cap;
+  L.z = P + 0 * cap;
+  L.lon = P + 1 * cap;
+  L.lat = P + 2 * cap;
+  L.p = P + 3 * cap;
+  L.t = P + 4 * cap;
+  L.ds = P + 5 * cap;
+  L.aux = P + 6 * cap;
+  L.qh2o = P + 7 * cap;
+  L.u = P + 8 * cap;
+  L.kw = L.u + (long long)c.ng * cap;
+  L.cgp = L.kw + (long long)c.nw * cap;
+  L.cgt = L.cgp + (long long)c.ng * cap;
+  L.cgu = L.cgt + (long long)c.ng * cap;
+  launch_trace_fill(c, ch, b, L, d_err, s);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(x->ev[3], s));
+
+  // reflection needs per-point source and emissivity per channel
+  const bool need_refl = c.sftype >= 2 && c.nsf > 0;
+  TblDev T = tbl_view(x);
+  int launches = 4 + (c.hydz >= 0);
+  if (precision == JGB_FP64) {
+    double* refl = nullptr;
+    if (need_refl) {
+      CK(x->refl.reserve(sizeof(double) * 2 * (size_t)cap * c.nd));
+      refl = x->refl.as<double>();
+    }
+    CK(cudaEventRecord(x->ev[4], s));
+    launch_path_fp64(c, T, ch, b, L, refl, s);
+    launches += 1;
+  } else {
+    if (x->srf_stale) {
+      launch_src_to_float(c.nd, x->s_sr.as<double>(), x->s_srf.as<float>(), s);
+      x->srf_stale = false;
+    }
+    // tile plan: rays sorted by LOS length, 32 per tile
+    const int ntile = (nray + 31) / 32;
+    CK(x->tiles_keys.reserve(sizeof(int) * (size_t)nray));
+    CK(x->tiles_keys2.reserve(sizeof(int) * (size_t)nray));
+    CK(x->tiles_vals.reserve(sizeof(int) * 2 * (size_t)nray));
+    CK(x->tiles_perm.reserve(sizeof(int) * 32 * (size_t)ntile));
+    CK(x->tiles_len.reserve(sizeof(int) * (size_t)ntile));
+    CK(x->tiles_off.reserve(sizeof(long long) * (size_t)(2 * ntile + 2)));
+    int* vals_in = x->tiles_vals.as<int>();
+    int* vals_out = vals_in + nray;
+    k_iota<<<(nray + 255) / 256, 256, 0, s>>>(nray, vals_in);
+    size_t sbytes = 0;
+    cub::DeviceRadixSort::SortPairsDescending(nullptr, sbytes, L.count, x->tiles_keys2.as<int>(),
+                                              vals_in, vals_out, nray, 0, 32, s);
+    CK(x->scan_tmp.reserve(std::max(sbytes, tmp_bytes) + 16));
+    cub::DeviceRadixSort::SortPairsDescending(x->scan_tmp.p, sbytes, L.count,
+                                              x->tiles_keys2.as<int>(), vals_in, vals_out, nray,
+                                              0, 32, s);
+    long long* tpts = x->tiles_off.as<long long>() + ntile + 1;
+    long long* toff = x->tiles_off.as<long long>();
+    MixedPlan Pm{};
+    Pm.ntile = ntile;
+    Pm.perm = x->tiles_perm.as<int>();
+    Pm.tlen = x->tiles_len.as<int>();
+    Pm.toff = toff;
+    k_tiles<<<(ntile + 127) / 128, 128, 0, s>>>(nray, ntile, x->tiles_keys2.as<int>(), vals_out,
+                                                 Pm.perm, Pm.tlen, tpts);
+    CK(cudaMemsetAsync(toff, 0, sizeof(long long), s));
+    size_t sb2 = 0;
+    cub::DeviceScan::InclusiveSum(nullptr, sb2, tpts, toff + 1, ntile, s);
+    CK(x->scan_tmp.reserve(std::max(std::max(sbytes, tmp_bytes), sb2) + 16));
+    cub::DeviceScan::InclusiveSum(x->scan_tmp.p, sb2, tpts, toff + 1, ntile, s);
+    long long tile_points = 0;
+    CK(cudaMemcpyAsync(&tile_points, toff + ntile, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    Pm.nfield = mixed_nfield(c);
+    CK(x->tiles_data.reserve(sizeof(float) * 32 * (size_t)std::max(tile_points, 1LL) * Pm.nfield));
+    Pm.data = x->tiles_data.as<float>();
+    launch_pack_tiles_n(c, L, Pm, tile_points, s);
+    CK(cudaGetLastError());
+    float* refl = nullptr;
+    if (need_refl) {
+      CK(x->refl.reserve(sizeof(float) * 2 * (size_t)cap * c.nd));
+      refl = x->refl.as<float>();
+    }
+    CK(cudaEventRecord(x->ev[4], s));
+    launch_path_mixed(c, T, ch, b, L, Pm, refl, s);
+    launches += 6;
+  }
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(x->ev[5], s));
+  x->stats.los_points = total;
+  x->stats.path_launches = launches;
+  return JGB_OK;
+}
+
+int check_ready(jgb_ctx* x) {
+  if (!x->tables_init) return fail(x, JGB_ERR_STATE, "emissivity tables not set");
+  for (int id = 0; id < x->c.nd; id++)
+    if (!x->src_set[id]) return fail(x, JGB_ERR_STATE, "source function of a channel not set");
+  return JGB_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+
+extern "C" {
+
+int jgb_create(const jgb_ctl* ctl, int device, jgb_ctx** out) {
+  if (!ctl || !out) return JGB_ERR_ARG;
+  *out = nullptr;
+  if (ctl->ng < 0 || ctl->ng > kMaxG || ctl->nd <= 0 || ctl->nw < 0 || ctl->nw > kMaxW ||
+      ctl->ncl < 0 || ctl->ncl == 1 || ctl->nsf < 0 || ctl->nsf == 1)
+    return JGB_ERR_ARG;
+  if (ctl->formod != 0 && ctl->formod != 1) return JGB_ERR_UNSUPPORTED;
+  jgb_ctx* x = new jgb_ctx();
+  x->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete x;
+    return JGB_ERR_CUDA;
+  }
+  for (auto& e : x->ev) cudaEventCreate(&e);
+  CtlDev& c = x->c;
+  c.ng = ctl->ng;
+  c.nd = ctl->nd;
+  c.nw = ctl->nw;
+  c.ncl = ctl->ncl;
+  c.nsf = ctl->nsf;
+  c.sftype = ctl->sftype;
+  c.sfsza = ctl->sfsza;
+  c.hydz = ctl->hydz;
+  c.ctm_co2 = ctl->ctm_co2;
+  c.ctm_h2o = ctl->ctm_h2o;
+  c.ctm_n2 = ctl->ctm_n2;
+  c.ctm_o2 = ctl->ctm_o2;
+  c.refrac = ctl->refrac;
+  c.formod = ctl->formod;
+  c.write_bbt = ctl->write_bbt;
+  c.rayds = ctl->rayds;
+  c.raydz = ctl->raydz;
+  c.nlos_max = ctl->nlos_max > 0 ? ctl->nlos_max : 4096;
+  c.ig_co2 = c.ig_h2o = -1;
+  for (int ig = 0; ig < c.ng; ig++) {
+    x->emitter.push_back(ctl->emitter && ctl->emitter[ig] ? ctl->emitter[ig] : "");
+    if (c.ig_co2 < 0 && iequal(x->emitter.back(), "CO2")) c.ig_co2 = ig;
+    if (c.ig_h2o < 0 && iequal(x->emitter.back(), "H2O")) c.ig_h2o = ig;
+  }
+  x->nu.assign(ctl->nu, ctl->nu + c.nd);
+  x->window.assign(c.nd, 0);
+  if (ctl->window)
+    for (int id = 0; id < c.nd; id++) x->window[id] = ctl->window[id];
+  for (int id = 0; id < c.nd; id++)
+    if (c.nw > 0 && (x->window[id] < 0 || x->window[id] >= c.nw)) {
+      jgb_destroy(x);
+      return JGB_ERR_ARG;
+    }
+  x->clnu.assign(ctl->clnu, ctl->clnu + c.ncl);
+  x->sfnu.assign(ctl->sfnu, ctl->sfnu + c.nsf);
+  x->retp_zmin = ctl->retp_zmin;
+  x->retp_zmax = ctl->retp_zmax;
+  x->rett_zmin = ctl->rett_zmin;
+  x->rett_zmax = ctl->rett_zmax;
+  for (int ig = 0; ig < c.ng; ig++) {
+    x->retq_zmin.push_back(ctl->retq_zmin ? ctl->retq_zmin[ig] : -999);
+    x->retq_zmax.push_back(ctl->retq_zmax ? ctl->retq_zmax[ig] : -999);
+  }
+  for (int iw = 0; iw < c.nw; iw++) {
+    x->retk_zmin.push_back(ctl->retk_zmin ? ctl->retk_zmin[iw] : -999);
+    x->retk_zmax.push_back(ctl->retk_zmax ? ctl->retk_zmax[iw] : -999);
+  }
+  const int rf[7] = {ctl->ret_clz, ctl->ret_cldz, ctl->ret_clk, ctl->ret_sfz,
+                     ctl->ret_sfp, ctl->ret_sft, ctl->ret_sfeps};
+  std::memcpy(x->ret_flags, rf, sizeof(rf));
+  // per-channel constants
+  std::vector<double> ctm((size_t)c.nd * kCtmStride);
+  for (int id = 0; id < c.nd; id++) ctm_coefficients(x->nu[id], &ctm[(size_t)id * kCtmStride]);
+  std::vector<double> st(kNS);
+  for (int it = 0; it < kNS; it++) st[it] = lin(0.0, kTMIN, kNS - 1.0, kTMAX, (double)it);
+  bool ok = x->d_nu.reserve(sizeof(double) * c.nd) == cudaSuccess &&
+            x->d_window.reserve(sizeof(int) * c.nd) == cudaSuccess &&
+            x->d_clnu.reserve(sizeof(double) * (c.ncl + 1)) == cudaSuccess &&
+            x->d_sfnu.reserve(sizeof(double) * (c.nsf + 1)) == cudaSuccess &&
+            x->d_ctm.reserve(sizeof(double) * ctm.size()) == cudaSuccess &&
+            x->s_st.reserve(sizeof(double) * kNS) == cudaSuccess &&
+            x->s_sr.reserve(sizeof(double) * kNS * c.nd) == cudaSuccess &&
+            x->s_srf.reserve(sizeof(float) * kNS * c.nd) == cudaSuccess;
+  ok = ok && cudaMemcpy(x->d_nu.p, x->nu.data(), sizeof(double) * c.nd, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok = ok && cudaMemcpy(x->d_window.p, x->window.data(), sizeof(int) * c.nd, cudaMemcpyHostToDevice) == cudaSuccess;
+  if (c.ncl) ok = ok && cudaMemcpy(x->d_clnu.p, x->clnu.data(), sizeof(double) * c.ncl, cudaMemcpyHostToDevice) == cudaSuccess;
+  if (c.nsf) ok = ok && cudaMemcpy(x->d_sfnu.p, x->sfnu.data(), sizeof(double) * c.nsf, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok = ok && cudaMemcpy(x->d_ctm.p, ctm.data(), sizeof(double) * ctm.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+  ok = ok && cudaMemcpy(x->s_st.p, st.data(), sizeof(double) * kNS, cudaMemcpyHostToDevice) == cudaSuccess;
+  if (!ok) {
+    jgb_destroy(x);
+    return JGB_ERR_CUDA;
+  }
+  x->src_set.assign(c.nd, 0);
+  *out = x;
+  return JGB_OK;
+}
+
+void jgb_destroy(jgb_ctx* x) {
+  if (!x) return;
+  cudaSetDevice(x->device);
+  if (x->stream) cudaStreamSynchronize(x->stream);
+  DevBuf* bufs[] = {&x->d_nu, &x->d_window, &x->d_clnu, &x->d_sfnu, &x->d_ctm, &x->t_np,
+                    &x->t_p, &x->t_nt, &x->t_t, &x->t_nu, &x->t_u, &x->t_eps, &x->t_pf,
+                    &x->t_tf, &x->s_st, &x->s_sr, &x->s_srf, &x->b_levoff, &x->b_rayoff,
+                    &x->b_rayobs, &x->b_lev, &x->b_scal, &x->b_geo, &x->b_rad, &x->b_tau,
+                    &x->b_tp, &x->b_mask, &x->b_p, &x->los_off, &x->los_cnt, &x->los_cnt64,
+                    &x->los_sft, &x->los_ends, &x->los_planes, &x->scan_tmp, &x->err_word,
+                    &x->tiles_perm, &x->tiles_keys, &x->tiles_keys2, &x->tiles_vals,
+                    &x->tiles_off, &x->tiles_len, &x->tiles_data, &x->refl};
+  for (DevBuf* b : bufs) b->release();
+  for (auto& e : x->ev)
+    if (e) cudaEventDestroy(e);
+  if (x->stream) cudaStreamDestroy(x->stream);
+  delete x;
+}
+
+const char* jgb_last_error(const jgb_ctx* x) { return x ? x->err.c_str() : "null context"; }
+
+int jgb_tables_init(jgb_ctx* x, int tp, int tt, int tu) {
+  if (!x || tp < 2 || tt < 2 || tu < 2) return fail(x, JGB_ERR_ARG, "bad table capacities");
+  cudaSetDevice(x->device);
+  const CtlDev& c = x->c;
+  const size_t ndg = (size_t)c.nd * c.ng;
+  x->tp = tp;
+  x->tt = tt;
+  x->tu = tu;
+  x->h_np.assign(ndg, -1);
+  CK(x->t_np.reserve(sizeof(int) * std::max<size_t>(ndg, 1)));
+  CK(x->t_p.reserve(sizeof(double) * std::max<size_t>(ndg * tp, 1)));
+  CK(x->t_nt.reserve(sizeof(int) * std::max<size_t>(ndg * tp, 1)));
+  CK(x->t_t.reserve(sizeof(double) * std::max<size_t>(ndg * tp * tt, 1)));
+  CK(x->t_nu.reserve(sizeof(int) * std::max<size_t>(ndg * tp * tt, 1)));
+  CK(x->t_u.reserve(sizeof(float) * std::max<size_t>(ndg * tp * tt * tu, 1)));
+  CK(x->t_eps.reserve(sizeof(float) * std::max<size_t>(ndg * tp * tt * tu, 1)));
+  CK(x->t_pf.reserve(sizeof(float) * std::max<size_t>(ndg * tp, 1)));
+  CK(x->t_tf.reserve(sizeof(float) * std::max<size_t>(ndg * tp * tt, 1)));
+  CK(cudaMemcpy(x->t_np.p, x->h_np.data(), sizeof(int) * ndg, cudaMemcpyHostToDevice));
+  CK(cudaMemset(x->t_nt.p, 0, sizeof(int) * ndg * tp));
+  CK(cudaMemset(x->t_nu.p, 0, sizeof(int) * ndg * tp * tt));
+  CK(cudaMemset(x->t_p.p, 0, sizeof(double) * ndg * tp));
+  CK(cudaMemset(x->t_t.p, 0, sizeof(double) * ndg * tp * tt));
+  x->tables_init = true;
+  return JGB_OK;
+}
+
+int jgb_set_table(jgb_ctx* x, int id, int ig, int np, const double* p, const int* nt,
+                  const double* t, const int* nu, const float* u, const float* eps, int tt_cap,
+                  int tu_cap) {
+  if (!x || !x->tables_init) return fail(x, JGB_ERR_STATE, "jgb_tables_init not called");
+  const CtlDev& c = x->c;
+  if (id < 0 || id >= c.nd || ig < 0 || ig >= c.ng) return fail(x, JGB_ERR_ARG, "table index");
+  if (np > x->tp) return fail(x, JGB_ERR_ARG, "Too many pressure levels!");
+  cudaSetDevice(x->device);
+  const size_t dg = (size_t)id * c.ng + ig;
+  x->h_np[dg] = np;
+  CK(cudaMemcpy(x->t_np.as<int>() + dg, &np, sizeof(int), cudaMemcpyHostToDevice));
+  if (np <= 0) return JGB_OK;
+  std::vector<int> ntv(x->tp, 0), nuv((size_t)x->tp * x->tt, 0);
+  std::vector<double> pv(x->tp, 0), tv((size_t)x->tp * x->tt, 0);
+  std::vector<float> pf(x->tp, 0), tf((size_t)x->tp * x->tt, 0);
+  for (int ip = 0; ip < np; ip++) {
+    if (nt[ip] > x->tt) return fail(x, JGB_ERR_ARG, "Too many temperatures!");
+    pv[ip] = p[ip];
+    pf[ip] = (float)p[ip];
+    ntv[ip] = nt[ip];
+    for (int it = 0; it < nt[ip]; it++) {
+      const int n = nu[(size_t)ip * tt_cap + it];
+      if (n > x->tu) return fail(x, JGB_ERR_ARG, "Too many column densities!");
+      tv[(size_t)ip * x->tt + it] = t[(size_t)ip * tt_cap + it];
+      tf[(size_t)ip * x->tt + it] = (float)t[(size_t)ip * tt_cap + it];
+      nuv[(size_t)ip * x->tt + it] = n;
+    }
+  }
+  CK(cudaMemcpy(x->t_p.as<double>() + dg * x->tp, pv.data(), sizeof(double) * x->tp, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(x->t_pf.as<float>() + dg * x->tp, pf.data(), sizeof(float) * x->tp, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(x->t_nt.as<int>() + dg * x->tp, ntv.data(), sizeof(int) * x->tp, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(x->t_t.as<double>() + dg * x->tp * x->tt, tv.data(), sizeof(double) * x->tp * x->tt, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(x->t_tf.as<float>() + dg * x->tp * x->tt, tf.data(), sizeof(float) * x->tp * x->tt, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(x->t_nu.as<int>() + dg * x->tp * x->tt, nuv.data(), sizeof(int) * x->tp * x->tt, cudaMemcpyHostToDevice));
+  // rows: (ip, it) -> device row of tu floats; source rows have pitch tu_cap
+  const size_t rows = (size_t)x->tp * x->tt;
+  float* du = x->t_u.as<float>() + dg * rows * x->tu;
+  float* de = x->t_eps.as<float>() + dg * rows * x->tu;
+  for (int ip = 0; ip < np; ip++) {
+    const int ntt = nt[ip];
+    const size_t w = std::min(tu_cap, x->tu);
+    CK(cudaMemcpy2D(du + (size_t)ip * x->tt * x->tu, sizeof(float) * x->tu,
+                    u + (size_t)ip * tt_cap * tu_cap, sizeof(float) * tu_cap, sizeof(float) * w,
+                    ntt, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy2D(de + (size_t)ip * x->tt * x->tu, sizeof(float) * x->tu,
+                    eps + (size_t)ip * tt_cap * tu_cap, sizeof(float) * tu_cap,
+                    sizeof(float) * w, ntt, cudaMemcpyHostToDevice));
+  }
+  return JGB_OK;
+}
+
+int jgb_set_filter(jgb_ctx* x, int id, int n, const double* fnu, const double* f) {
+  if (!x || id < 0 || id >= x->c.nd || n < 2 || !fnu || !f)
+    return fail(x, JGB_ERR_ARG, "bad filter function");
+  cudaSetDevice(x->device);
+  DevBuf tmp;
+  const size_t bytes = sizeof(double) * 2 * n + 2 * sizeof(int) + 16;
+  CK(tmp.reserve(bytes));
+  double* dx = tmp.as<double>();
+  double* dy = dx + n;
+  int* off = reinterpret_cast<int*>(dy + n);
+  const int hoff[2] = {0, n};
+  CK(cudaMemcpy(dx, fnu, sizeof(double) * n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(dy, f, sizeof(double) * n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(off, hoff, sizeof(hoff), cudaMemcpyHostToDevice));
+  launch_srcfunc(x->c.nd, id, 1, off, dx, dy, x->s_st.as<double>(), x->s_sr.as<double>(), x->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(x->stream));
+  tmp.release();
+  x->src_set[id] = 1;
+  x->srf_stale = true;
+  return JGB_OK;
+}
+
+int jgb_set_srcfunc(jgb_ctx* x, const double* sr) {
+  if (!x || !sr) return fail(x, JGB_ERR_ARG, "null source function");
+  cudaSetDevice(x->device);
+  CK(cudaMemcpy(x->s_sr.p, sr, sizeof(double) * kNS * x->c.nd, cudaMemcpyHostToDevice));
+  std::fill(x->src_set.begin(), x->src_set.end(), 1);
+  x->srf_stale = true;
+  return JGB_OK;
+}
+
+int jgb_get_srcfunc(jgb_ctx* x, double* st, double* sr) {
+  if (!x) return JGB_ERR_ARG;
+  cudaSetDevice(x->device);
+  if (st) CK(cudaMemcpy(st, x->s_st.p, sizeof(double) * kNS, cudaMemcpyDeviceToHost));
+  if (sr) CK(cudaMemcpy(sr, x->s_sr.p, sizeof(double) * kNS * x->c.nd, cudaMemcpyDeviceToHost));
+  return JGB_OK;
+}
+
+int jgb_formod_batch(jgb_ctx* x, const jgb_batch* hb, int precision) {
+  if (!x || !hb || hb->nobs <= 0) return fail(x, JGB_ERR_ARG, "empty batch");
+  if (precision != JGB_FP64 && precision != JGB_MIXED) return fail(x, JGB_ERR_ARG, "precision");
+  int rc = check_ready(x);
+  if (rc) return rc;
+  cudaSetDevice(x->device);
+  const CtlDev& c = x->c;
+  cudaStream_t s = x->stream;
+  const int nobs = hb->nobs;
+  const int nlev = hb->lev_off[nobs], nray = hb->ray_off[nobs];
+  if (nlev <= 0 || nray <= 0) return fail(x, JGB_ERR_ARG, "no levels or rays");
+  for (int o = 0; o < nobs; o++)
+    if (hb->lev_off[o + 1] - hb->lev_off[o] < 2)
+      return fail(x, JGB_ERR_ARG, "an atmosphere needs at least two levels");
+  const int nscal = 5 + c.ncl + c.nsf;
+  const int nlevf = 6 + c.ng + c.nw;  // time z lon lat p t q[] k[]
+  CK(x->b_levoff.reserve(sizeof(int) * (nobs + 1)));
+  CK(x->b_rayoff.reserve(sizeof(int) * (nobs + 1)));
+  CK(x->b_rayobs.reserve(sizeof(int) * nray));
+  CK(x->b_lev.reserve(sizeof(double) * (size_t)nlev * nlevf));
+  CK(x->b_scal.reserve(sizeof(double) * (size_t)nobs * nscal));
+  CK(x->b_geo.reserve(sizeof(double) * 7 * (size_t)nray));
+  CK(x->b_rad.reserve(sizeof(double) * (size_t)c.nd * nray));
+  CK(x->b_tau.reserve(sizeof(double) * (size_t)c.nd * nray));
+  CK(x->b_tp.reserve(sizeof(double) * 3 * (size_t)nray));
+  CK(x->b_mask.reserve((size_t)c.nd * nray));
+  double* lev = x->b_lev.as<double>();
+  BatchDev b{};
+  b.nobs = nobs;
+  b.nlev = nlev;
+  b.nray = nray;
+  b.nscal = nscal;
+  b.lev_off = x->b_levoff.as<int>();
+  b.ray_obs = x->b_rayobs.as<int>();
+  b.time = lev;
+  b.z = lev + (size_t)nlev;
+  b.lon = lev + 2 * (size_t)nlev;
+  b.lat = lev + 3 * (size_t)nlev;
+  b.p = lev + 4 * (size_t)nlev;
+  b.t = lev + 5 * (size_t)nlev;
+  b.q = lev + 6 * (size_t)nlev;
+  b.k = lev + (6 + (size_t)c.ng) * nlev;
+  b.scal = x->b_scal.as<double>();
+  b.geo = x->b_geo.as<double>();
+  b.rad = x->b_rad.as<double>();
+  b.tau = x->b_tau.as<double>();
+  b.tp = x->b_tp.as<double>();
+  b.mask = x->b_mask.as<unsigned char>();
+  CK(cudaEventRecord(x->ev[0], s));
+  const size_t L = (size_t)nlev * sizeof(double);
+  CK(cudaMemcpyAsync(x->b_levoff.p, hb->lev_off, sizeof(int) * (nobs + 1), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(x->b_rayoff.p, hb->ray_off, sizeof(int) * (nobs + 1), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync((void*)b.time, hb->time, L, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync((void*)b.z, hb->z, L, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync((void*)b.lon, hb->lon, L, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync((void*)b.lat, hb->lat, L, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync((void*)b.p, hb->p, L, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync((void*)b.t, hb->t, L, cudaMemcpyHostToDevice, s));
+  if (c.ng) CK(cudaMemcpyAsync((void*)b.q, hb->q, L * c.ng, cudaMemcpyHostToDevice, s));
+  if (c.nw) CK(cudaMemcpyAsync((void*)b.k, hb->k, L * c.nw, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync((void*)b.scal, hb->scal, sizeof(double) * (size_t)nobs * nscal, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync((void*)b.geo, hb->geo, sizeof(double) * 7 * (size_t)nray, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b.rad, hb->rad, sizeof(double) * (size_t)c.nd * nray, cudaMemcpyHostToDevice, s));
+  k_ray_obs<<<(nobs + 127) / 128, 128, 0, s>>>(nobs, x->b_rayoff.as<int>(), x->b_rayobs.as<int>());
+  const long long nm = (long long)c.nd * nray;
+  k_mask<<<(unsigned)((nm + 255) / 256), 256, 0, s>>>(nm, b.rad, x->b_mask.as<unsigned char>());
+  CK(cudaEventRecord(x->ev[1], s));
+  rc = run_core(x, b, precision, true);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(hb->rad, b.rad, sizeof(double) * (size_t)c.nd * nray, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(hb->tau, b.tau, sizeof(double) * (size_t)c.nd * nray, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(hb->tp, b.tp, sizeof(double) * 3 * (size_t)nray, cudaMemcpyDeviceToHost, s));
+  if (c.hydz >= 0) CK(cudaMemcpyAsync(hb->p, b.p, L, cudaMemcpyDeviceToHost, s));
+  CK(cudaEventRecord(x->ev[6], s));
+  CK(cudaStreamSynchronize(s));
+  x->stats.h2d_ms = elapsed(x->ev[0], x->ev[1]);
+  x->stats.hydro_ms = elapsed(x->ev[1], x->ev[2]);
+  x->stats.trace_ms = elapsed(x->ev[2], x->ev[3]);
+  x->stats.pack_ms = elapsed(x->ev[3], x->ev[4]);
+  x->stats.path_ms = elapsed(x->ev[4], x->ev[5]);
+  x->stats.d2h_ms = elapsed(x->ev[5], x->ev[6]);
+  x->stats.total_ms = elapsed(x->ev[0], x->ev[6]);
+  return JGB_OK;
+}
+
+int jgb_formod_batch_dev(jgb_ctx* x, const jgb_batch* db, int precision) {
+  if (!x || !db || db->nobs <= 0) return fail(x, JGB_ERR_ARG, "empty batch");
+  if (precision != JGB_FP64 && precision != JGB_MIXED) return fail(x, JGB_ERR_ARG, "precision");
+  int rc = check_ready(x);
+  if (rc) return rc;
+  cudaSetDevice(x->device);
+  const CtlDev& c = x->c;
+  cudaStream_t s = x->stream;
+  const int nobs = db->nobs;
+  int nlev = 0, nray = 0;
+  CK(cudaMemcpy(&nlev, db->lev_off + nobs, sizeof(int), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(&nray, db->ray_off + nobs, sizeof(int), cudaMemcpyDeviceToHost));
+  if (nlev <= 0 || nray <= 0) return fail(x, JGB_ERR_ARG, "no levels or rays");
+  CK(x->b_rayobs.reserve(sizeof(int) * nray));
+  CK(x->b_mask.reserve((size_t)c.nd * nray));
+  BatchDev b{};
+  b.nobs = nobs;
+  b.nlev = nlev;
+  b.nray = nray;
+  b.nscal = 5 + c.ncl + c.nsf;
+  b.lev_off = db->lev_off;
+  b.ray_obs = x->b_rayobs.as<int>();
+  b.time = db->time;
+  b.z = db->z;
+  b.lon = db->lon;
+  b.lat = db->lat;
+  b.p = db->p;
+  b.t = db->t;
+  b.q = db->q;
+  b.k = db->k;
+  b.scal = db->scal;
+  b.geo = db->geo;
+  b.rad = db->rad;
+  b.tau = db->tau;
+  b.tp = db->tp;
+  b.mask = x->b_mask.as<unsigned char>();
+  CK(cudaEventRecord(x->ev[0], s));
+  k_ray_obs<<<(nobs + 127) / 128, 128, 0, s>>>(nobs, db->ray_off, x->b_rayobs.as<int>());
+  const long long nm = (long long)c.nd * nray;
+  k_mask<<<(unsigned)((nm + 255) / 256), 256, 0, s>>>(nm, b.rad, x->b_mask.as<unsigned char>());
+  rc = run_core(x, b, precision, false);
+  if (rc) return rc;
+  CK(cudaEventRecord(x->ev[6], s));
+  CK(cudaStreamSynchronize(s));
+  x->stats.h2d_ms = 0;
+  x->stats.hydro_ms = elapsed(x->ev[1], x->ev[2]);
+  x->stats.trace_ms = elapsed(x->ev[2], x->ev[3]);
+  x->stats.pack_ms = elapsed(x->ev[3], x->ev[4]);
+  x->stats.path_ms = elapsed(x->ev[4], x->ev[5]);
+  x->stats.d2h_ms = 0;
+  x->stats.total_ms = elapsed(x->ev[0], x->ev[6]);
+  return JGB_OK;
+}
+
+int jgb_formod(jgb_ctx* x, int np, const double* time, const double* z, const double* lon,
+               const double* lat, double* p, const double* t, const double* q, const double* k,
+               const double* scal, int nr, const double* geo, double* rad, double* tau,
+               double* tp, int precision) {
+  const int lev_off[2] = {0, np};
+  const int ray_off[2] = {0, nr};
+  jgb_batch b{};
+  b.nobs = 1;
+  b.lev_off = lev_off;
+  b.time = time;
+  b.z = z;
+  b.lon = lon;
+  b.lat = lat;
+  b.p = p;
+  b.t = t;
+  b.q = q;
+  b.k = k;
+  b.scal = scal;
+  b.ray_off = ray_off;
+  b.geo = geo;
+  b.rad = rad;
+  b.tau = tau;
+  b.tp = tp;
+  return jgb_formod_batch(x, &b, precision);
+}
+
+int jgb_get_stats(const jgb_ctx* x, jgb_stats* out) {
+  if (!x || !out) return JGB_ERR_ARG;
+  *out = x->stats;
+  return JGB_OK;
+}
+
+void* jgb_host_alloc(unsigned long long bytes) {
+  void* p = nullptr;
+  if (cudaHostAlloc(&p, bytes, cudaHostAllocDefault) != cudaSuccess) return nullptr;
+  return p;
+}
+
+void jgb_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
+void* jgb_dev_alloc(unsigned long long bytes) {
+  void* p = nullptr;
+  if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+  return p;
+}
+
+void jgb_dev_free(void* p) {
+  if (p) cudaFree(p);
+}
+
+int jgb_memcpy_h2d(void* dst, const void* src, unsigned long long bytes) {
+  return cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess ? JGB_OK : JGB_ERR_CUDA;
+}
+
+int jgb_memcpy_d2h(void* dst, const void* src, unsigned long long bytes) {
+  return cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost) == cudaSuccess ? JGB_OK : JGB_ERR_CUDA;
+}
+
+}  // extern "C"

@@ -1,0 +1,39 @@
+// Launch wrappers shared between the translation units of libjurassic_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "jgb_common.cuh"
+
+namespace jgb {
+
+// jgb_fp64.cu
+void launch_trace_count(const CtlDev& c, const ChanDev& ch, const BatchDev& b, const LosDev& L,
+                        unsigned* err, cudaStream_t s);
+void launch_trace_fill(const CtlDev& c, const ChanDev& ch, const BatchDev& b, const LosDev& L,
+                       unsigned* err, cudaStream_t s);
+void launch_path_fp64(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
+                      const LosDev& L, double* refl_scratch, cudaStream_t s);
+void launch_srcfunc(int nd, int id0, int nch, const int* fn_off, const double* fnu,
+                    const double* f, const double* st, double* sr, cudaStream_t s);
+void launch_hydrostatic(const CtlDev& c, const BatchDev& b, double* p_out, cudaStream_t s);
+
+// jgb_mixed.cu
+struct MixedPlan {
+  int ntile;
+  int* perm;            // [ntile*32]
+  long long* toff;      // [ntile+1]
+  int* tlen;            // [ntile]
+  float* data;          // tile planes
+  int nfield;
+};
+int mixed_nfield(const CtlDev& c);
+void launch_pack_tiles_n(const CtlDev& c, const LosDev& L, const MixedPlan& P,
+                         long long total_tile_points, cudaStream_t s);
+void launch_path_mixed(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
+                       const LosDev& L, const MixedPlan& P, float* refl_scratch,
+                       cudaStream_t s);
+void launch_src_to_float(int nd, const double* sr, float* srf, cudaStream_t s);
+void launch_tables_to_float(long long n, const double* src, float* dst, cudaStream_t s);
+
+}  // namespace jgb

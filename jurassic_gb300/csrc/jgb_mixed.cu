@@ -1,0 +1,433 @@
+// Mixed-precision forward model: FP32 path loop with compensated sums.
+//
+// Work decomposition: rays are sorted by LOS length and grouped into tiles
+// of 32 (one ray per lane); a warp walks one tile for one channel, so all
+// lanes of a warp read the same emissivity table (same channel, emitter)
+// at neighbouring rows and the same LOS plane entries (one 128-byte line
+// per field and point).  A block holds 4 warps = 4 channels of one tile,
+// which share the tile's LOS data through L1.
+//
+// Numerics (same algorithm as intpol_tbl_ega/cga, jurassic.c:3710-3891, and
+// formod_pencil, 3196-3338):
+//  * each (channel, emitter) carries its path transmittance t and path
+//    emissivity e = 1 - t as two floats, each accurate where it is small,
+//    so that neither 1 - t nor 1 - e is ever formed from a rounded value;
+//  * segment emissivities are combined as E <- E + (1 - E) eps_g (no
+//    cancellation for small eps), the continuum as -expm1(-beta ds);
+//  * the radiance sum is Kahan-compensated.
+#include "jgb_common.cuh"
+#include "jgb_internal.h"
+
+namespace jgb {
+
+// Field indices of a tile plane.
+struct Fields {
+  int p, t, ds, qh2o, aux, kw0, u0, cgp0, cgt0, cgu0, n;
+};
+
+__host__ __device__ inline Fields fields_of(const CtlDev& c) {
+  Fields f;
+  f.p = 0;
+  f.t = 1;
+  f.ds = 2;
+  f.qh2o = 3;
+  f.aux = 4;
+  f.kw0 = 5;
+  f.u0 = 5 + c.nw;
+  f.cgp0 = f.u0 + c.ng;
+  f.cgt0 = f.cgp0 + c.ng;
+  f.cgu0 = f.cgt0 + c.ng;
+  f.n = c.formod == 0 ? f.cgu0 + c.ng : f.u0 + c.ng;
+  return f;
+}
+
+int mixed_nfield(const CtlDev& c) { return fields_of(c).n; }
+
+// One thread per (tile, point, lane) converts the FP64 LOS to float tiles.
+__global__ void k_pack_tiles(CtlDev c, LosDev L, MixedPlan P, long long total) {
+  const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total * 32) return;
+  const int lane = (int)(gid & 31);
+  const long long tp = gid >> 5;  // tile-point
+  // locate the tile by binary search over tile offsets
+  int lo = 0, hi = P.ntile;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (P.toff[mid] <= tp) lo = mid; else hi = mid;
+  }
+  const int tile = lo;
+  const int ip = (int)(tp - P.toff[tile]);
+  const int r = P.perm[tile * 32 + lane];
+  const Fields F = fields_of(c);
+  float* out = P.data + tp * (long long)F.n * 32 + lane;
+  if (r < 0 || ip >= L.count[r]) {
+    for (int f = 0; f < F.n; f++) out[f * 32] = 0.f;
+    return;
+  }
+  const long long q = L.off[r] + ip;
+  out[F.p * 32] = (float)L.p[q];
+  out[F.t * 32] = (float)L.t[q];
+  out[F.ds * 32] = (float)L.ds[q];
+  out[F.qh2o * 32] = c.ig_h2o >= 0 ? (float)L.qh2o[q] : 0.f;
+  out[F.aux * 32] = (float)L.aux[q];
+  for (int w = 0; w < c.nw; w++) out[(F.kw0 + w) * 32] = (float)L.kw[w * L.cap + q];
+  for (int g = 0; g < c.ng; g++) out[(F.u0 + g) * 32] = (float)L.u[g * L.cap + q];
+  if (c.formod == 0)
+    for (int g = 0; g < c.ng; g++) {
+      out[(F.cgp0 + g) * 32] = (float)L.cgp[g * L.cap + q];
+      out[(F.cgt0 + g) * 32] = (float)L.cgt[g * L.cap + q];
+      out[(F.cgu0 + g) * 32] = (float)L.cgu[g * L.cap + q];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// float table access
+
+struct RowF {
+  const float* u;
+  const float* e;
+  int n;
+};
+
+__device__ __forceinline__ RowF rowf_at(const TblDev& T, long long dg, int ip, int it) {
+  const long long r = (dg * T.tp + ip) * T.tt + it;
+  RowF w;
+  w.u = T.u + r * T.tu;
+  w.e = T.eps + r * T.tu;
+  w.n = __ldg(T.nu + r);
+  return w;
+}
+
+__device__ __forceinline__ int bracket_rowf(const float* g, int n, float x) {
+  int lo = 0, hi = n - 1;
+  while (hi > lo + 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(g + mid) > x) hi = mid; else lo = mid;
+  }
+  return lo;
+}
+
+// Emissivity at column u (intpol_tbl_eps) in float.
+__device__ __forceinline__ float rowf_eps(const RowF& r, float u) {
+  const float u0 = __ldg(r.u), un = __ldg(r.u + r.n - 1);
+  if (u < u0) return __ldg(r.e) / u0 * u;
+  if (u > un) {
+    const float a = log1pf(-__ldg(r.e + r.n - 1)) / un;
+    return -expm1f(a * u);
+  }
+  const int i = bracket_rowf(r.u, r.n, u);
+  const float xa = __ldg(r.u + i), xb = __ldg(r.u + i + 1);
+  const float ya = __ldg(r.e + i), yb = __ldg(r.e + i + 1);
+  return ya + (yb - ya) / (xb - xa) * (u - xa);
+}
+
+// Column at emissivity e (intpol_tbl_u) in float.
+__device__ __forceinline__ float rowf_u(const RowF& r, float e) {
+  const float e0 = __ldg(r.e), en = __ldg(r.e + r.n - 1);
+  if (e < e0) return __ldg(r.u) / e0 * e;
+  if (e > en) {
+    const float a = log1pf(-en) / __ldg(r.u + r.n - 1);
+    return log1pf(-e) / a;
+  }
+  const int i = bracket_rowf(r.e, r.n, e);
+  const float xa = __ldg(r.e + i), xb = __ldg(r.e + i + 1);
+  const float ya = __ldg(r.u + i), yb = __ldg(r.u + i + 1);
+  return ya + (yb - ya) / (xb - xa) * (e - xa);
+}
+
+__device__ __forceinline__ int bracket_regf(const float* g, int n, float x) {
+  const float g0 = __ldg(g), g1 = __ldg(g + 1);
+  const int i = (int)((x - g0) / (g1 - g0));
+  return i < 0 ? 0 : (i > n - 2 ? n - 2 : i);
+}
+
+__device__ __forceinline__ int bracket_irrf(const float* g, int n, float x) {
+  int lo = 0, hi = n - 1, mid = (lo + hi) >> 1;
+  const bool up = __ldg(g + mid) < __ldg(g + mid + 1);
+  while (hi > lo + 1) {
+    mid = (lo + hi) >> 1;
+    const float v = __ldg(g + mid);
+    const bool go_low = up ? (v > x) : (v <= x);
+    if (go_low) hi = mid; else lo = mid;
+  }
+  return lo;
+}
+
+// Path state of one (channel, emitter): transmittance t and emissivity e.
+struct GasState {
+  float t, e;
+};
+
+// One (channel, emitter) at one LOS point.  Returns the segment emissivity
+// and updates the path state; *sat is set where the reference's segment
+// transmittance becomes zero (emissivity exactly one).
+__device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, bool cga, float pq,
+                                           float tq, float du, float ucg, GasState& s,
+                                           bool& sat) {
+  const int np = __ldg(T.np + dg);
+  if (np < 30) return 0.f;
+  if (s.t < 1e-9f) {
+    s.t = 0.f;
+    s.e = 1.f;
+    sat = true;
+    return 1.f;
+  }
+  const float* pg = T.pf + dg * T.tp;
+  const int* ntg = T.nt + dg * T.tp;
+  const int ipr = bracket_irrf(pg, np, pq);
+  const int nt0 = __ldg(ntg + ipr), nt1 = __ldg(ntg + ipr + 1);
+  if (nt0 < 2 || nt1 < 2) return 0.f;
+  const float* t0g = T.tf + (dg * T.tp + ipr) * T.tt;
+  const float* t1g = t0g + T.tt;
+  const int it0 = bracket_regf(t0g, nt0, tq);
+  const int it1 = bracket_regf(t1g, nt1, tq);
+  const RowF r00 = rowf_at(T, dg, ipr, it0), r01 = rowf_at(T, dg, ipr, it0 + 1);
+  const RowF r10 = rowf_at(T, dg, ipr + 1, it1), r11 = rowf_at(T, dg, ipr + 1, it1 + 1);
+  if (r00.n < 2 || r01.n < 2 || r10.n < 2 || r11.n < 2) return 0.f;
+  float e00, e01, e10, e11;
+  if (cga) {
+    e00 = rowf_eps(r00, ucg);
+    e01 = rowf_eps(r01, ucg);
+    e10 = rowf_eps(r10, ucg);
+    e11 = rowf_eps(r11, ucg);
+  } else {
+    e00 = rowf_eps(r00, rowf_u(r00, s.e) + du);
+    e01 = rowf_eps(r01, rowf_u(r01, s.e) + du);
+    e10 = rowf_eps(r10, rowf_u(r10, s.e) + du);
+    e11 = rowf_eps(r11, rowf_u(r11, s.e) + du);
+  }
+  const float ta = __ldg(t0g + it0), tb = __ldg(t0g + it0 + 1);
+  const float tc = __ldg(t1g + it1), td = __ldg(t1g + it1 + 1);
+  const float ea = e00 + (e01 - e00) / (tb - ta) * (tq - ta);
+  const float eb = e10 + (e11 - e10) / (td - tc) * (tq - tc);
+  const float pa = __ldg(pg + ipr), pb = __ldg(pg + ipr + 1);
+  float w;
+  if (cga && pq / pa > 0.f && pb / pa > 0.f)
+    w = __logf(pq / pa) / __logf(pb / pa);
+  else
+    w = (pq - pa) / (pb - pa);
+  float e = ea + (eb - ea) * w;
+  e = fminf(fmaxf(e, 0.f), 1.f);
+  // transmittance of the extended path; 1 - e is exact for e >= 0.5
+  const float te = 1.f - e;
+  float eps;
+  if (s.e < 0.5f)
+    eps = (e - s.e) / s.t;
+  else
+    eps = 1.f - te / s.t;
+  if (e >= 1.f) sat = true;
+  s.t = te;
+  s.e = e;
+  return eps;
+}
+
+__global__ void __launch_bounds__(128) k_path_mixed(CtlDev c, TblDev T, ChanDev ch, BatchDev b,
+                                                    LosDev L, MixedPlan P, float* refl) {
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int nchb = (c.nd + 3) / 4;
+  const int tile = blockIdx.x / nchb;
+  const int id = (blockIdx.x % nchb) * 4 + warp;
+  if (tile >= P.ntile || id >= c.nd) return;
+  const int r = P.perm[tile * 32 + lane];
+  const int n = r >= 0 ? L.count[r] : 0;
+  const Fields F = fields_of(c);
+  const float* base = P.data + P.toff[tile] * (long long)F.n * 32 + lane;
+  const bool cga = c.formod == 0;
+  const double nud = ch.nu[id];
+  const float nu = (float)nud;
+
+  // per-(observation, channel) constants
+  float cloud = 0.f, sfeps = 1.f;
+  bool has_cloud = false;
+  if (r >= 0) {
+    const double* s = b.scal + (long long)b.ray_obs[r] * b.nscal;
+    has_cloud = c.ncl > 0 && s[1] > 0;
+    if (has_cloud) {
+      const int icl = bracket_irr(ch.clnu, c.ncl, nud);
+      cloud = (float)lin(ch.clnu[icl], s[2 + icl], ch.clnu[icl + 1], s[2 + icl + 1], nud);
+    }
+    if (c.nsf > 0) {
+      const double* se = s + 5 + c.ncl;
+      const int isf = bracket_irr(ch.sfnu, c.nsf, nud);
+      sfeps = (float)lin(ch.sfnu[isf], se[isf], ch.sfnu[isf + 1], se[isf + 1], nud);
+    }
+  }
+  const int w = c.nw > 0 ? ch.window[id] : 0;
+  const double* cc = ch.ctm + (long long)id * kCtmStride;
+  const bool co2_on = c.ctm_co2 && c.ig_co2 >= 0 && cc[0] != 0;
+  const bool h2o_on = c.ctm_h2o && c.ig_h2o >= 0 && cc[4] != 0;
+  const bool n2_on = c.ctm_n2 && cc[8] != 0;
+  const bool o2_on = c.ctm_o2 && cc[11] != 0;
+  const float co2_296 = (float)cc[1], co2_260 = (float)cc[2], co2_230 = (float)cc[3];
+  const float h2o_s296 = (float)cc[5], h2o_lr = (float)log(cc[6] > 0 ? cc[6] : 1.0);
+  const float h2o_frn = (float)cc[7];
+  const float n2_b = (float)cc[9], n2_beta = (float)cc[10];
+  const float o2_b = (float)cc[12], o2_beta = (float)cc[13];
+  const float* srf = T.srf + (long long)id * kNS;
+  const float st0 = (float)kTMIN, sdt = (float)((kTMAX - kTMIN) / (kNS - 1.0));
+
+  GasState gs[kMaxG];
+  for (int g = 0; g < c.ng; g++) gs[g] = GasState{1.f, 0.f};
+  float rad = 0.f, comp = 0.f, tau = 1.f;
+  const bool do_refl = refl != nullptr && r >= 0 && c.sftype >= 2 && sfeps < 1.f && L.sft[r] > 0;
+  float* sc = do_refl ? refl + 2 * (L.off[r] * c.nd) : nullptr;
+
+  const int len = P.tlen[tile];
+  for (int ip = 0; ip < len; ip++) {
+    if (ip >= n) break;
+    const float* f = base + (long long)ip * F.n * 32;
+    const float p = f[F.p * 32], t = f[F.t * 32], ds = f[F.ds * 32];
+    float E = 0.f;
+    bool sat = false;
+    for (int g = 0; g < c.ng; g++) {
+      const long long dg = (long long)id * c.ng + g;
+      const float du = cga ? 0.f : f[(F.u0 + g) * 32];
+      const float pq = cga ? f[(F.cgp0 + g) * 32] : p;
+      const float tq = cga ? f[(F.cgt0 + g) * 32] : t;
+      const float ucg = cga ? f[(F.cgu0 + g) * 32] : 0.f;
+      const float eg = gas_eps_f(T, dg, cga, pq, tq, du, ucg, gs[g], sat);
+      E = E + (1.f - E) * eg;
+    }
+    // extinction and continua
+    float beta = c.nw > 0 ? f[(F.kw0 + w) * 32] : 0.f;
+    if (has_cloud) beta += f[F.aux * 32] * cloud;
+    const float pr = p / (float)kP0;
+    if (co2_on) {
+      const float d230 = t - 230.f, d260 = t - 260.f, d296 = t - 296.f;
+      const float ctw = d260 * 5.050505e-4f * d296 * co2_230 - d230 * 9.259259e-4f * d296 * co2_260 +
+                        d230 * 4.208754e-4f * d260 * co2_296;
+      const float uco2 = f[(F.u0 + c.ig_co2) * 32];
+      beta += (uco2 / ds) * (float)(1.0 / (kNA * 1000.0)) * pr * ctw;
+    }
+    if (h2o_on) {
+      const float q = f[F.qh2o * 32];
+      const float uh = f[(F.u0 + c.ig_h2o) * 32];
+      const float self = h2o_s296 * __expf(h2o_lr * (296.f - t) * (1.f / 36.f));
+      const float a1 = nu * ((uh / ds) * 1e-20f) * tanhf(.7193876f / t * nu);
+      beta += a1 * (296.f / t) * pr * (q * self + (1.f - q) * h2o_frn);
+    }
+    if (n2_on || o2_on) {
+      const float x = pr * 273.f / t;
+      const float x2 = 0.1f * x * x;
+      if (n2_on)
+        beta += x2 * __expf(n2_beta * (1.f / 296.f - 1.f / t)) * 0.79f * n2_b *
+                (0.79f + 0.21f * (1.294f - 0.4545f * t / 296.f));
+      if (o2_on) beta += x2 * __expf(o2_beta * (1.f / 296.f - 1.f / t)) * 0.21f * o2_b;
+    }
+    // source function (formod_srcfunc)
+    const float xs = (t - st0) / sdt;
+    int is = (int)xs;
+    is = is < 0 ? 0 : (is > kNS - 2 ? kNS - 2 : is);
+    const float s0 = __ldg(srf + is), s1 = __ldg(srf + is + 1);
+    const float src = s0 + (s1 - s0) * (xs - (float)is);
+    float eps = 0.f;
+    if (!sat) {
+      eps = E + (1.f - E) * (-expm1f(-beta * ds));
+      // Kahan-compensated radiance sum
+      const float y = src * eps * tau - comp;
+      const float tsum = rad + y;
+      comp = (tsum - rad) - y;
+      rad = tsum;
+      tau *= (1.f - eps);
+    }
+    if (sc) {
+      sc[2 * ((long long)ip * c.nd + id)] = src;
+      sc[2 * ((long long)ip * c.nd + id) + 1] = eps;
+    }
+  }
+  if (r < 0) return;
+
+  double radd = (double)rad;
+  const double sft = L.sft[r];
+  if (c.sftype >= 1 && sft > 0) {
+    const float xs = ((float)sft - st0) / sdt;
+    int is = (int)xs;
+    is = is < 0 ? 0 : (is > kNS - 2 ? kNS - 2 : is);
+    const float s0 = srf[is], s1 = srf[is + 1];
+    const float ssf = s0 + (s1 - s0) * (xs - (float)is);
+    radd += (double)(sfeps * ssf * tau);
+    if (do_refl) {
+      float tr = 1.f;
+      double acc = 0;
+      for (int ip = n - 1; ip >= 0; ip--) {
+        const float src = sc[2 * ((long long)ip * c.nd + id)];
+        const float e = sc[2 * ((long long)ip * c.nd + id) + 1];
+        acc += (double)(src * e * tr);
+        tr *= (1.f - e);
+      }
+      radd += acc * (double)tau * (double)(1.f - sfeps);
+      if (c.sftype >= 3) {
+        const double* e6 = L.ends + 6LL * r;
+        // solar zenith angle and incidence (double, once per ray and channel)
+        const double d = b.geo[r] / 86400 - 0.5;
+        const double g = (357.529 + 0.98560028 * d) * (kPI / 180.0);
+        const double qq = 280.459 + 0.98564736 * d;
+        const double l = (qq + 1.915 * sin(g) + 0.020 * sin(2 * g)) * (kPI / 180.0);
+        const double ee = (23.439 - 0.00000036 * d) * (kPI / 180.0);
+        const double dec = asin(sin(ee) * sin(l));
+        const double ra = atan2(cos(ee) * sin(l), cos(l));
+        const double lst = 18.697374558 + 24.06570982441908 * d + e6[4] / 15;
+        const double h = lst / 12 * kPI - ra;
+        const double latr = e6[5] * (kPI / 180.0);
+        const double sza2 = c.sfsza < 0 ? acos(sin(latr) * sin(dec) + cos(latr) * cos(dec) * cos(h)) *
+                                              (180.0 / kPI)
+                                        : c.sfsza;
+        if (sza2 < 89.999) {
+          double x0[3], x1[3];
+          to_cart(e6[3], e6[4], e6[5], x0);
+          to_cart(e6[0], e6[1], e6[2], x1);
+          for (int i = 0; i < 3; i++) x1[i] -= x0[i];
+          const double cosa = (x0[0] * x1[0] + x0[1] * x1[1] + x0[2] * x1[2]) /
+                              sqrt(x0[0] * x0[0] + x0[1] * x0[1] + x0[2] * x0[2]) /
+                              sqrt(x1[0] * x1[0] + x1[1] * x1[1] + x1[2] * x1[2]);
+          const double rcos = cosa / cos(sza2 * (kPI / 180.0));
+          radd += 6.764e-5 / (2. * kPI) * planck(kTSUN, nud) * tr * (1 - sfeps) * tau * rcos;
+        }
+      }
+    }
+  }
+  if (c.write_bbt) radd = kC2 * nud / log1p(kC1 * (nud * nud * nud) / radd);
+  const long long oi = (long long)id * b.nray + r;
+  b.rad[oi] = b.mask[oi] ? __longlong_as_double(0x7ff8000000000000LL) : radd;
+  b.tau[oi] = (double)tau;
+}
+
+__global__ void k_src_to_float(int nd, const double* sr, float* srf) {
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= nd * kNS) return;
+  const int id = gid / kNS, it = gid % kNS;
+  srf[gid] = (float)sr[(long long)it * nd + id];
+}
+
+__global__ void k_to_float(long long n, const double* src, float* dst) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (float)src[i];
+}
+
+void launch_pack_tiles_n(const CtlDev& c, const LosDev& L, const MixedPlan& P,
+                         long long total_tile_points, cudaStream_t s) {
+  const long long nth = total_tile_points * 32;
+  const int bs = 256;
+  k_pack_tiles<<<(unsigned)((nth + bs - 1) / bs), bs, 0, s>>>(c, L, P, total_tile_points);
+}
+
+void launch_path_mixed(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
+                       const LosDev& L, const MixedPlan& P, float* refl_scratch,
+                       cudaStream_t s) {
+  const int nchb = (c.nd + 3) / 4;
+  const long long nblk = (long long)P.ntile * nchb;
+  k_path_mixed<<<(unsigned)nblk, 128, 0, s>>>(c, T, ch, b, L, P, refl_scratch);
+}
+
+void launch_src_to_float(int nd, const double* sr, float* srf, cudaStream_t s) {
+  const int n = nd * kNS, bs = 256;
+  k_src_to_float<<<(n + bs - 1) / bs, bs, 0, s>>>(nd, sr, srf);
+}
+
+void launch_tables_to_float(long long n, const double* src, float* dst, cudaStream_t s) {
+  const int bs = 256;
+  if (n > 0) k_to_float<<<(unsigned)((n + bs - 1) / bs), bs, 0, s>>>(n, src, dst);
+}
+
+}  // namespace jgb

@@ -1,0 +1,250 @@
+"""ctypes binding to libjurassic_gb300.so and the Python mirror of the
+reference's forward-model interface.
+
+``Context`` owns one device context (``jgb_ctx``); its methods follow the
+reference functions they replace:
+
+* ``formod(atm, obs)``        -- formod (src/jurassic.c:3026-3071)
+* ``formod_batch(batch)``     -- jur_unified_formod_multiple_packages seam
+                                 (src/formod.c:72-73), host buffers
+* ``formod_batch_dev(dev)``   -- same on device-resident inputs
+
+The CUDA library is the only compute path: if it cannot be loaded the
+import fails with an error; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+from .model import Atm, Ctl, JurassicError, Obs
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libjurassic_gb300.so")
+
+JGB_OK = 0
+FP64 = 0
+MIXED = 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_fp = C.POINTER(C.c_float)
+
+
+class _Ctl(C.Structure):
+    _fields_ = [("ng", C.c_int), ("emitter", C.POINTER(C.c_char_p)), ("nd", C.c_int),
+                ("nu", _dp), ("nw", C.c_int), ("window", _ip), ("ncl", C.c_int),
+                ("clnu", _dp), ("nsf", C.c_int), ("sfnu", _dp), ("sftype", C.c_int),
+                ("sfsza", C.c_double), ("hydz", C.c_double), ("ctm_co2", C.c_int),
+                ("ctm_h2o", C.c_int), ("ctm_n2", C.c_int), ("ctm_o2", C.c_int),
+                ("refrac", C.c_int), ("rayds", C.c_double), ("raydz", C.c_double),
+                ("formod", C.c_int), ("write_bbt", C.c_int), ("retp_zmin", C.c_double),
+                ("retp_zmax", C.c_double), ("rett_zmin", C.c_double), ("rett_zmax", C.c_double),
+                ("retq_zmin", _dp), ("retq_zmax", _dp), ("retk_zmin", _dp), ("retk_zmax", _dp),
+                ("ret_clz", C.c_int), ("ret_cldz", C.c_int), ("ret_clk", C.c_int),
+                ("ret_sfz", C.c_int), ("ret_sfp", C.c_int), ("ret_sft", C.c_int),
+                ("ret_sfeps", C.c_int), ("nlos_max", C.c_int)]
+
+
+class _Batch(C.Structure):
+    _fields_ = [("nobs", C.c_int), ("lev_off", _ip), ("time", _dp), ("z", _dp), ("lon", _dp),
+                ("lat", _dp), ("p", _dp), ("t", _dp), ("q", _dp), ("k", _dp), ("scal", _dp),
+                ("ray_off", _ip), ("geo", _dp), ("rad", _dp), ("tau", _dp), ("tp", _dp)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("h2d_ms", C.c_double), ("hydro_ms", C.c_double), ("trace_ms", C.c_double),
+                ("pack_ms", C.c_double), ("path_ms", C.c_double), ("d2h_ms", C.c_double),
+                ("total_ms", C.c_double), ("los_points", C.c_longlong),
+                ("path_launches", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# exported symbols and their signatures (the contract of include/jurassic_gb300.h)
+SIGNATURES = {
+    "jgb_create": (C.c_int, [C.POINTER(_Ctl), C.c_int, C.POINTER(C.c_void_p)]),
+    "jgb_destroy": (None, [C.c_void_p]),
+    "jgb_last_error": (C.c_char_p, [C.c_void_p]),
+    "jgb_tables_init": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "jgb_set_table": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _ip, _dp, _ip, _fp,
+                                _fp, C.c_int, C.c_int]),
+    "jgb_set_filter": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp]),
+    "jgb_set_srcfunc": (C.c_int, [C.c_void_p, _dp]),
+    "jgb_get_srcfunc": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "jgb_formod": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                             C.c_int, _dp, _dp, _dp, _dp, C.c_int]),
+    "jgb_formod_batch": (C.c_int, [C.c_void_p, C.POINTER(_Batch), C.c_int]),
+    "jgb_formod_batch_dev": (C.c_int, [C.c_void_p, C.POINTER(_Batch), C.c_int]),
+    "jgb_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    "jgb_host_alloc": (C.c_void_p, [C.c_ulonglong]),
+    "jgb_host_free": (None, [C.c_void_p]),
+    "jgb_dev_alloc": (C.c_void_p, [C.c_ulonglong]),
+    "jgb_dev_free": (None, [C.c_void_p]),
+    "jgb_memcpy_h2d": (C.c_int, [C.c_void_p, C.c_void_p, C.c_ulonglong]),
+    "jgb_memcpy_d2h": (C.c_int, [C.c_void_p, C.c_void_p, C.c_ulonglong]),
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the CUDA library (raises if it is missing: no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise ImportError("libjurassic_gb300.so not built (run __graft_entry__.build())")
+        L = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _p(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+class Context:
+    """One device context: control set, tables and source function."""
+
+    def __init__(self, ctl: Ctl, tables=None, filters=None, device: int = 0,
+                 nlos_max: int = 4096, srcfunc: Optional[np.ndarray] = None):
+        L = load()
+        self.ctl = ctl
+        self._keep = dict(
+            names=(C.c_char_p * max(ctl.ng, 1))(*[e.encode() for e in ctl.emitter]),
+            nu=_d(ctl.nu), window=np.ascontiguousarray(ctl.window, np.int32),
+            clnu=_d(ctl.clnu), sfnu=_d(ctl.sfnu), rqn=_d(ctl.retq_zmin), rqx=_d(ctl.retq_zmax),
+            rkn=_d(ctl.retk_zmin), rkx=_d(ctl.retk_zmax))
+        k = self._keep
+        c = _Ctl(ng=ctl.ng, emitter=C.cast(k["names"], C.POINTER(C.c_char_p)), nd=ctl.nd,
+                 nu=_p(k["nu"]), nw=ctl.nw, window=_p(k["window"], _ip), ncl=ctl.ncl,
+                 clnu=_p(k["clnu"]), nsf=ctl.nsf, sfnu=_p(k["sfnu"]), sftype=ctl.sftype,
+                 sfsza=ctl.sfsza, hydz=ctl.hydz, ctm_co2=ctl.ctm_co2, ctm_h2o=ctl.ctm_h2o,
+                 ctm_n2=ctl.ctm_n2, ctm_o2=ctl.ctm_o2, refrac=ctl.refrac, rayds=ctl.rayds,
+                 raydz=ctl.raydz, formod=ctl.formod, write_bbt=ctl.write_bbt,
+                 retp_zmin=ctl.retp_zmin, retp_zmax=ctl.retp_zmax, rett_zmin=ctl.rett_zmin,
+                 rett_zmax=ctl.rett_zmax, retq_zmin=_p(k["rqn"]), retq_zmax=_p(k["rqx"]),
+                 retk_zmin=_p(k["rkn"]), retk_zmax=_p(k["rkx"]), ret_clz=ctl.ret_clz,
+                 ret_cldz=ctl.ret_cldz, ret_clk=ctl.ret_clk, ret_sfz=ctl.ret_sfz,
+                 ret_sfp=ctl.ret_sfp, ret_sft=ctl.ret_sft, ret_sfeps=ctl.ret_sfeps,
+                 nlos_max=nlos_max)
+        h = C.c_void_p()
+        rc = L.jgb_create(C.byref(c), device, C.byref(h))
+        if rc != JGB_OK:
+            raise JurassicError("jgb_create failed (%d)" % rc)
+        self.h = h
+        if tables is not None:
+            self.set_tables(tables)
+        if srcfunc is not None:
+            self.set_srcfunc(srcfunc)
+        elif filters is not None:
+            self.set_filters(filters)
+
+    def _check(self, rc):
+        if rc != JGB_OK:
+            raise JurassicError("libjurassic_gb300 error %d: %s" % (
+                rc, load().jgb_last_error(self.h).decode()))
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().jgb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_tables(self, tbl):
+        L = load()
+        nd, ng, tp, tt, tu = tbl.u.shape
+        self._check(L.jgb_tables_init(self.h, tp, tt, tu))
+        for id in range(nd):
+            for ig in range(ng):
+                n = int(tbl.np_[id, ig])
+                p = _d(tbl.p[id, ig])
+                nt = np.ascontiguousarray(tbl.nt[id, ig], np.int32)
+                t = _d(tbl.t[id, ig])
+                nu = np.ascontiguousarray(tbl.nu[id, ig], np.int32)
+                u = np.ascontiguousarray(tbl.u[id, ig], np.float32)
+                e = np.ascontiguousarray(tbl.eps[id, ig], np.float32)
+                self._check(L.jgb_set_table(self.h, id, ig, n, _p(p), _p(nt, _ip), _p(t),
+                                            _p(nu, _ip), _p(u, _fp), _p(e, _fp), tt, tu))
+
+    def set_filters(self, filters):
+        for id, (fnu, f) in enumerate(filters):
+            fnu, f = _d(fnu), _d(f)
+            self._check(load().jgb_set_filter(self.h, id, len(fnu), _p(fnu), _p(f)))
+
+    def set_srcfunc(self, sr):
+        sr = _d(sr)
+        self._check(load().jgb_set_srcfunc(self.h, _p(sr)))
+
+    def srcfunc(self):
+        st = np.zeros(1200)
+        sr = np.zeros((1200, self.ctl.nd))
+        self._check(load().jgb_get_srcfunc(self.h, _p(st), _p(sr)))
+        return st, sr
+
+    def stats(self) -> dict:
+        s = Stats()
+        load().jgb_get_stats(self.h, C.byref(s))
+        return s.as_dict()
+
+    # --------------------------------------------------------------
+    def formod(self, atm: Atm, obs: Obs, precision: int = FP64) -> Obs:
+        """Forward model of one observation; returns a new Obs with rad/tau/tp
+        filled (and updates atm.p when hydrostatic equilibrium is on)."""
+        ctl = self.ctl
+        out = obs.copy()
+        a = dict(time=_d(atm.time), z=_d(atm.z), lon=_d(atm.lon), lat=_d(atm.lat),
+                 p=_d(atm.p).copy(), t=_d(atm.t), q=_d(np.asarray(atm.q).reshape(ctl.ng, -1)),
+                 k=_d(np.asarray(atm.k).reshape(max(ctl.nw, 0), -1)), scal=_d(atm.scal(ctl)))
+        geo = _d(obs.geo())
+        rad = _d(obs.rad).copy()
+        tau = np.zeros((ctl.nd, obs.nr))
+        tp = np.zeros((3, obs.nr))
+        self._check(load().jgb_formod(self.h, atm.np, _p(a["time"]), _p(a["z"]), _p(a["lon"]),
+                                      _p(a["lat"]), _p(a["p"]), _p(a["t"]), _p(a["q"]),
+                                      _p(a["k"]), _p(a["scal"]), obs.nr, _p(geo), _p(rad),
+                                      _p(tau), _p(tp), precision))
+        out.rad, out.tau = rad, tau
+        out.tpz, out.tplon, out.tplat = tp[0].copy(), tp[1].copy(), tp[2].copy()
+        atm.p = a["p"]
+        return out
+
+    def formod_batch(self, batch, precision: int = FP64):
+        """Batched forward model on host arrays; returns a new Batch."""
+        b = batch.copy()
+        arr = {k: _d(getattr(b, k)) for k in ("time", "z", "lon", "lat", "p", "t", "q", "k",
+                                               "scal", "geo", "rad", "tau", "tp")}
+        lev = np.ascontiguousarray(b.lev_off, np.int32)
+        ray = np.ascontiguousarray(b.ray_off, np.int32)
+        s = _Batch(nobs=b.nobs, lev_off=_p(lev, _ip), ray_off=_p(ray, _ip),
+                   **{k: _p(v) for k, v in arr.items()})
+        self._check(load().jgb_formod_batch(self.h, C.byref(s), precision))
+        for k in ("rad", "tau", "tp", "p"):
+            setattr(b, k, arr[k])
+        return b
+
+    def formod_batch_ptrs(self, ptrs: dict, nobs: int, precision: int = FP64,
+                          device: bool = True):
+        """Batched forward model on raw pointers (device pointers by default);
+        ``ptrs`` maps jgb_batch field names to integer addresses."""
+        s = _Batch(nobs=nobs, **{k: C.cast(C.c_void_p(v), _ip if k in ("lev_off", "ray_off") else _dp)
+                                 for k, v in ptrs.items()})
+        fn = load().jgb_formod_batch_dev if device else load().jgb_formod_batch
+        self._check(fn(self.h, C.byref(s), precision))

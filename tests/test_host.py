@@ -1,0 +1,104 @@
+"""Host logic: control-file parsing (scan_ctl/read_ctl semantics), file
+formats, table writer/reader round trip, batch packing."""
+import os
+
+import numpy as np
+import pytest
+
+from jurassic_gb300 import synth
+from jurassic_gb300.model import (JurassicError, read_atm, read_ctl, read_obs, read_ret,
+                                  scan_ctl, write_atm, write_obs)
+from jurassic_gb300.tables import read_filter, write_filter, write_tbl
+
+
+def test_scan_ctl_semantics(tmp_path):
+    f = tmp_path / "a.ctl"
+    f.write_text("NG = 2\nEMITTER[0] = CO2\nemitter[*] = H2O\nND = 1\nNU[0] = 792.0\n"
+                 "RAYDZ = 0.5\n")
+    argv = ["prog", str(f), "RAYDZ", "0.25"]
+    assert scan_ctl(argv, "EMITTER", 0) == "CO2"        # exact index wins first match
+    assert scan_ctl(argv, "EMITTER", 1) == "H2O"        # NAME[*] applies to every index
+    assert scan_ctl(argv, "raydz") == "0.25"            # argv overrides, case-insensitive
+    assert scan_ctl(argv, "RAYDS", -1, "10") == "10"   # default
+    with pytest.raises(JurassicError):
+        scan_ctl(argv, "MISSING")                      # no default -> error
+    ctl = read_ctl(argv)
+    assert ctl.emitter == ["CO2", "H2O"] and ctl.nd == 1 and ctl.raydz == 0.25
+    assert ctl.formod == 1 and ctl.ctm_co2 == 1 and ctl.sftype == 2  # reference defaults
+
+
+def test_read_ctl_errors(tmp_path):
+    f = tmp_path / "b.ctl"
+    f.write_text("NCL = 1\n")
+    with pytest.raises(JurassicError):
+        read_ctl(["p", str(f)])
+    f.write_text("SFTYPE = 4\n")
+    with pytest.raises(JurassicError):
+        read_ctl(["p", str(f)])
+
+
+def test_ctl_roundtrip(tmp_path):
+    w = synth.config_limb_ega()
+    f = tmp_path / "c.ctl"
+    f.write_text("\n".join(w.ctl.to_lines()) + "\n")
+    c2 = read_ctl(["p", str(f)])
+    assert c2.emitter == w.ctl.emitter
+    assert np.array_equal(c2.nu, w.ctl.nu)
+    assert c2.raydz == w.ctl.raydz and c2.formod == w.ctl.formod
+
+
+def test_atm_obs_file_roundtrip(tmp_path):
+    w = synth.config_limb_ega()
+    atm, obs = w.batch.item(w.ctl, 0)
+    write_atm(str(tmp_path), "atm.tab", w.ctl, atm)
+    a2 = read_atm(str(tmp_path), "atm.tab", w.ctl)
+    assert np.array_equal(a2.p, atm.p) and np.array_equal(a2.q, atm.q)
+    obs.rad[:] = 0.5
+    write_obs(str(tmp_path), "obs.tab", w.ctl, obs, full_precision=True)
+    o2 = read_obs(str(tmp_path), "obs.tab", w.ctl)
+    assert np.array_equal(o2.vplat, obs.vplat) and np.array_equal(o2.rad, obs.rad)
+
+
+def test_binary_table_layout(tmp_path):
+    """TBLFMT=2 record layout of read_tbl/write_tbl (jurassic.c:5030-5084)."""
+    w = synth.config_limb_ega()
+    tbl = synth.make_tables(w.ctl, 3, tp=32, tt=4, tu=40)
+    w.ctl.tblbase = str(tmp_path / "t")
+    w.ctl.tblfmt = 2
+    write_tbl(w.ctl, tbl)
+    raw = open(w.ctl.table_filename(0, 0), "rb").read()
+    np_ = np.frombuffer(raw[:4], "<i4")[0]
+    assert np_ == 32
+    p = np.frombuffer(raw[4:4 + 8 * 32], "<f8")
+    assert np.array_equal(p, tbl.p[0, 0, :32])
+    nt = np.frombuffer(raw[4 + 256:4 + 256 + 4], "<i4")[0]
+    assert nt == 4
+
+
+def test_filter_roundtrip(tmp_path):
+    fnu, f = np.linspace(700, 701, 11), np.linspace(0, 1, 11)
+    write_filter(str(tmp_path / "x.filt"), fnu, f)
+    a, b = read_filter(str(tmp_path / "x.filt"))
+    assert np.array_equal(a, fnu) and np.array_equal(b, f)
+
+
+def test_batch_pack_item_roundtrip():
+    w = synth.config_nadir(5, nd=4, nlev=21, ztop=20.0)
+    b = w.batch
+    assert b.nobs == 5 and b.nray == 5 and b.nlev == 5 * 21
+    atm, obs = b.item(w.ctl, 3)
+    assert atm.np == 21 and obs.nr == 1
+    b2 = synth.pack(w.ctl, [b.item(w.ctl, i) for i in range(5)])
+    for k in ("z", "p", "t", "q", "geo", "scal"):
+        assert np.array_equal(getattr(b2, k), getattr(b, k))
+
+
+def test_read_ret_defaults(tmp_path):
+    f = tmp_path / "r.ctl"
+    f.write_text("NG = 1\nEMITTER[0] = CO2\nND = 2\nNU[0] = 700\nNU[1] = 710\n"
+                 "ERR_NOISE[*] = 1e-4\nERR_TEMP = 2\n")
+    argv = ["p", str(f)]
+    ctl = read_ctl(argv)
+    r = read_ret(argv, ctl)
+    assert r.kernel_recomp == 3 and r.conv_itmax == 30 and r.conv_dmin == 0.1
+    assert np.array_equal(r.err_noise, [1e-4, 1e-4]) and r.err_temp == 2.0
