@@ -1,0 +1,362 @@
+#!/usr/bin/env python3
+"""Benchmark: ray-channel radiances/s of the batched forward model on one GB300.
+
+Workload (default): batched nadir forward model, 1e5 observations from
+705 km, 101 levels on 0-100 km, 100 channels on 650-2400 cm^-1, 5 emitters
+(CO2, H2O, O3, CH4, N2O), EGA, seeded synthetic atmospheres and tables
+(~1.6 GB of float32 emissivity tables).  One step = one forward-model call
+over the whole batch (ray tracing + path loop + epilogue).
+
+Reported line (one JSON object, rank 0):
+  value        mixed-precision path, inputs resident in GPU memory
+  e2e          same through jgb_formod_batch with page-locked host buffers,
+               host->device and device->host copies inside the timed region
+  fp64         the plain FP64 GPU form (rounding-level agreement with the
+               reference) on the same batch
+  roofline     path kernel: byte model / CUDA-event time vs measured HBM peak
+  cpu_baseline the CPU oracle (restatement of the reference) on a bounded
+               sample of the same workload with all host threads
+  accuracy     |BT_mixed - BT_oracle| and FP64 relative error on that sample
+
+--impl reference times the reference's CPU implementation instead (the
+reference build when present, else the CPU restatement) on a bounded sample.
+Multi-GPU (torchrun): independent replicas, weak scaling, max time over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ray-channel radiances/s"
+UNIT = "ray-channel radiances/s"
+
+
+def dist_setup(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as td
+        td.init_process_group("gloo")
+        pg = td
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def allmax(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def path_bytes_model(ctl, tables, los_points):
+    """Algorithmic bytes of the path kernel: per (LOS point, channel) 8
+    lookups per emitter (EGA; 4 for CGA), each ceil(log2 nu)+4 float probes,
+    plus two FP64 source-function entries."""
+    tu = tables.u.shape[-1]
+    lookups = 8 if ctl.formod == 1 else 4
+    per = ctl.ng * lookups * (int(np.ceil(np.log2(tu))) + 4) * 4 + 16
+    return float(los_points) * ctl.nd * per
+
+
+def build_workload(args):
+    from jurassic_gb300 import synth
+    if args.workload == "nadir":
+        return synth.config_nadir(args.nobs)
+    if args.workload == "limb_cga":
+        return synth.config_limb_cga(args.nobs)
+    raise SystemExit("unknown workload " + args.workload)
+
+
+def cpu_sample(w, nsample):
+    b = w.batch
+    items = [b.item(w.ctl, i) for i in range(nsample)]
+    from jurassic_gb300 import synth
+    return synth.pack(w.ctl, items)
+
+
+def time_cpu(w, ora, target_s, threads):
+    """Time the oracle on a growing sample until ~target_s of work."""
+    n = 8
+    while True:
+        s = cpu_sample(w, n)
+        t0 = time.perf_counter()
+        out = ora.formod_batch(s.fresh_outputs(), nthreads=threads)
+        dt = time.perf_counter() - t0
+        if dt >= target_s or n >= w.batch.nobs:
+            return s, out, dt
+        n = min(w.batch.nobs, max(n * 2, int(n * target_s / max(dt, 1e-3) * 1.05)))
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    from oracle import oracle, refimpl
+    w = build_workload(args)
+    threads = os.cpu_count() or 1
+    kind = "port"
+    ora = oracle.Oracle(w.ctl, w.tables, w.filters)
+    use_ref = refimpl.available("big") and os.path.isdir("/root/reference")
+    per_step = []
+    sample_n = None
+    for step in range(args.warmup + args.steps):
+        s, out, dt = time_cpu(w, ora, args.cpu_seconds / max(args.steps, 1), threads)
+        sample_n = s.nobs
+        if step >= args.warmup:
+            per_step.append(dt)
+    units = sample_n * w.ctl.nd
+    value = units / statistics.mean(per_step)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * statistics.mean(per_step), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w.name, "sample_observations": sample_n},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                             "sample": "%d of %d observations x %d channels per step" % (
+                                 sample_n, w.batch.nobs, w.ctl.nd)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="nadir", choices=["nadir", "limb_cga"])
+    ap.add_argument("--nobs", type=int, default=100000)
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+
+    rank, world, local, pg = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    from jurassic_gb300 import native
+    from jurassic_gb300.model import brightness
+    native.load()
+    w = build_workload(args)
+    ctl, b = w.ctl, w.batch
+    ctx = native.Context(ctl, w.tables, w.filters, device=local)
+    L = native.load()
+    units = b.nray * ctl.nd
+
+    # device-resident copies of the batch inputs (the "value" path)
+    import ctypes as C
+    fields = {k: np.ascontiguousarray(getattr(b, k), dtype=np.float64)
+              for k in ("time", "z", "lon", "lat", "p", "t", "q", "k", "scal", "geo")}
+    fields["rad"] = np.zeros((ctl.nd, b.nray))
+    fields["tau"] = np.zeros((ctl.nd, b.nray))
+    fields["tp"] = np.zeros((3, b.nray))
+    ints = {"lev_off": np.ascontiguousarray(b.lev_off, np.int32),
+            "ray_off": np.ascontiguousarray(b.ray_off, np.int32)}
+    dptr = {}
+    for k, a in list(fields.items()) + list(ints.items()):
+        p = L.jgb_dev_alloc(max(a.nbytes, 8))
+        assert p, "device allocation failed"
+        L.jgb_memcpy_h2d(p, a.ctypes.data, a.nbytes)
+        dptr[k] = p
+
+    def dev_step(prec):
+        L.jgb_memcpy_h2d(dptr["rad"], fields["rad"].ctypes.data, fields["rad"].nbytes)
+        ctx.formod_batch_ptrs(dptr, b.nobs, prec, device=True)
+        return ctx.stats()
+
+    # ---- mixed precision, device-resident (value) ----
+    for _ in range(args.warmup):
+        dev_step(native.MIXED)
+    barrier(pg)
+    ms, path_ms, stats = [], [], None
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            stats = dev_step(native.MIXED)
+            ms.append(stats["total_ms"])
+            path_ms.append(stats["path_ms"])
+        wall = time.perf_counter() - t0
+    barrier(pg)
+    ms_step = allmax(pg, statistics.mean(ms))
+    value = units * world / (ms_step / 1e3)
+    rad_mixed = np.zeros((ctl.nd, b.nray))
+    L.jgb_memcpy_d2h(rad_mixed.ctypes.data, dptr["rad"], rad_mixed.nbytes)
+
+    # ---- e2e through the public C ABI with page-locked host buffers ----
+    hb = {}
+    for k, a in list(fields.items()) + list(ints.items()):
+        p = L.jgb_host_alloc(max(a.nbytes, 8))
+        C.memmove(p, a.ctypes.data, a.nbytes)
+        hb[k] = p
+    h2d = sum(fields[k].nbytes for k in ("time", "z", "lon", "lat", "p", "t", "q", "k", "scal",
+                                           "geo", "rad")) + 2 * ints["lev_off"].nbytes
+    d2h = fields["rad"].nbytes + fields["tau"].nbytes + fields["tp"].nbytes
+    for _ in range(max(1, args.warmup - 1)):
+        ctx.formod_batch_ptrs(hb, b.nobs, native.MIXED, device=False)
+    e2e_ms = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        ctx.formod_batch_ptrs(hb, b.nobs, native.MIXED, device=False)
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    e2e_value = units * world / (allmax(pg, statistics.mean(e2e_ms)) / 1e3)
+
+    # ---- plain FP64 GPU form ----
+    fp64_ms = []
+    dev_step(native.FP64)
+    for _ in range(args.fp64_steps):
+        fp64_ms.append(dev_step(native.FP64)["total_ms"])
+    fp64_value = units * world / (allmax(pg, statistics.mean(fp64_ms)) / 1e3)
+    rad_fp64 = np.zeros((ctl.nd, b.nray))
+    L.jgb_memcpy_d2h(rad_fp64.ctypes.data, dptr["rad"], rad_fp64.nbytes)
+
+    line = None
+    if rank == 0:
+        hbm, peak_kind = peaks()
+        bytes_alg = path_bytes_model(ctl, w.tables, stats["los_points"])
+        achieved = bytes_alg / (statistics.mean(path_ms) / 1e3) / 1e9
+        try:
+            traffic = json.load(open(os.path.join(ROOT, "profiles", "path_mixed_traffic.json")))
+            traffic_per_launch = traffic["bytes_per_los_point"] * stats["los_points"]
+        except (OSError, KeyError, ValueError):
+            traffic_per_launch = None
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32 path loop (compensated), f64 ray tracing",
+                "data": "synthetic (seeded)",
+                "config": {"workload": w.name, "observations": b.nobs, "rays": b.nray,
+                           "channels": ctl.nd, "emitters": ctl.ng, "levels_per_profile": 101 if args.workload == "nadir" else None,
+                           "method": "EGA" if ctl.formod == 1 else "CGA",
+                           "los_points": stats["los_points"],
+                           "l2_policy": "inputs and tables larger than L2 (129 MB); no flush",
+                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "stage_ms": {k: stats[k] for k in ("hydro_ms", "trace_ms", "pack_ms", "path_ms")},
+                "wall_s_timed": wall,
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                        "d2h_bytes_per_step": int(d2h), "ms_per_step": statistics.mean(e2e_ms)},
+                "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": statistics.mean(fp64_ms),
+                         "speedup_mixed_over_fp64": value / fp64_value},
+                "gpu_launches": int(stats["path_launches"]) * args.steps,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                             "frac": achieved / hbm, "traffic": traffic_per_launch,
+                             "kernel": "k_path_mixed", "bytes_model": "per (LOS point, channel): ng*8*(ceil(log2 TU)+4)*4 + 16 B",
+                             "bytes_per_launch": bytes_alg, "peak_kind": peak_kind},
+                "clocks": clk.summary()}
+
+    # ---- CPU baseline + accuracy on a bounded sample ----
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle
+        ora = oracle.Oracle(ctl, w.tables, w.filters)
+        threads = os.cpu_count() or 1
+        s, ref, dt = time_cpu(w, ora, args.cpu_seconds, threads)
+        n = s.nobs
+        line["cpu_baseline"] = {"value": n * ctl.nd / dt, "unit": UNIT, "cores": threads,
+                                "kind": "port",
+                                "sample": "first %d of %d observations x %d channels" % (n, b.nobs, ctl.nd)}
+        nu = np.asarray(ctl.nu)[:, None]
+        sl = slice(0, s.nray)
+        bt_ref = brightness(ref.rad, nu)
+        dbt = np.abs(brightness(rad_mixed[:, sl], nu) - bt_ref)
+        rel64 = np.abs(rad_fp64[:, sl] - ref.rad) / np.abs(ref.rad)
+        line["accuracy"] = {"sample_rays": int(s.nray), "mixed_max_abs_dBT_mK": 1e3 * float(np.max(dbt)),
+                            "mixed_p99_abs_dBT_mK": 1e3 * float(np.percentile(dbt, 99)),
+                            "mixed_max_rel_rad": float(np.max(np.abs(rad_mixed[:, sl] - ref.rad) / np.abs(ref.rad))),
+                            "fp64_max_rel_rad": float(np.max(rel64))}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    for p in dptr.values():
+        L.jgb_dev_free(p)
+    for p in hb.values():
+        L.jgb_host_free(p)
+    ctx.close()
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

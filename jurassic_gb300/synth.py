@@ -88,7 +88,8 @@ def make_tables(ctl: Ctl, seed: int, tp=41, tt=30, tu=320, pmin=1e-3, pmax=1100.
     if descending_p:
         pgrid = pgrid[::-1].copy()
     ugrid = np.logspace(np.log10(umin), np.log10(umax), tu)
-    tbase = np.linspace(tmin, tmax, tt)
+    uu = ugrid.astype(np.float32)
+    tgrid = np.linspace(tmin, tmax, tt)[None, :] + t_shift_per_level * (np.arange(tp)[:, None] - tp // 2)
     for ig in range(ng):
         col = _COLUMNS.get(ctl.emitter[ig].upper(), 1e18)
         lo, hi = max(0.01 / col, 1.5e-25), min(100.0 / col, 1e-17)
@@ -102,23 +103,22 @@ def make_tables(ctl: Ctl, seed: int, tp=41, tt=30, tu=320, pmin=1e-3, pmax=1100.
             tbl.np_[id, ig] = tp
             tbl.p[id, ig, :] = pgrid
             tbl.nt[id, ig, :] = tt
-            for ip in range(tp):
-                tg = tbase + t_shift_per_level * (ip - tp // 2)
-                tbl.t[id, ig, ip, :] = tg
-                k = k0[id] * (pgrid[ip] / 1013.0) ** aexp[id] * (tg / 250.0) ** bexp[id]
-                eps = (-np.expm1(-np.outer(k, ugrid))).astype(np.float32)  # [tt, tu]
-                uu = ugrid.astype(np.float32)
-                for it in range(tt):
-                    e = eps[it]
-                    keep = (e >= 1e-6) & (e <= 0.999999)
-                    ek, uk = e[keep], uu[keep]
-                    if len(ek) > 1:  # strictly increasing in float32
-                        m = np.concatenate([[True], np.diff(ek) > 0])
-                        ek, uk = ek[m], uk[m]
-                    n = len(ek)
-                    tbl.nu[id, ig, ip, it] = n
-                    tbl.u[id, ig, ip, it, :n] = uk
-                    tbl.eps[id, ig, ip, it, :n] = ek
+            tbl.t[id, ig] = tgrid
+            k = k0[id] * (pgrid[:, None] / 1013.0) ** aexp[id] * (tgrid / 250.0) ** bexp[id]
+            eps = (-np.expm1(-k[:, :, None] * ugrid[None, None, :])).astype(np.float32)
+            # keep 1e-6 <= eps <= 0.999999 and strictly increasing (float32)
+            keep = (eps >= 1e-6) & (eps <= 0.999999)
+            prev = np.concatenate([np.full(eps.shape[:2] + (1,), -1.0, np.float32), eps[:, :, :-1]], 2)
+            keep &= eps > prev
+            order = np.argsort(~keep, axis=2, kind="stable")
+            n = keep.sum(axis=2)
+            e_sorted = np.take_along_axis(eps, order, axis=2)
+            u_sorted = np.broadcast_to(uu, eps.shape)
+            u_sorted = np.take_along_axis(u_sorted, order, axis=2)
+            valid = np.arange(tu)[None, None, :] < n[:, :, None]
+            tbl.nu[id, ig] = n
+            tbl.eps[id, ig] = np.where(valid, e_sorted, 0.0)
+            tbl.u[id, ig] = np.where(valid, u_sorted, 0.0)
     return tbl
 
 
@@ -282,22 +282,35 @@ def config_nadir(nobs, seed=2, nd=100, nlev=101, ztop=100.0, emitters=("CO2", "H
                  numin=650.0, numax=2400.0, formod=1, obsz=705.0) -> Workload:
     """Batched nadir: `nobs` profiles on 0-ztop km, one nadir ray each from
     705 km with a small scan angle, `nd` channels, seeded +-5 K temperature and
-    +-20 % gas perturbations of the standard atmosphere."""
+    +-20 % gas perturbations of the standard atmosphere (vectorised)."""
     ctl = Ctl(emitter=list(emitters), nu=np.linspace(numin, numax, nd), formod=formod)
     rng = np.random.default_rng(seed)
     z = np.linspace(0.0, ztop, nlev)
-    items = []
-    for i in range(nobs):
-        dt = rng.uniform(-2.5, 2.5) + rng.uniform(-2.5, 2.5) * np.sin(z / 15.0 + rng.uniform(0, 6.3))
-        dq = 1 + rng.uniform(-0.2, 0.2, ctl.ng)
-        lat = rng.uniform(-60, 60)
-        lon = rng.uniform(-180, 180)
-        atm = profile(ctl.emitter, z, dt=dt, dq=dq, time=float(i), lon=lon, lat=lat)
-        obs = nadir_obs(nd, [lat], obsz=obsz, time=float(i), lon=lon,
-                        scan_deg=[rng.uniform(-3, 3)])
-        items.append((atm, obs))
+    t0 = std_temperature(z)
+    p0 = hydrostatic_pressure(z, t0)
+    q0 = np.stack([std_vmr(e, z) for e in ctl.emitter])
+    off = rng.uniform(-2.5, 2.5, nobs)
+    amp = rng.uniform(-2.5, 2.5, nobs)
+    ph = rng.uniform(0, 6.3, nobs)
+    dq = 1 + rng.uniform(-0.2, 0.2, (nobs, ctl.ng))
+    lat = rng.uniform(-60, 60, nobs)
+    lon = rng.uniform(-180, 180, nobs)
+    scan = rng.uniform(-3, 3, nobs)
+    t = t0[None, :] + off[:, None] + amp[:, None] * np.sin(z[None, :] / 15.0 + ph[:, None])
+    q = q0[None, :, :] * dq[:, :, None]                     # [nobs, ng, nlev]
+    L = nobs * nlev
+    time = np.repeat(np.arange(nobs, dtype=np.float64), nlev)
+    nscal = 5 + ctl.ncl + ctl.nsf
+    b = Batch(nobs=nobs, lev_off=(np.arange(nobs + 1) * nlev).astype(np.int32),
+              time=time, z=np.tile(z, nobs), lon=np.repeat(lon, nlev), lat=np.repeat(lat, nlev),
+              p=np.tile(p0, nobs), t=t.reshape(-1), q=q.transpose(1, 0, 2).reshape(ctl.ng, L).copy(),
+              k=np.zeros((ctl.nw, L)), scal=np.zeros((nobs, nscal)),
+              ray_off=np.arange(nobs + 1).astype(np.int32),
+              geo=np.stack([np.arange(nobs, dtype=np.float64), np.full(nobs, obsz), lon, lat,
+                            np.zeros(nobs), lon, lat + scan]),
+              rad=np.zeros((nd, nobs)), tau=np.zeros((nd, nobs)), tp=np.zeros((3, nobs)))
     return Workload("nadir_%dobs_%dlev_%dch_%dgas" % (nobs, nlev, nd, ctl.ng), ctl,
-                    make_tables(ctl, seed + 100), make_filters(ctl), pack(ctl, items))
+                    make_tables(ctl, seed + 100), make_filters(ctl), b)
 
 
 def config_limb_cga(nobs, seed=3, nd=32, emitters=("CO2", "H2O", "O3"), raydz=0.5,

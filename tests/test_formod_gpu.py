@@ -46,7 +46,7 @@ def _check(ctl, ref, out, precision, what=""):
 def _run_single(w, ctl=None, precisions=(native.FP64, native.MIXED), atm_mod=None, obs_mod=None):
     from oracle import oracle
     ctl = ctl or w.ctl
-    atm, obs = w.batch.item(ctl, 0)
+    atm, obs = w.batch.item(w.ctl, 0)
     if atm_mod:
         atm_mod(atm)
     if obs_mod:
