@@ -286,13 +286,14 @@ def main():
     e2e_value = units * world / (allmax(pg, statistics.mean(e2e_ms)) / 1e3)
 
     # ---- plain FP64 GPU form ----
-    fp64_ms = []
-    dev_step(native.FP64)
-    for _ in range(args.fp64_steps):
-        fp64_ms.append(dev_step(native.FP64)["total_ms"])
-    fp64_value = units * world / (allmax(pg, statistics.mean(fp64_ms)) / 1e3)
-    rad_fp64 = np.zeros((ctl.nd, b.nray))
-    L.jgb_memcpy_d2h(rad_fp64.ctypes.data, dptr["rad"], rad_fp64.nbytes)
+    fp64_ms, fp64_value, rad_fp64 = [], None, None
+    if args.fp64_steps > 0:
+        dev_step(native.FP64)
+        for _ in range(args.fp64_steps):
+            fp64_ms.append(dev_step(native.FP64)["total_ms"])
+        fp64_value = units * world / (allmax(pg, statistics.mean(fp64_ms)) / 1e3)
+        rad_fp64 = np.zeros((ctl.nd, b.nray))
+        L.jgb_memcpy_d2h(rad_fp64.ctypes.data, dptr["rad"], rad_fp64.nbytes)
 
     line = None
     if rank == 0:
@@ -319,8 +320,9 @@ def main():
                 "wall_s_timed": wall,
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h), "ms_per_step": statistics.mean(e2e_ms)},
-                "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": statistics.mean(fp64_ms),
-                         "speedup_mixed_over_fp64": value / fp64_value},
+                "fp64": None if fp64_value is None else {
+                    "value": fp64_value, "unit": UNIT, "ms_per_step": statistics.mean(fp64_ms),
+                    "speedup_mixed_over_fp64": value / fp64_value},
                 "gpu_launches": int(stats["path_launches"]) * args.steps,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                              "frac": achieved / hbm, "traffic": traffic_per_launch,
@@ -342,7 +344,7 @@ def main():
         sl = slice(0, s.nray)
         bt_ref = brightness(ref.rad, nu)
         dbt = np.abs(brightness(rad_mixed[:, sl], nu) - bt_ref)
-        rel64 = np.abs(rad_fp64[:, sl] - ref.rad) / np.abs(ref.rad)
+        rel64 = (np.abs(rad_fp64[:, sl] - ref.rad) / np.abs(ref.rad)) if rad_fp64 is not None else np.array([np.nan])
         line["accuracy"] = {"sample_rays": int(s.nray), "mixed_max_abs_dBT_mK": 1e3 * float(np.max(dbt)),
                             "mixed_p99_abs_dBT_mK": 1e3 * float(np.percentile(dbt, 99)),
                             "mixed_max_rel_rad": float(np.max(np.abs(rad_mixed[:, sl] - ref.rad) / np.abs(ref.rad))),
