@@ -130,6 +130,22 @@ int jgb_formod_batch_dev(jgb_ctx *ctx, const jgb_batch *b, int precision);
 
 int jgb_get_stats(const jgb_ctx *ctx, jgb_stats *out);
 
+/* Allocation-free FP64 forward model of a device-resident batch.  This entry
+   point has no counterpart in the reference.  It is for callers that cannot
+   allocate GPU memory while they run (a fixed memory budget handed over at
+   start-up, an allocator owned by another runtime, sections where allocation
+   is forbidden): all scratch comes from one 64 MiB device array that the
+   library holds on every GPU where it is loaded until the process exits, and
+   no cudaMalloc/cudaFree or allocating library routine is called.  Same
+   arguments and results as jgb_formod_batch_dev with JGB_FP64.
+   - A batch whose rays and LOS points need more than 64 MiB of scratch is
+     rejected with JGB_ERR_ARG (jgb_last_error names the bytes needed).
+   - The first call on a device resolves the array's address on that device;
+     make that first call before any stream capture.
+   - All calls on a device share the array and it keeps the previous call's
+     contents: calls that overlap on the GPU race and must be serialised. */
+int jgb_formod_batch_dev_noalloc(jgb_ctx *ctx, const jgb_batch *b);
+
 /* Page-locked host memory for fast transfers (cudaHostAlloc). */
 void *jgb_host_alloc(unsigned long long bytes);
 void jgb_host_free(void *p);

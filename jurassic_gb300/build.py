@@ -27,6 +27,7 @@ UNITS = {
     "jgb_fp64.cu": ["-fmad=false"],
     "jgb_mixed.cu": [],
     "jgb_api.cu": [],
+    "jgb_noalloc.cu": [],
 }
 
 

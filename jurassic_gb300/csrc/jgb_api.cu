@@ -383,6 +383,24 @@ int check_ready(jgb_ctx* x) {
 
 }  // namespace
 
+namespace jgb {
+
+int ctx_view(jgb_ctx* x, CtxView* out) {
+  if (!x || !out) return JGB_ERR_ARG;
+  const int rc = check_ready(x);
+  if (rc) return rc;
+  out->device = x->device;
+  out->stream = x->stream;
+  out->c = x->c;
+  out->T = tbl_view(x);
+  out->ch = chan_view(x);
+  return JGB_OK;
+}
+
+int ctx_fail(jgb_ctx* x, int code, const char* msg) { return fail(x, code, msg); }
+
+}  // namespace jgb
+
 // ===========================================================================
 // C ABI
 

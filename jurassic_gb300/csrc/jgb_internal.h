@@ -5,6 +5,8 @@
 
 #include "jgb_common.cuh"
 
+struct jgb_ctx;
+
 namespace jgb {
 
 // jgb_fp64.cu
@@ -35,5 +37,18 @@ void launch_path_mixed(const CtlDev& c, const TblDev& T, const ChanDev& ch, cons
                        cudaStream_t s);
 void launch_src_to_float(int nd, const double* sr, float* srf, cudaStream_t s);
 void launch_tables_to_float(long long n, const double* src, float* dst, cudaStream_t s);
+
+// jgb_api.cu: read-only view of a context for entry points defined in other
+// translation units.  Returns JGB_OK, or an error code with the context's
+// message set when tables or source functions are missing.
+struct CtxView {
+  int device;
+  cudaStream_t stream;
+  CtlDev c;
+  TblDev T;
+  ChanDev ch;
+};
+int ctx_view(jgb_ctx* x, CtxView* out);
+int ctx_fail(jgb_ctx* x, int code, const char* msg);
 
 }  // namespace jgb

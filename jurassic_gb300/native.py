@@ -81,6 +81,7 @@ SIGNATURES = {
     "jgb_formod_batch": (C.c_int, [C.c_void_p, C.POINTER(_Batch), C.c_int]),
     "jgb_formod_batch_dev": (C.c_int, [C.c_void_p, C.POINTER(_Batch), C.c_int]),
     "jgb_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    "jgb_formod_batch_dev_noalloc": (C.c_int, [C.c_void_p, C.POINTER(_Batch)]),
     "jgb_host_alloc": (C.c_void_p, [C.c_ulonglong]),
     "jgb_host_free": (None, [C.c_void_p]),
     "jgb_dev_alloc": (C.c_void_p, [C.c_ulonglong]),
