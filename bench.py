@@ -317,6 +317,9 @@ def main():
                            "l2_policy": "inputs and tables larger than L2 (129 MB); no flush",
                            "parallelism": "replicas" if world > 1 else "single GPU"},
                 "stage_ms": {k: stats[k] for k in ("hydro_ms", "trace_ms", "pack_ms", "path_ms")},
+                "autotune": {"path_variant": stats["path_variant"], "variant_ms": stats["tune_ms"][:4],
+                             "variants": ["no register cap", "5 blocks/SM (<=102 regs)",
+                                          "6 blocks/SM (<=85 regs)", "4 blocks/SM (<=128 regs)"]},
                 "wall_s_timed": wall,
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h), "ms_per_step": statistics.mean(e2e_ms)},

@@ -90,6 +90,8 @@ typedef struct {
   double h2d_ms, hydro_ms, trace_ms, pack_ms, path_ms, d2h_ms, total_ms;
   long long los_points;          /* LOS points of the batch */
   int path_launches;             /* kernels launched by the last call */
+  int path_variant;              /* mixed path kernel variant chosen by the autotuner */
+  float tune_ms[4];              /* autotuner timings of the variants [ms] */
 } jgb_stats;
 
 /* Context: replaces the process-global table state initialised by the first
@@ -127,6 +129,59 @@ int jgb_formod(jgb_ctx *ctx, int np, const double *time, const double *z, const 
 int jgb_formod_batch(jgb_ctx *ctx, const jgb_batch *b, int precision);
 /* Same with every jgb_batch pointer a device pointer. */
 int jgb_formod_batch_dev(jgb_ctx *ctx, const jgb_batch *b, int precision);
+
+/* Finite-difference Jacobian of every observation of a batch (kernel,
+   jurassic.c:4004-4099).  jgb_kernel_sizes gives per observation the
+   measurement size m (finite rad entries, obs2y order: ray-major, then
+   channel) and the state size n (atm2x order, jurassic.c:29-83, from the
+   RET* windows of the control set).  jgb_kernel_batch writes K_i (m_i x n_i,
+   row-major) of observation i at kmat + sum_{j<i} m_j n_j, and returns the
+   unperturbed forward model in b->rad/tau/tp (and the hydrostatic p) like
+   jgb_formod_batch.  All n_i perturbed forward models of a chunk of
+   observations run as one batched launch sequence.  Host buffers. */
+int jgb_kernel_sizes(jgb_ctx *ctx, const jgb_batch *b, int *m, int *n);
+int jgb_kernel_batch(jgb_ctx *ctx, const jgb_batch *b, double *kmat, int precision);
+
+/* Normal-equation products of the retrieval for nret retrievals of sizes
+   m[i] x n[i] (matrix_product, retrieval.c:403-444, and the gradient
+   K^T W dy of retrieval.c:573-577):  A_i = K_i^T W_i K_i (n_i x n_i) and
+   b_i = K_i^T W_i dy_i with W_i = diag(w_i^2), w = 1/sigma_eps.
+   K, w, dy, A, b are concatenations of the per-retrieval arrays (K_i
+   row-major).  JGB_MIXED: 3xTF32 on the tensor cores (FP32-level
+   accuracy); JGB_FP64: FP64 in the reference's operation order. */
+int jgb_normal_equations(jgb_ctx *ctx, int nret, const int *m, const int *n, const double *K,
+                         const double *w, const double *dy, double *A, double *b,
+                         int precision);
+
+/* Retrieval settings (ret_t, retrieval.c:32-112; read_ret, 753-804). */
+typedef struct {
+  int kernel_recomp, conv_itmax, err_ana;
+  double conv_dmin;
+  const double *err_formod, *err_noise;       /* [nd]: percent, radiance units */
+  double err_press, err_press_cz, err_press_ch;
+  double err_temp, err_temp_cz, err_temp_ch;
+  const double *err_q, *err_q_cz, *err_q_ch;  /* [ng] */
+  const double *err_k, *err_k_cz, *err_k_ch;  /* [nw] */
+  double err_clz, err_cldz;
+  const double *err_clk;                      /* [ncl] */
+  double err_sfz, err_sfp, err_sft;
+  const double *err_sfeps;                    /* [nsf] */
+} jgb_ret;
+
+/* Optimal-estimation retrievals (optimal_estimation, retrieval.c:448-749)
+   of every observation of a batch, advancing in lockstep on the device.
+   In:  b holds the a-priori atmospheres and in b->rad the measurement
+        (NaN = channel not used).
+   Out: x: final state vectors (atm2x of the final atmosphere, sizes n_i of
+        jgb_kernel_sizes, concatenated); b->rad/tau/tp: forward model of the
+        final iterate, b->p its pressure; cov (optional, err_ana): retrieval
+        covariances n_i x n_i concatenated; costs (optional):
+        [nobs][conv_itmax+1] chi^2/m after each iteration (NaN after
+        convergence); iters (optional): iterations done.
+   JGB_MIXED: FP32 forward model and Jacobian, 3xTF32 normal equations;
+   FP64 Cholesky, LM step, cost and convergence test in both modes. */
+int jgb_retrieve_batch(jgb_ctx *ctx, const jgb_ret *ret, const jgb_batch *b, double *x,
+                       double *cov, double *costs, int *iters, int precision);
 
 int jgb_get_stats(const jgb_ctx *ctx, jgb_stats *out);
 

@@ -25,9 +25,11 @@ COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-con
                  "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 UNITS = {
     "jgb_fp64.cu": ["-fmad=false"],
-    "jgb_mixed.cu": [],
+    "jgb_mixed.cu": ["-prec-div=false", "-ftz=true"],
     "jgb_api.cu": [],
     "jgb_noalloc.cu": [],
+    "jgb_normal.cu": ["-fmad=false"],
+    "jgb_retrieval.cu": ["-fmad=false"],
 }
 
 
@@ -83,7 +85,7 @@ def build(force=False, verbose=False, extra=()):
         list(ex.map(run, jobs))
     objs = [os.path.join(BUILD, u.replace(".cu", ".o")) for u in UNITS] + [ctm_obj]
     tmp = LIB + ".%d.tmp" % os.getpid()
-    run([cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
+    run([cc] + ARCH + ["-shared", "-Xlinker", "--no-undefined", "-o", tmp] + objs + ["-lcudart"])
     os.replace(tmp, LIB)
     return LIB
 

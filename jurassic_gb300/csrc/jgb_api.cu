@@ -11,6 +11,7 @@
 #include <cctype>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -18,6 +19,7 @@
 #include "../../include/jurassic_gb300.h"
 #include "jgb_common.cuh"
 #include "jgb_internal.h"
+#include "jgb_ctx.h"
 
 extern "C" const double jgb_continua_blob[];
 extern "C" const long jgb_continua_count;
@@ -25,29 +27,6 @@ extern "C" const long jgb_continua_count;
 using namespace jgb;
 
 namespace {
-
-// Grow-only device buffer.
-struct DevBuf {
-  void* p = nullptr;
-  size_t n = 0;
-  cudaError_t reserve(size_t bytes) {
-    if (bytes <= n) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-    const size_t want = bytes + bytes / 8;  // headroom for slightly larger batches
-    cudaError_t e = cudaMalloc(&p, want);
-    if (e == cudaSuccess) n = want;
-    return e;
-  }
-  template <typename T>
-  T* as() const { return static_cast<T*>(p); }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-  }
-};
 
 // Offsets of the continuum tables inside the blob (order of continua.bin).
 enum { CT_CO2_296 = 0, CT_CO2_260 = 2001, CT_CO2_230 = 4002, CT_H2O_296 = 6003,
@@ -110,35 +89,6 @@ void ctm_coefficients(double nu, double* out) {
 
 }  // namespace
 
-struct jgb_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  CtlDev c{};
-  std::vector<std::string> emitter;
-  std::vector<double> nu, clnu, sfnu, retq_zmin, retq_zmax, retk_zmin, retk_zmax;
-  std::vector<int> window;
-  double retp_zmin = 0, retp_zmax = 0, rett_zmin = 0, rett_zmax = 0;
-  int ret_flags[7] = {0, 0, 0, 0, 0, 0, 0};
-  // device constants
-  DevBuf d_nu, d_window, d_clnu, d_sfnu, d_ctm;
-  // tables
-  int tp = 0, tt = 0, tu = 0;
-  bool tables_init = false;
-  std::vector<int> h_np;
-  DevBuf t_np, t_p, t_nt, t_t, t_nu, t_u, t_eps, t_pf, t_tf;
-  // source function
-  DevBuf s_st, s_sr, s_srf;
-  std::vector<char> src_set;
-  bool srf_stale = true;
-  // per-call scratch
-  DevBuf b_levoff, b_rayoff, b_rayobs, b_lev, b_scal, b_geo, b_rad, b_tau, b_tp, b_mask, b_p;
-  DevBuf los_off, los_cnt, los_cnt64, los_sft, los_ends, los_planes, scan_tmp, err_word;
-  DevBuf tiles_perm, tiles_keys, tiles_keys2, tiles_vals, tiles_off, tiles_len, tiles_data;
-  DevBuf refl;
-  cudaEvent_t ev[8] = {};
-  jgb_stats stats{};
-  std::string err;
-};
 
 namespace {
 
@@ -175,6 +125,7 @@ TblDev tbl_view(const jgb_ctx* x) {
   T.eps = x->t_eps.as<float>();
   T.pf = x->t_pf.as<float>();
   T.tf = x->t_tf.as<float>();
+  T.rowmeta = x->t_meta.as<float4>();
   T.sr = x->s_sr.as<double>();
   T.srf = x->s_srf.as<float>();
   T.st = x->s_st.as<double>();
@@ -233,8 +184,10 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
   return ms;
 }
 
+}  // namespace
+
 // Forward model of a device-resident batch (BatchDev pointers on device).
-int run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
+int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
   cudaStream_t s = x->stream;
   const CtlDev& c = x->c;
   const int nray = b.nray;
@@ -318,6 +271,11 @@ int run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
       launch_src_to_float(c.nd, x->s_sr.as<double>(), x->s_srf.as<float>(), s);
       x->srf_stale = false;
     }
+    if (x->meta_stale) {
+      launch_rowmeta((long long)c.nd * c.ng * x->tp * x->tt, x->tu, x->t_nu.as<int>(),
+                     x->t_u.as<float>(), x->t_eps.as<float>(), x->t_meta.as<float4>(), s);
+      x->meta_stale = false;
+    }
     // tile plan: rays sorted by LOS length, 32 per tile
     const int ntile = (nray + 31) / 32;
     CK(x->tiles_keys.reserve(sizeof(int) * (size_t)nray));
@@ -363,16 +321,42 @@ int run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
       CK(x->refl.reserve(sizeof(float) * 2 * (size_t)cap * c.nd));
       refl = x->refl.as<float>();
     }
+    if (x->path_variant < 0) {
+      // autotune: time every variant on this batch (results are identical)
+      const char* force = getenv("JGB_PATH_VARIANT");
+      if (force) {
+        x->path_variant = atoi(force) % path_mixed_variants();
+      } else {
+        float best = 1e30f;
+        x->tune_ms.clear();
+        for (int v = 0; v < path_mixed_variants(); v++) {
+          CK(cudaEventRecord(x->ev[4], s));
+          launch_path_mixed(c, T, ch, b, L, Pm, refl, v, s);
+          CK(cudaEventRecord(x->ev[5], s));
+          CK(cudaEventSynchronize(x->ev[5]));
+          const float ms = elapsed(x->ev[4], x->ev[5]);
+          x->tune_ms.push_back(ms);
+          if (ms < best) {
+            best = ms;
+            x->path_variant = v;
+          }
+        }
+      }
+    }
     CK(cudaEventRecord(x->ev[4], s));
-    launch_path_mixed(c, T, ch, b, L, Pm, refl, s);
+    launch_path_mixed(c, T, ch, b, L, Pm, refl, x->path_variant, s);
     launches += 6;
   }
   CK(cudaGetLastError());
   CK(cudaEventRecord(x->ev[5], s));
   x->stats.los_points = total;
   x->stats.path_launches = launches;
+  x->stats.path_variant = x->path_variant;
+  for (int v = 0; v < 4; v++) x->stats.tune_ms[v] = v < (int)x->tune_ms.size() ? x->tune_ms[v] : 0.f;
   return JGB_OK;
 }
+
+namespace {
 
 int check_ready(jgb_ctx* x) {
   if (!x->tables_init) return fail(x, JGB_ERR_STATE, "emissivity tables not set");
@@ -381,23 +365,337 @@ int check_ready(jgb_ctx* x) {
   return JGB_OK;
 }
 
+// ---------------------------------------------------------------------------
+// finite-difference Jacobian (kernel, jurassic.c:4004-4099)
+
+__device__ inline int upper_index(const int* off, int n, long long v) {
+  // largest e in [0, n-1] with off[e] <= v
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (off[mid] <= v) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// Copy levels of the source observation into every expanded copy.
+__global__ void k_expand_levels(int ne, const int* eoff, const int* esrc, const int* boff,
+                                int nplanes, long long nlev_b, const double* lb,
+                                long long nlev_e, double* le) {
+  const long long l = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= nlev_e) return;
+  const int e = upper_index(eoff, ne, l);
+  const long long src = boff[esrc[e]] + (l - eoff[e]);
+  for (int k = 0; k < nplanes; k++) le[k * nlev_e + l] = lb[k * nlev_b + src];
+}
+
+// Copy rays (geometry and input mask) and scal records into the copies.
+__global__ void k_expand_rays(int ne, const int* eoff, const int* esrc, const int* boff,
+                              long long nray_b, const double* geo_b, const double* rad_b,
+                              int nd, long long nray_e, double* geo_e, double* rad_e) {
+  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nray_e) return;
+  const int e = upper_index(eoff, ne, r);
+  const long long src = boff[esrc[e]] + (r - eoff[e]);
+  for (int k = 0; k < 7; k++) geo_e[k * nray_e + r] = geo_b[k * nray_b + src];
+  for (int id = 0; id < nd; id++) rad_e[id * nray_e + r] = rad_b[id * nray_b + src];
+}
+
+__global__ void k_expand_scal(int ne, const int* esrc, int nscal, const double* sb, double* se) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  for (int k = 0; k < nscal; k++) se[(long long)e * nscal + k] = sb[(long long)esrc[e] * nscal + k];
+}
+
+// Raise the perturbed element of every copy by the step of kernel().
+// pert[e] = {arr, plane, level-in-copy or scal slot, hkind}.
+__global__ void k_perturb(int ne, const int4* pert, const int* eoff, long long nlev_e, int nscal,
+                          double* le_p, double* le_t, double* le_q, double* le_k, double* se,
+                          double* hout) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const int4 pr = pert[e];
+  double* v;
+  const long long l = (long long)eoff[e] + pr.z;
+  switch (pr.x) {
+    case 0: v = le_p + l; break;
+    case 1: v = le_t + l; break;
+    case 2: v = le_q + pr.y * nlev_e + l; break;
+    case 3: v = le_k + pr.y * nlev_e + l; break;
+    default: v = se + (long long)e * nscal + pr.z; break;
+  }
+  const double x0 = *v;
+  double h;
+  switch (pr.w) {
+    case 0: h = fabs(0.01 * x0) > 1e-7 ? fabs(0.01 * x0) : 1e-7; break;
+    case 2: h = fabs(0.01 * x0) > 1e-15 ? fabs(0.01 * x0) : 1e-15; break;
+    case 1: h = 1.0; break;
+    case 3: h = 1e-4; break;
+    case 4: h = 0.1; break;
+    case 5: h = 10.0; break;
+    default: h = 1e-2; break;
+  }
+  *v = x0 + h;
+  hout[e] = h;
+}
+
+// K[row][col] = (y_col - y0) / h for every observation of the chunk.
+// ymap[row] = (ray within observation, channel); kb: block offsets;
+// e0[i]: first copy of observation i (copy of element col = e0[i] + col).
+__global__ void k_fd(int nobs, const long long* kb, const int* mcount, const int* ncount,
+                     const int* yoff, const int2* ymap, const int* e0, const int* eray,
+                     const double* rad_e, long long nray_e, const int* bray,
+                     const double* rad0, long long nray0, const double* h,
+                     const long long* kdst, double* K) {
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= kb[nobs]) return;
+  int lo = 0, hi = nobs;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (kb[mid] <= g) lo = mid; else hi = mid;
+  }
+  const int i = lo;
+  const long long k = g - kb[i];
+  const int n = ncount[i];
+  const int row = (int)(k / n), col = (int)(k % n);
+  const int2 ym = ymap[yoff[i] + row];
+  const int e = e0[i] + col;
+  const double y1 = rad_e[(long long)ym.y * nray_e + eray[e] + ym.x];
+  const double y0 = rad0[(long long)ym.y * nray0 + bray[i] + ym.x];
+  K[kdst[i] + k] = (y1 - y0) / h[e];
+}
+
 }  // namespace
 
 namespace jgb {
 
 int ctx_view(jgb_ctx* x, CtxView* out) {
   if (!x || !out) return JGB_ERR_ARG;
-  const int rc = check_ready(x);
-  if (rc) return rc;
   out->device = x->device;
   out->stream = x->stream;
   out->c = x->c;
   out->T = tbl_view(x);
   out->ch = chan_view(x);
-  return JGB_OK;
+  return check_ready(x);
 }
 
 int ctx_fail(jgb_ctx* x, int code, const char* msg) { return fail(x, code, msg); }
+int ctx_error(jgb_ctx* x, int code, const std::string& msg) { return fail(x, code, msg); }
+
+}  // namespace jgb
+
+namespace jgb {
+
+void state_layout(const jgb_ctx* x, const double* z, int nl, std::vector<Elem>& out) {
+  const CtlDev& c = x->c;
+  out.clear();
+  for (int ip = 0; ip < nl; ip++)
+    if (z[ip] >= x->retp_zmin && z[ip] <= x->retp_zmax) out.push_back({0, 0, ip, 0});
+  for (int ip = 0; ip < nl; ip++)
+    if (z[ip] >= x->rett_zmin && z[ip] <= x->rett_zmax) out.push_back({1, 0, ip, 1});
+  for (int ig = 0; ig < c.ng; ig++)
+    for (int ip = 0; ip < nl; ip++)
+      if (z[ip] >= x->retq_zmin[ig] && z[ip] <= x->retq_zmax[ig]) out.push_back({2, ig, ip, 2});
+  for (int iw = 0; iw < c.nw; iw++)
+    for (int ip = 0; ip < nl; ip++)
+      if (z[ip] >= x->retk_zmin[iw] && z[ip] <= x->retk_zmax[iw]) out.push_back({3, iw, ip, 3});
+  if (x->ret_flags[0]) out.push_back({4, 0, -1, 1});
+  if (x->ret_flags[1]) out.push_back({4, 1, -1, 1});
+  if (x->ret_flags[2])
+    for (int icl = 0; icl < c.ncl; icl++) out.push_back({4, 2 + icl, -1, 3});
+  const int o = 2 + c.ncl;
+  if (x->ret_flags[3]) out.push_back({4, o, -1, 4});
+  if (x->ret_flags[4]) out.push_back({4, o + 1, -1, 5});
+  if (x->ret_flags[5]) out.push_back({4, o + 2, -1, 1});
+  if (x->ret_flags[6])
+    for (int isf = 0; isf < c.nsf; isf++) out.push_back({4, o + 3 + isf, -1, 6});
+}
+
+void launch_ray_obs_mask(int nobs, const int* ray_off, int* ray_obs, long long n, const double* rad,
+                         unsigned char* mask, cudaStream_t s) {
+  k_ray_obs<<<(nobs + 127) / 128, 128, 0, s>>>(nobs, ray_off, ray_obs);
+  k_mask<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, rad, mask);
+}
+
+int fd_layout(jgb_ctx* x, int nobs, const int* lev_off, const int* ray_off, const double* z,
+              const double* rad_mask, FdLayout& H) {
+  const CtlDev& c = x->c;
+  const int nray = ray_off[nobs];
+  H.nobs = nobs;
+  H.lev_off.assign(lev_off, lev_off + nobs + 1);
+  H.ray_off.assign(ray_off, ray_off + nobs + 1);
+  H.lay.assign(nobs, {});
+  H.mcnt.assign(nobs, 0);
+  H.ncnt.assign(nobs, 0);
+  H.yoff.assign(nobs + 1, 0);
+  H.ymap.clear();
+  H.kb.assign(nobs + 1, 0);
+  for (int i = 0; i < nobs; i++) {
+    state_layout(x, z + lev_off[i], lev_off[i + 1] - lev_off[i], H.lay[i]);
+    H.ncnt[i] = (int)H.lay[i].size();
+    for (int r = ray_off[i]; r < ray_off[i + 1]; r++)
+      for (int id = 0; id < c.nd; id++)
+        if (std::isfinite(rad_mask[(size_t)id * nray + r])) H.ymap.push_back(make_int2(r - ray_off[i], id));
+    H.yoff[i + 1] = (int)H.ymap.size();
+    H.mcnt[i] = H.yoff[i + 1] - H.yoff[i];
+    if (H.ncnt[i] == 0 || H.mcnt[i] == 0) return fail(x, JGB_ERR_ARG, "Check problem definition!");
+    H.kb[i + 1] = H.kb[i] + (long long)H.mcnt[i] * H.ncnt[i];
+  }
+  return JGB_OK;
+}
+
+// Finite-difference Jacobians of the observations in `list` of a device
+// batch: every state element of every listed observation becomes one
+// perturbed copy; chunks of copies (bounded by LOS points) run through the
+// forward model as one batch; K blocks are written at K + H.kb[obs].
+int fd_core(jgb_ctx* x, const FdLayout& H, const FdInput& in, const std::vector<int>& list,
+            double* K, int precision) {
+  const CtlDev& c = x->c;
+  cudaStream_t s = x->stream;
+  const int nscal = 5 + c.ncl + c.nsf;
+  const int nplanes = 6 + c.ng + c.nw;
+  const long long nlev = H.lev_off[H.nobs], nray = H.ray_off[H.nobs];
+  const long long budget = 60000000LL;
+  size_t i0 = 0;
+  while (i0 < list.size()) {
+    long long pts = 0;
+    size_t i1 = i0;
+    while (i1 < list.size()) {
+      const int o = list[i1];
+      long long p_i = 0;
+      for (int r = H.ray_off[o]; r < H.ray_off[o + 1]; r++) p_i += in.cnt[r] + 2;
+      p_i *= H.ncnt[o];
+      if (i1 > i0 && pts + p_i > budget) break;
+      pts += p_i;
+      i1++;
+    }
+    const int nob = (int)(i1 - i0);
+    std::vector<int> eoff_l(1, 0), eoff_r(1, 0), esrc, e0(nob);
+    std::vector<int4> pert;
+    for (size_t q = i0; q < i1; q++) {
+      const int o = list[q];
+      e0[q - i0] = (int)esrc.size();
+      const int nl = H.lev_off[o + 1] - H.lev_off[o];
+      const int nr = H.ray_off[o + 1] - H.ray_off[o];
+      for (const Elem& el : H.lay[o]) {
+        esrc.push_back(o);
+        eoff_l.push_back(eoff_l.back() + nl);
+        eoff_r.push_back(eoff_r.back() + nr);
+        pert.push_back(make_int4(el.arr, el.idx, el.arr == 4 ? el.idx : el.lev, el.hkind));
+      }
+    }
+    const int ne = (int)esrc.size();
+    const long long nlev_e = eoff_l.back(), nray_e = eoff_r.back();
+    CK(x->kx_levoff.reserve(sizeof(int) * (ne + 1)));
+    CK(x->kx_rayoff.reserve(sizeof(int) * (ne + 1)));
+    CK(x->kx_src.reserve(sizeof(int) * ne));
+    CK(x->kx_pert.reserve(sizeof(int4) * ne));
+    CK(x->kx_h.reserve(sizeof(double) * ne));
+    CK(x->kx_lev.reserve(sizeof(double) * (size_t)nlev_e * nplanes));
+    CK(x->kx_scal.reserve(sizeof(double) * (size_t)ne * nscal));
+    CK(x->kx_geo.reserve(sizeof(double) * 7 * (size_t)nray_e));
+    CK(x->kx_tp.reserve(sizeof(double) * ((size_t)c.nd * 2 + 3) * (size_t)nray_e));
+    CK(x->kx_mask.reserve((size_t)c.nd * nray_e));
+    CK(x->kx_rayobs.reserve(sizeof(int) * nray_e));
+    CK(cudaMemcpyAsync(x->kx_levoff.p, eoff_l.data(), sizeof(int) * (ne + 1), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(x->kx_rayoff.p, eoff_r.data(), sizeof(int) * (ne + 1), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(x->kx_src.p, esrc.data(), sizeof(int) * ne, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(x->kx_pert.p, pert.data(), sizeof(int4) * ne, cudaMemcpyHostToDevice, s));
+    double* le = x->kx_lev.as<double>();
+    double* rad_e = x->kx_tp.as<double>();
+    double* tau_e = rad_e + (size_t)c.nd * nray_e;
+    double* tp_e = tau_e + (size_t)c.nd * nray_e;
+    k_expand_levels<<<(unsigned)((nlev_e + 255) / 256), 256, 0, s>>>(
+        ne, x->kx_levoff.as<int>(), x->kx_src.as<int>(), in.lev_off, nplanes, nlev, in.lev, nlev_e, le);
+    k_expand_rays<<<(unsigned)((nray_e + 255) / 256), 256, 0, s>>>(
+        ne, x->kx_rayoff.as<int>(), x->kx_src.as<int>(), in.ray_off, nray, in.geo, in.radmask,
+        c.nd, nray_e, x->kx_geo.as<double>(), rad_e);
+    k_expand_scal<<<(ne + 127) / 128, 128, 0, s>>>(ne, x->kx_src.as<int>(), nscal, in.scal,
+                                                    x->kx_scal.as<double>());
+    k_perturb<<<(ne + 127) / 128, 128, 0, s>>>(ne, x->kx_pert.as<int4>(), x->kx_levoff.as<int>(),
+                                               nlev_e, nscal, le + 4 * nlev_e, le + 5 * nlev_e,
+                                               le + 6 * nlev_e, le + (6 + (size_t)c.ng) * nlev_e,
+                                               x->kx_scal.as<double>(), x->kx_h.as<double>());
+    BatchDev b{};
+    b.nobs = ne;
+    b.nlev = (int)nlev_e;
+    b.nray = (int)nray_e;
+    b.nscal = nscal;
+    b.lev_off = x->kx_levoff.as<int>();
+    b.ray_obs = x->kx_rayobs.as<int>();
+    b.time = le;
+    b.z = le + nlev_e;
+    b.lon = le + 2 * nlev_e;
+    b.lat = le + 3 * nlev_e;
+    b.p = le + 4 * nlev_e;
+    b.t = le + 5 * nlev_e;
+    b.q = le + 6 * nlev_e;
+    b.k = le + (6 + (size_t)c.ng) * nlev_e;
+    b.scal = x->kx_scal.as<double>();
+    b.geo = x->kx_geo.as<double>();
+    b.rad = rad_e;
+    b.tau = tau_e;
+    b.tp = tp_e;
+    b.mask = x->kx_mask.as<unsigned char>();
+    k_ray_obs<<<(ne + 127) / 128, 128, 0, s>>>(ne, x->kx_rayoff.as<int>(), x->kx_rayobs.as<int>());
+    const long long nm = (long long)c.nd * nray_e;
+    k_mask<<<(unsigned)((nm + 255) / 256), 256, 0, s>>>(nm, rad_e, x->kx_mask.as<unsigned char>());
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(x->ev[0], s));
+    int rc = run_core(x, b, precision, false);
+    if (rc) return rc;
+    // finite differences
+    std::vector<long long> kbl(nob + 1, 0), kdst(nob);
+    std::vector<int> mc(nob), nc(nob), yo(nob), bray(nob);
+    for (int q = 0; q < nob; q++) {
+      const int o = list[i0 + q];
+      kbl[q + 1] = kbl[q] + (long long)H.mcnt[o] * H.ncnt[o];
+      kdst[q] = H.kb[o];
+      mc[q] = H.mcnt[o];
+      nc[q] = H.ncnt[o];
+      yo[q] = H.yoff[o];
+      bray[q] = H.ray_off[o];
+    }
+    // bookkeeping arrays carved from one buffer, each 16-byte aligned
+    size_t off = 0;
+    auto carve = [&](size_t bytes) {
+      const size_t o = off;
+      off = (off + bytes + 15) & ~size_t(15);
+      return o;
+    };
+    const size_t o_kb = carve(sizeof(long long) * (nob + 1)), o_kd = carve(sizeof(long long) * nob);
+    const size_t o_mc = carve(sizeof(int) * nob), o_nc = carve(sizeof(int) * nob);
+    const size_t o_yo = carve(sizeof(int) * nob), o_e0 = carve(sizeof(int) * nob);
+    const size_t o_br = carve(sizeof(int) * nob), o_ym = carve(sizeof(int2) * H.ymap.size());
+    CK(x->kx_ymap.reserve(off + 16));
+    char* qp = x->kx_ymap.as<char>();
+    long long* d_kb = reinterpret_cast<long long*>(qp + o_kb);
+    long long* d_kd = reinterpret_cast<long long*>(qp + o_kd);
+    int* d_mc = reinterpret_cast<int*>(qp + o_mc);
+    int* d_nc = reinterpret_cast<int*>(qp + o_nc);
+    int* d_yo = reinterpret_cast<int*>(qp + o_yo);
+    int* d_e0 = reinterpret_cast<int*>(qp + o_e0);
+    int* d_br = reinterpret_cast<int*>(qp + o_br);
+    int2* d_ym = reinterpret_cast<int2*>(qp + o_ym);
+    CK(cudaMemcpyAsync(d_kb, kbl.data(), sizeof(long long) * (nob + 1), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_kd, kdst.data(), sizeof(long long) * nob, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_mc, mc.data(), sizeof(int) * nob, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_nc, nc.data(), sizeof(int) * nob, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_yo, yo.data(), sizeof(int) * nob, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_e0, e0.data(), sizeof(int) * nob, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_br, bray.data(), sizeof(int) * nob, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_ym, H.ymap.data(), sizeof(int2) * H.ymap.size(), cudaMemcpyHostToDevice, s));
+    const long long nk = kbl[nob];
+    k_fd<<<(unsigned)((nk + 255) / 256), 256, 0, s>>>(nob, d_kb, d_mc, d_nc, d_yo, d_ym, d_e0,
+                                                       x->kx_rayoff.as<int>(), rad_e, nray_e,
+                                                       d_br, in.rad0, nray, x->kx_h.as<double>(),
+                                                       d_kd, K);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s));
+    i0 = i1;
+  }
+  return JGB_OK;
+}
 
 }  // namespace jgb
 
@@ -505,12 +803,16 @@ void jgb_destroy(jgb_ctx* x) {
   if (x->stream) cudaStreamSynchronize(x->stream);
   DevBuf* bufs[] = {&x->d_nu, &x->d_window, &x->d_clnu, &x->d_sfnu, &x->d_ctm, &x->t_np,
                     &x->t_p, &x->t_nt, &x->t_t, &x->t_nu, &x->t_u, &x->t_eps, &x->t_pf,
-                    &x->t_tf, &x->s_st, &x->s_sr, &x->s_srf, &x->b_levoff, &x->b_rayoff,
+                    &x->t_tf, &x->t_meta, &x->s_st, &x->s_sr, &x->s_srf, &x->b_levoff, &x->b_rayoff,
                     &x->b_rayobs, &x->b_lev, &x->b_scal, &x->b_geo, &x->b_rad, &x->b_tau,
                     &x->b_tp, &x->b_mask, &x->b_p, &x->los_off, &x->los_cnt, &x->los_cnt64,
                     &x->los_sft, &x->los_ends, &x->los_planes, &x->scan_tmp, &x->err_word,
                     &x->tiles_perm, &x->tiles_keys, &x->tiles_keys2, &x->tiles_vals,
-                    &x->tiles_off, &x->tiles_len, &x->tiles_data, &x->refl};
+                    &x->tiles_off, &x->tiles_len, &x->tiles_data, &x->refl,
+                    &x->kx_levoff, &x->kx_rayoff, &x->kx_rayobs, &x->kx_src, &x->kx_lev,
+                    &x->kx_scal, &x->kx_geo, &x->kx_rad, &x->kx_tau, &x->kx_tp, &x->kx_mask,
+                    &x->kx_pert, &x->kx_h, &x->kx_ymap, &x->kx_K, &x->kx_base_rayoff,
+                    &x->kx_base_levoff};
   for (DevBuf* b : bufs) b->release();
   for (auto& e : x->ev)
     if (e) cudaEventDestroy(e);
@@ -525,6 +827,8 @@ int jgb_tables_init(jgb_ctx* x, int tp, int tt, int tu) {
   cudaSetDevice(x->device);
   const CtlDev& c = x->c;
   const size_t ndg = (size_t)c.nd * c.ng;
+  if ((double)ndg * tp * tt * tu >= 4294967296.0)
+    return fail(x, JGB_ERR_ARG, "emissivity tables larger than 2^32 entries per array");
   x->tp = tp;
   x->tt = tt;
   x->tu = tu;
@@ -538,6 +842,8 @@ int jgb_tables_init(jgb_ctx* x, int tp, int tt, int tu) {
   CK(x->t_eps.reserve(sizeof(float) * std::max<size_t>(ndg * tp * tt * tu, 1)));
   CK(x->t_pf.reserve(sizeof(float) * std::max<size_t>(ndg * tp, 1)));
   CK(x->t_tf.reserve(sizeof(float) * std::max<size_t>(ndg * tp * tt, 1)));
+  CK(x->t_meta.reserve(sizeof(float4) * std::max<size_t>(ndg * tp * tt, 1)));
+  x->meta_stale = true;
   CK(cudaMemcpy(x->t_np.p, x->h_np.data(), sizeof(int) * ndg, cudaMemcpyHostToDevice));
   CK(cudaMemset(x->t_nt.p, 0, sizeof(int) * ndg * tp));
   CK(cudaMemset(x->t_nu.p, 0, sizeof(int) * ndg * tp * tt));
@@ -557,6 +863,7 @@ int jgb_set_table(jgb_ctx* x, int id, int ig, int np, const double* p, const int
   cudaSetDevice(x->device);
   const size_t dg = (size_t)id * c.ng + ig;
   x->h_np[dg] = np;
+  x->meta_stale = true;
   CK(cudaMemcpy(x->t_np.as<int>() + dg, &np, sizeof(int), cudaMemcpyHostToDevice));
   if (np <= 0) return JGB_OK;
   std::vector<int> ntv(x->tp, 0), nuv((size_t)x->tp * x->tt, 0);
@@ -801,6 +1108,70 @@ int jgb_formod(jgb_ctx* x, int np, const double* time, const double* z, const do
   b.tau = tau;
   b.tp = tp;
   return jgb_formod_batch(x, &b, precision);
+}
+
+int jgb_kernel_sizes(jgb_ctx* x, const jgb_batch* hb, int* m, int* n) {
+  if (!x || !hb || !m || !n || hb->nobs <= 0) return fail(x, JGB_ERR_ARG, "bad arguments");
+  const CtlDev& c = x->c;
+  const int nray = hb->ray_off[hb->nobs];
+  std::vector<Elem> el;
+  for (int i = 0; i < hb->nobs; i++) {
+    const int l0 = hb->lev_off[i];
+    state_layout(x, hb->z + l0, hb->lev_off[i + 1] - l0, el);
+    n[i] = (int)el.size();
+    int mm = 0;
+    for (int r = hb->ray_off[i]; r < hb->ray_off[i + 1]; r++)
+      for (int id = 0; id < c.nd; id++) mm += std::isfinite(hb->rad[(size_t)id * nray + r]) ? 1 : 0;
+    m[i] = mm;
+  }
+  return JGB_OK;
+}
+
+int jgb_kernel_batch(jgb_ctx* x, const jgb_batch* hb, double* kmat, int precision) {
+  if (!x || !hb || !kmat || hb->nobs <= 0) return fail(x, JGB_ERR_ARG, "bad arguments");
+  cudaSetDevice(x->device);
+  const CtlDev& c = x->c;
+  const int nobs = hb->nobs;
+  const int nray = hb->ray_off[nobs], nlev = hb->lev_off[nobs];
+  FdLayout H;
+  int rc = fd_layout(x, nobs, hb->lev_off, hb->ray_off, hb->z, hb->rad, H);
+  if (rc) return rc;
+  // keep the caller's mask: the base forward model overwrites rad
+  std::vector<double> rad_in(hb->rad, hb->rad + (size_t)c.nd * nray);
+  // base forward model (also applies hydrostatic equilibrium to p)
+  rc = jgb_formod_batch(x, hb, precision);
+  if (rc) return rc;
+  std::vector<int> cnt(nray);
+  CK(cudaMemcpy(cnt.data(), x->los_cnt.p, sizeof(int) * nray, cudaMemcpyDeviceToHost));
+  // snapshot of the post-hydrostatic base batch (the perturbed runs reuse b_*)
+  const int nscal = 5 + c.ncl + c.nsf, nplanes = 6 + c.ng + c.nw;
+  DevBuf snap;
+  const size_t nb_lev = (size_t)nlev * nplanes, nb_scal = (size_t)nobs * nscal,
+               nb_geo = 7 * (size_t)nray, nb_rad = (size_t)c.nd * nray;
+  CK(snap.reserve(sizeof(double) * (nb_lev + nb_scal + nb_geo + 2 * nb_rad) + sizeof(int) * 2 * (nobs + 1)));
+  double* lev = snap.as<double>();
+  double* scal = lev + nb_lev;
+  double* geo = scal + nb_scal;
+  double* radm = geo + nb_geo;
+  double* rad0 = radm + nb_rad;
+  int* loff = reinterpret_cast<int*>(rad0 + nb_rad);
+  int* roff = loff + nobs + 1;
+  CK(cudaMemcpy(lev, x->b_lev.p, sizeof(double) * nb_lev, cudaMemcpyDeviceToDevice));
+  CK(cudaMemcpy(scal, x->b_scal.p, sizeof(double) * nb_scal, cudaMemcpyDeviceToDevice));
+  CK(cudaMemcpy(geo, x->b_geo.p, sizeof(double) * nb_geo, cudaMemcpyDeviceToDevice));
+  CK(cudaMemcpy(rad0, x->b_rad.p, sizeof(double) * nb_rad, cudaMemcpyDeviceToDevice));
+  CK(cudaMemcpy(radm, rad_in.data(), sizeof(double) * nb_rad, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(loff, hb->lev_off, sizeof(int) * (nobs + 1), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(roff, hb->ray_off, sizeof(int) * (nobs + 1), cudaMemcpyHostToDevice));
+  FdInput in{lev, scal, geo, radm, loff, roff, rad0, cnt.data()};
+  DevBuf kd;
+  CK(kd.reserve(sizeof(double) * (size_t)std::max(H.kb[nobs], 1LL)));
+  std::vector<int> all(nobs);
+  for (int i = 0; i < nobs; i++) all[i] = i;
+  rc = fd_core(x, H, in, all, kd.as<double>(), precision);
+  if (rc) return rc;
+  CK(cudaMemcpy(kmat, kd.p, sizeof(double) * (size_t)H.kb[nobs], cudaMemcpyDeviceToHost));
+  return JGB_OK;
 }
 
 int jgb_get_stats(const jgb_ctx* x, jgb_stats* out) {

@@ -24,6 +24,7 @@ namespace jgb {
 
 struct AtmView {
   int np, ng, nw;
+  bool asc;           // altitude grid strictly ascending
   long long stride;   // level stride of q/k planes (total levels of the batch)
   const double *z, *p, *t, *q, *k;   // q[ig*stride + i], k[iw*stride + i]
   double clz, cldz, sfz, sfp, sft;
@@ -50,12 +51,38 @@ __device__ inline AtmView atm_view(const CtlDev& c, const BatchDev& b, int o) {
   a.sfp = s[3 + c.ncl];
   a.sft = s[4 + c.ncl];
   a.sfeps = s + 5 + c.ncl;
+  a.asc = true;
+  for (int i = 0; i + 1 < a.np; i++)
+    if (!(a.z[i] < a.z[i + 1])) a.asc = false;
   return a;
 }
 
-// intpol_atm (jurassic.c:3685-3706): p (log-linear) and T only.
-__device__ inline int atm_pt(const AtmView& a, double z, double* p, double* t) {
+// Altitude of a Cartesian point: the z of cart2geo (jurassic.c:108-120)
+// without the latitude/longitude, which the reference computes and discards
+// at the refraction sub-points and which the counting pass never needs.
+__device__ inline double z_of(const double* x) {
+  return sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]) - kRE;
+}
+
+// Level bracket with a hint: on a strictly ascending grid the bisection of
+// locate_irr returns the unique i with z[i] <= x < z[i+1] (0 below, n-2
+// above the grid), so a hint that satisfies this is the bisection result.
+__device__ inline int level_of(const AtmView& a, double z, int* hint) {
+  const int h = *hint;
+  if (a.asc && h >= 0 && h <= a.np - 2) {
+    const bool in = a.z[h] <= z && z < a.z[h + 1];
+    const bool below = h == 0 && z < a.z[0];
+    const bool above = h == a.np - 2 && z >= a.z[a.np - 1];
+    if (in || below || above) return h;
+  }
   const int i = bracket_irr(a.z, a.np, z);
+  *hint = i;
+  return i;
+}
+
+// intpol_atm (jurassic.c:3685-3706): p (log-linear) and T only.
+__device__ inline int atm_pt(const AtmView& a, double z, double* p, double* t, int* hint) {
+  const int i = level_of(a, z, hint);
   *p = logy(a.z[i], a.p[i], a.z[i + 1], a.p[i + 1], z);
   *t = lin(a.z[i], a.t[i], a.z[i + 1], a.t[i + 1], z);
   return i;
@@ -73,7 +100,7 @@ __device__ int walk(const CtlDev& c, const ChanDev& ch, const AtmView& a, const 
   const double h = 0.02, zrefrac = 60;
   double ex0[3], ex1[3], x[3], xh[3], xobs[3], xvp[3], ngr[3];
   double z = 1e99, lon = 0, lat = 0, p, t;
-  int stop = 0, n = 0;
+  int stop = 0, n = 0, hint = -1;
   const double obsz = g[1 * nray + r], obslon = g[2 * nray + r], obslat = g[3 * nray + r];
   const double vpz = g[4 * nray + r], vplon = g[5 * nray + r], vplat = g[6 * nray + r];
   double last_z = 0, last_lon = 0, last_lat = 0;
@@ -110,7 +137,7 @@ __device__ int walk(const CtlDev& c, const ChanDev& ch, const AtmView& a, const 
     for (int guard = 0; fabs(dmin - dmax) > 0.001 && guard < 200; guard++) {
       const double d = (dmax + dmin) / 2;
       for (int i = 0; i < 3; i++) x[i] = xobs[i] + d * ex0[i];
-      to_geo(x, &z, &lon, &lat);
+      z = z_of(x);
       if (z <= zmax && z > zmax - 0.001) break;
       if (z < zmax - 0.0005) dmax = d; else dmin = d;
     }
@@ -124,8 +151,18 @@ __device__ int walk(const CtlDev& c, const ChanDev& ch, const AtmView& a, const 
       const double cosa = fabs(ex0[0] * xh[0] + ex0[1] * xh[1] + ex0[2] * xh[2]);
       if (cosa != 0) ds = c.rayds < c.raydz / cosa ? c.rayds : c.raydz / cosa;
     }
-    to_geo(x, &z, &lon, &lat);
+    if (STORE)
+      to_geo(x, &z, &lon, &lat);
+    else
+      z = z_of(x);
     if ((z < zmin || z > zmax) && n > 0) {
+      if (!STORE) {  // the clipped last point ends the count
+        if (n >= cap) {
+          atomicOr(err, kErrLosOverflow);
+          return -1;
+        }
+        return n + 1;
+      }
       stop = (z < zmin ? 2 : 1);
       const double frac = ((z < zmin ? zmin : zmax) - last_z) / (z - last_z);
       to_cart(last_z, last_lon, last_lat, xh);
@@ -138,7 +175,7 @@ __device__ int walk(const CtlDev& c, const ChanDev& ch, const AtmView& a, const 
       atomicOr(err, kErrLosOverflow);
       return -1;
     }
-    const int i = atm_pt(a, z, &p, &t);
+    const int i = atm_pt(a, z, &p, &t, &hint);
     if (STORE) {
       const long long s = base + n;
       L.z[s] = z;
@@ -170,13 +207,13 @@ __device__ int walk(const CtlDev& c, const ChanDev& ch, const AtmView& a, const 
     for (int k = 0; k < 3; k++) ex1[k] = ex0[k] * nref;
     if (bend) {
       for (int k = 0; k < 3; k++) xh[k] = x[k] + 0.5 * ds * ex0[k];
-      to_geo(xh, &z, &lon, &lat);
-      atm_pt(a, z, &p, &t);
+      z = z_of(xh);
+      atm_pt(a, z, &p, &t, &hint);
       nref = JGB_REFRAC(p, t);
       for (int k = 0; k < 3; k++) {
         xh[k] += h;
-        to_geo(xh, &z, &lon, &lat);
-        atm_pt(a, z, &p, &t);
+        z = z_of(xh);
+        atm_pt(a, z, &p, &t, &hint);
         ngr[k] = (JGB_REFRAC(p, t) - nref) / h;
         xh[k] -= h;
       }

@@ -32,11 +32,14 @@ struct MixedPlan {
 int mixed_nfield(const CtlDev& c);
 void launch_pack_tiles_n(const CtlDev& c, const LosDev& L, const MixedPlan& P,
                          long long total_tile_points, cudaStream_t s);
+int path_mixed_variants();
 void launch_path_mixed(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
-                       const LosDev& L, const MixedPlan& P, float* refl_scratch,
+                       const LosDev& L, const MixedPlan& P, float* refl_scratch, int variant,
                        cudaStream_t s);
 void launch_src_to_float(int nd, const double* sr, float* srf, cudaStream_t s);
 void launch_tables_to_float(long long n, const double* src, float* dst, cudaStream_t s);
+void launch_rowmeta(long long nrow, int tu, const int* nu, const float* u, const float* e,
+                    float4* meta, cudaStream_t s);
 
 // jgb_api.cu: read-only view of a context for entry points defined in other
 // translation units.  Returns JGB_OK, or an error code with the context's
@@ -48,7 +51,13 @@ struct CtxView {
   TblDev T;
   ChanDev ch;
 };
-int ctx_view(jgb_ctx* x, CtxView* out);
+int ctx_view(jgb_ctx* x, CtxView* out);  // fills *out; returns JGB_ERR_STATE if not ready
+
+// jgb_normal.cu: batched normal-equation products on device buffers
+int normal_equations_dev(int nret, const int* m, const int* n, const double* K, const double* w,
+                         const double* dy, double* A, double* b, int precision, void* desc_dev,
+                         cudaStream_t s);
+size_t normal_desc_bytes(int nret);
 int ctx_fail(jgb_ctx* x, int code, const char* msg);
 
 }  // namespace jgb

@@ -81,25 +81,42 @@ __global__ void k_pack_tiles(CtlDev c, LosDev L, MixedPlan P, long long total) {
 }
 
 // ---------------------------------------------------------------------------
-// float table access
+// float table access with hinted searches
+//
+// Along a path the column density of every (channel, emitter) only grows
+// and pressure/temperature change slowly, so the bracket found at one LOS
+// point is almost always the bracket (or its neighbour) at the next point.
+// Each search therefore first tests the remembered bracket and the next one
+// with independent loads (one round trip) and falls back to bisection
+// only on a miss.  Any valid bracket gives the same interpolated value, so
+// the result does not depend on the hint.
 
 struct RowF {
   const float* u;
   const float* e;
   int n;
+  float u0, un, e0, en;  // first/last entries of the row (one 16-byte load)
 };
 
+// 32-bit row arithmetic (the table upload checks that rows x TU < 2^32)
 __device__ __forceinline__ RowF rowf_at(const TblDev& T, long long dg, int ip, int it) {
-  const long long r = (dg * T.tp + ip) * T.tt + it;
+  const unsigned r = ((unsigned)dg * (unsigned)T.tp + (unsigned)ip) * (unsigned)T.tt + (unsigned)it;
   RowF w;
-  w.u = T.u + r * T.tu;
-  w.e = T.eps + r * T.tu;
+  const size_t off = (size_t)(r * (unsigned)T.tu);
+  w.u = T.u + off;
+  w.e = T.eps + off;
   w.n = __ldg(T.nu + r);
+  const float4 m = __ldg(T.rowmeta + r);
+  w.u0 = m.x;
+  w.un = m.y;
+  w.e0 = m.z;
+  w.en = m.w;
   return w;
 }
 
-__device__ __forceinline__ int bracket_rowf(const float* g, int n, float x) {
-  int lo = 0, hi = n - 1;
+// Largest i in [lo, hi-1] with g[i] <= x, given g[lo] <= x and
+// (g[hi] > x or hi == n-1).
+__device__ __forceinline__ int bisect_f(const float* g, int lo, int hi, float x) {
   while (hi > lo + 1) {
     const int mid = (lo + hi) >> 1;
     if (__ldg(g + mid) > x) hi = mid; else lo = mid;
@@ -107,29 +124,45 @@ __device__ __forceinline__ int bracket_rowf(const float* g, int n, float x) {
   return lo;
 }
 
-// Emissivity at column u (intpol_tbl_eps) in float.
-__device__ __forceinline__ float rowf_eps(const RowF& r, float u) {
-  const float u0 = __ldg(r.u), un = __ldg(r.u + r.n - 1);
-  if (u < u0) return __ldg(r.e) / u0 * u;
-  if (u > un) {
-    const float a = log1pf(-__ldg(r.e + r.n - 1)) / un;
+// Bracket of x on an ascending row of n entries with g[0] <= x <= g[n-1],
+// starting from hint h (locate_tbl semantics, jurassic.c:4152-4170).
+__device__ __forceinline__ int hunt_f(const float* g, int n, float x, int h) {
+  h = h < 0 ? 0 : (h > n - 2 ? n - 2 : h);
+  const float a = __ldg(g + h), b = __ldg(g + h + 1);
+  const float c = (h + 2 <= n - 1) ? __ldg(g + h + 2) : b;
+  if (a <= x) {
+    if (x < b) return h;
+    if (h + 1 >= n - 1) return n - 2;
+    if (x < c) return h + 1;
+    if (h + 2 >= n - 1) return n - 2;
+    return bisect_f(g, h + 2, n - 1, x);
+  }
+  return bisect_f(g, 0, h, x);
+}
+
+// Emissivity at column u (intpol_tbl_eps) in float; *hint holds the bracket.
+__device__ __forceinline__ float rowf_eps(const RowF& r, float u, int* hint) {
+  if (u < r.u0) return r.e0 / r.u0 * u;
+  if (u > r.un) {
+    const float a = log1pf(-r.en) / r.un;
     return -expm1f(a * u);
   }
-  const int i = bracket_rowf(r.u, r.n, u);
+  const int i = hunt_f(r.u, r.n, u, *hint);
+  *hint = i;
   const float xa = __ldg(r.u + i), xb = __ldg(r.u + i + 1);
   const float ya = __ldg(r.e + i), yb = __ldg(r.e + i + 1);
   return ya + (yb - ya) / (xb - xa) * (u - xa);
 }
 
-// Column at emissivity e (intpol_tbl_u) in float.
-__device__ __forceinline__ float rowf_u(const RowF& r, float e) {
-  const float e0 = __ldg(r.e), en = __ldg(r.e + r.n - 1);
-  if (e < e0) return __ldg(r.u) / e0 * e;
-  if (e > en) {
-    const float a = log1pf(-en) / __ldg(r.u + r.n - 1);
+// Column at emissivity e (intpol_tbl_u) in float; *hint holds the bracket.
+__device__ __forceinline__ float rowf_u(const RowF& r, float e, int* hint) {
+  if (e < r.e0) return r.u0 / r.e0 * e;
+  if (e > r.en) {
+    const float a = log1pf(-r.en) / r.un;
     return log1pf(-e) / a;
   }
-  const int i = bracket_rowf(r.e, r.n, e);
+  const int i = hunt_f(r.e, r.n, e, *hint);
+  *hint = i;
   const float xa = __ldg(r.e + i), xb = __ldg(r.e + i + 1);
   const float ya = __ldg(r.u + i), yb = __ldg(r.u + i + 1);
   return ya + (yb - ya) / (xb - xa) * (e - xa);
@@ -153,14 +186,33 @@ __device__ __forceinline__ int bracket_irrf(const float* g, int n, float x) {
   return lo;
 }
 
-// Path state of one (channel, emitter): transmittance t and emissivity e.
+// Pressure bracket with a hint: keeps ipr while p lies inside its interval
+// (or beyond the grid end it is clamped to), else bisects.
+__device__ __forceinline__ int pbracket_f(const float* g, int n, float x, int ipr) {
+  if (ipr >= 0) {
+    const float a = __ldg(g + ipr), b = __ldg(g + ipr + 1);
+    const float lo = fminf(a, b), hi = fmaxf(a, b);
+    const bool low_end = (ipr == 0) && ((a < b) ? (x < a) : (x > a));
+    const bool high_end = (ipr == n - 2) && ((a < b) ? (x >= b) : (x <= b));
+    if ((x >= lo && x < hi) || low_end || high_end) return ipr;
+  }
+  return bracket_irrf(g, n, x);
+}
+
+constexpr int kStateWords = 7;  // t, e, ipr, 2 words of u hints, 2 of eps hints
+
+// Per (channel, emitter) state carried along the path: transmittance t and
+// emissivity e of the extended path (each accurate where it is small), the
+// pressure bracket and the search hints of the four table corners (16 bit).
 struct GasState {
   float t, e;
+  int ipr;
+  unsigned short hu[4], he[4];
 };
 
-// One (channel, emitter) at one LOS point.  Returns the segment emissivity
-// and updates the path state; *sat is set where the reference's segment
-// transmittance becomes zero (emissivity exactly one).
+// One (channel, emitter) at one LOS point (intpol_tbl_ega / intpol_tbl_cga,
+// jurassic.c:3710-3891).  Returns the segment emissivity; *sat is set where
+// the reference's segment transmittance becomes zero.
 __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, bool cga, float pq,
                                            float tq, float du, float ucg, GasState& s,
                                            bool& sat) {
@@ -174,7 +226,10 @@ __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, bool c
   }
   const float* pg = T.pf + dg * T.tp;
   const int* ntg = T.nt + dg * T.tp;
-  const int ipr = bracket_irrf(pg, np, pq);
+  const int ipr = pbracket_f(pg, np, pq, s.ipr);
+  if (ipr != s.ipr) {
+    s.ipr = ipr;
+  }
   const int nt0 = __ldg(ntg + ipr), nt1 = __ldg(ntg + ipr + 1);
   if (nt0 < 2 || nt1 < 2) return 0.f;
   const float* t0g = T.tf + (dg * T.tp + ipr) * T.tt;
@@ -184,18 +239,17 @@ __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, bool c
   const RowF r00 = rowf_at(T, dg, ipr, it0), r01 = rowf_at(T, dg, ipr, it0 + 1);
   const RowF r10 = rowf_at(T, dg, ipr + 1, it1), r11 = rowf_at(T, dg, ipr + 1, it1 + 1);
   if (r00.n < 2 || r01.n < 2 || r10.n < 2 || r11.n < 2) return 0.f;
-  float e00, e01, e10, e11;
-  if (cga) {
-    e00 = rowf_eps(r00, ucg);
-    e01 = rowf_eps(r01, ucg);
-    e10 = rowf_eps(r10, ucg);
-    e11 = rowf_eps(r11, ucg);
-  } else {
-    e00 = rowf_eps(r00, rowf_u(r00, s.e) + du);
-    e01 = rowf_eps(r01, rowf_u(r01, s.e) + du);
-    e10 = rowf_eps(r10, rowf_u(r10, s.e) + du);
-    e11 = rowf_eps(r11, rowf_u(r11, s.e) + du);
+  float ec[4];
+  const RowF* rows[4] = {&r00, &r01, &r10, &r11};
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    int hu = s.hu[k], he = s.he[k];
+    const float uq = cga ? ucg : rowf_u(*rows[k], s.e, &he) + du;
+    ec[k] = rowf_eps(*rows[k], uq, &hu);
+    s.hu[k] = (unsigned short)hu;
+    s.he[k] = (unsigned short)he;
   }
+  const float e00 = ec[0], e01 = ec[1], e10 = ec[2], e11 = ec[3];
   const float ta = __ldg(t0g + it0), tb = __ldg(t0g + it0 + 1);
   const float tc = __ldg(t1g + it1), td = __ldg(t1g + it1 + 1);
   const float ea = e00 + (e01 - e00) / (tb - ta) * (tq - ta);
@@ -208,21 +262,26 @@ __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, bool c
     w = (pq - pa) / (pb - pa);
   float e = ea + (eb - ea) * w;
   e = fminf(fmaxf(e, 0.f), 1.f);
-  // transmittance of the extended path; 1 - e is exact for e >= 0.5
-  const float te = 1.f - e;
-  float eps;
-  if (s.e < 0.5f)
-    eps = (e - s.e) / s.t;
-  else
-    eps = 1.f - te / s.t;
+  const float te = 1.f - e;  // exact for e >= 0.5
+  const float eps = (s.e < 0.5f) ? (e - s.e) / s.t : 1.f - te / s.t;
   if (e >= 1.f) sat = true;
   s.t = te;
   s.e = e;
   return eps;
 }
 
-__global__ void __launch_bounds__(128) k_path_mixed(CtlDev c, TblDev T, ChanDev ch, BatchDev b,
-                                                    LosDev L, MixedPlan P, float* refl) {
+// The emitter loop runs over a runtime count with the per-emitter state in
+// shared memory: unrolling it over the emitters multiplies the code size
+// beyond the instruction cache and the register count beyond what keeps
+// enough warps resident to hide load latency, and thread-local arrays spill
+// through L1 into L2.
+// MINB is the minimum number of resident blocks per SM requested from the
+// register allocator (1 = no cap); the variants are chosen by the autotuner.
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, ChanDev ch,
+                                                          BatchDev b, LosDev L, MixedPlan P,
+                                                          float* refl) {
+  const int ng = c.ng;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int nchb = (c.nd + 3) / 4;
@@ -267,26 +326,68 @@ __global__ void __launch_bounds__(128) k_path_mixed(CtlDev c, TblDev T, ChanDev 
   const float* srf = T.srf + (long long)id * kNS;
   const float st0 = (float)kTMIN, sdt = (float)((kTMAX - kTMIN) / (kNS - 1.0));
 
-  GasState gs[kMaxG];
-  for (int g = 0; g < c.ng; g++) gs[g] = GasState{1.f, 0.f};
+  // per-emitter path state in shared memory, word-major per thread:
+  // sh[(g * kStateWords + w) * blockDim.x + threadIdx.x]
+  extern __shared__ unsigned sh_state[];
+  const int nth = blockDim.x, tid = threadIdx.x;
+  auto sload = [&](int g) {
+    const unsigned* q = sh_state + (g * kStateWords) * nth + tid;
+    GasState st;
+    st.t = __uint_as_float(q[0]);
+    st.e = __uint_as_float(q[nth]);
+    st.ipr = (int)q[2 * nth];
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      const unsigned hu = q[(3 + k) * nth], he = q[(5 + k) * nth];
+      st.hu[2 * k] = (unsigned short)(hu & 0xffffu);
+      st.hu[2 * k + 1] = (unsigned short)(hu >> 16);
+      st.he[2 * k] = (unsigned short)(he & 0xffffu);
+      st.he[2 * k + 1] = (unsigned short)(he >> 16);
+    }
+    return st;
+  };
+  auto sstore = [&](int g, const GasState& st) {
+    unsigned* q = sh_state + (g * kStateWords) * nth + tid;
+    q[0] = __float_as_uint(st.t);
+    q[nth] = __float_as_uint(st.e);
+    q[2 * nth] = (unsigned)st.ipr;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      q[(3 + k) * nth] = (unsigned)st.hu[2 * k] | ((unsigned)st.hu[2 * k + 1] << 16);
+      q[(5 + k) * nth] = (unsigned)st.he[2 * k] | ((unsigned)st.he[2 * k + 1] << 16);
+    }
+  };
+  for (int g = 0; g < ng; g++) {
+    GasState st;
+    st.t = 1.f;
+    st.e = 0.f;
+    st.ipr = -1;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      st.hu[k] = 0;
+      st.he[k] = 0;
+    }
+    sstore(g, st);
+  }
   float rad = 0.f, comp = 0.f, tau = 1.f;
   const bool do_refl = refl != nullptr && r >= 0 && c.sftype >= 2 && sfeps < 1.f && L.sft[r] > 0;
   float* sc = do_refl ? refl + 2 * (L.off[r] * c.nd) : nullptr;
+  const long long dg0 = (long long)id * ng;
 
-  const int len = P.tlen[tile];
-  for (int ip = 0; ip < len; ip++) {
-    if (ip >= n) break;
+  for (int ip = 0; ip < n; ip++) {
     const float* f = base + (long long)ip * F.n * 32;
     const float p = f[F.p * 32], t = f[F.t * 32], ds = f[F.ds * 32];
     float E = 0.f;
     bool sat = false;
-    for (int g = 0; g < c.ng; g++) {
-      const long long dg = (long long)id * c.ng + g;
+#pragma unroll 1
+    for (int g = 0; g < ng; g++) {
       const float du = cga ? 0.f : f[(F.u0 + g) * 32];
       const float pq = cga ? f[(F.cgp0 + g) * 32] : p;
       const float tq = cga ? f[(F.cgt0 + g) * 32] : t;
       const float ucg = cga ? f[(F.cgu0 + g) * 32] : 0.f;
-      const float eg = gas_eps_f(T, dg, cga, pq, tq, du, ucg, gs[g], sat);
+      GasState st = sload(g);
+      const float eg = gas_eps_f(T, dg0 + g, cga, pq, tq, du, ucg, st, sat);
+      sstore(g, st);
       E = E + (1.f - E) * eg;
     }
     // extinction and continua
@@ -359,7 +460,7 @@ __global__ void __launch_bounds__(128) k_path_mixed(CtlDev c, TblDev T, ChanDev 
       radd += acc * (double)tau * (double)(1.f - sfeps);
       if (c.sftype >= 3) {
         const double* e6 = L.ends + 6LL * r;
-        // solar zenith angle and incidence (double, once per ray and channel)
+        // solar zenith angle (sza, jurassic.c:5183-5219) and incidence
         const double d = b.geo[r] / 86400 - 0.5;
         const double g = (357.529 + 0.98560028 * d) * (kPI / 180.0);
         const double qq = 280.459 + 0.98564736 * d;
@@ -393,6 +494,28 @@ __global__ void __launch_bounds__(128) k_path_mixed(CtlDev c, TblDev T, ChanDev 
   b.tau[oi] = (double)tau;
 }
 
+// First and last entries of every table row in one float4 (rows with fewer
+// than two entries are never interpolated and get zeros).
+__global__ void k_rowmeta(long long nrow, int tu, const int* nu, const float* u, const float* e,
+                          float4* meta) {
+  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrow) return;
+  const int n = nu[r];
+  float4 m = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (n >= 2) {
+    const float* ur = u + r * tu;
+    const float* er = e + r * tu;
+    m = make_float4(ur[0], ur[n - 1], er[0], er[n - 1]);
+  }
+  meta[r] = m;
+}
+
+void launch_rowmeta(long long nrow, int tu, const int* nu, const float* u, const float* e,
+                    float4* meta, cudaStream_t s) {
+  const int bs = 256;
+  if (nrow > 0) k_rowmeta<<<(unsigned)((nrow + bs - 1) / bs), bs, 0, s>>>(nrow, tu, nu, u, e, meta);
+}
+
 __global__ void k_src_to_float(int nd, const double* sr, float* srf) {
   const int gid = blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= nd * kNS) return;
@@ -412,12 +535,26 @@ void launch_pack_tiles_n(const CtlDev& c, const LosDev& L, const MixedPlan& P,
   k_pack_tiles<<<(unsigned)((nth + bs - 1) / bs), bs, 0, s>>>(c, L, P, total_tile_points);
 }
 
+int path_mixed_variants() { return 4; }
+
 void launch_path_mixed(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
-                       const LosDev& L, const MixedPlan& P, float* refl_scratch,
+                       const LosDev& L, const MixedPlan& P, float* refl_scratch, int variant,
                        cudaStream_t s) {
   const int nchb = (c.nd + 3) / 4;
-  const long long nblk = (long long)P.ntile * nchb;
-  k_path_mixed<<<(unsigned)nblk, 128, 0, s>>>(c, T, ch, b, L, P, refl_scratch);
+  const unsigned nblk = (unsigned)((long long)P.ntile * nchb);
+  const size_t smem = sizeof(unsigned) * kStateWords * 128 * (size_t)(c.ng > 0 ? c.ng : 1);
+  if (smem > 48 * 1024) {  // more than 13 emitters: opt in to the larger shared memory
+    cudaFuncSetAttribute(k_path_mixed<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_path_mixed<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_path_mixed<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_path_mixed<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  }
+  switch (variant) {
+    case 1: k_path_mixed<5><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl_scratch); break;
+    case 2: k_path_mixed<6><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl_scratch); break;
+    case 3: k_path_mixed<4><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl_scratch); break;
+    default: k_path_mixed<1><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl_scratch); break;
+  }
 }
 
 void launch_src_to_float(int nd, const double* sr, float* srf, cudaStream_t s) {

@@ -55,14 +55,29 @@ class _Batch(C.Structure):
                 ("ray_off", _ip), ("geo", _dp), ("rad", _dp), ("tau", _dp), ("tp", _dp)]
 
 
+class _Ret(C.Structure):
+    _fields_ = [("kernel_recomp", C.c_int), ("conv_itmax", C.c_int), ("err_ana", C.c_int),
+                ("conv_dmin", C.c_double), ("err_formod", _dp), ("err_noise", _dp),
+                ("err_press", C.c_double), ("err_press_cz", C.c_double),
+                ("err_press_ch", C.c_double), ("err_temp", C.c_double),
+                ("err_temp_cz", C.c_double), ("err_temp_ch", C.c_double),
+                ("err_q", _dp), ("err_q_cz", _dp), ("err_q_ch", _dp), ("err_k", _dp),
+                ("err_k_cz", _dp), ("err_k_ch", _dp), ("err_clz", C.c_double),
+                ("err_cldz", C.c_double), ("err_clk", _dp), ("err_sfz", C.c_double),
+                ("err_sfp", C.c_double), ("err_sft", C.c_double), ("err_sfeps", _dp)]
+
+
 class Stats(C.Structure):
     _fields_ = [("h2d_ms", C.c_double), ("hydro_ms", C.c_double), ("trace_ms", C.c_double),
                 ("pack_ms", C.c_double), ("path_ms", C.c_double), ("d2h_ms", C.c_double),
                 ("total_ms", C.c_double), ("los_points", C.c_longlong),
-                ("path_launches", C.c_int)]
+                ("path_launches", C.c_int), ("path_variant", C.c_int),
+                ("tune_ms", C.c_float * 4)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["tune_ms"] = list(self.tune_ms)
+        return d
 
 
 # exported symbols and their signatures (the contract of include/jurassic_gb300.h)
@@ -80,6 +95,12 @@ SIGNATURES = {
                              C.c_int, _dp, _dp, _dp, _dp, C.c_int]),
     "jgb_formod_batch": (C.c_int, [C.c_void_p, C.POINTER(_Batch), C.c_int]),
     "jgb_formod_batch_dev": (C.c_int, [C.c_void_p, C.POINTER(_Batch), C.c_int]),
+    "jgb_kernel_sizes": (C.c_int, [C.c_void_p, C.POINTER(_Batch), _ip, _ip]),
+    "jgb_kernel_batch": (C.c_int, [C.c_void_p, C.POINTER(_Batch), _dp, C.c_int]),
+    "jgb_normal_equations": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _dp, _dp, _dp, _dp, _dp,
+                                       C.c_int]),
+    "jgb_retrieve_batch": (C.c_int, [C.c_void_p, C.POINTER(_Ret), C.POINTER(_Batch), _dp, _dp,
+                                     _dp, _ip, C.c_int]),
     "jgb_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "jgb_formod_batch_dev_noalloc": (C.c_int, [C.c_void_p, C.POINTER(_Batch)]),
     "jgb_host_alloc": (C.c_void_p, [C.c_ulonglong]),
@@ -249,3 +270,104 @@ class Context:
                                  for k, v in ptrs.items()})
         fn = load().jgb_formod_batch_dev if device else load().jgb_formod_batch
         self._check(fn(self.h, C.byref(s), precision))
+
+    # --------------------------------------------------------------
+    def _batch_struct(self, b):
+        arr = {k: _d(getattr(b, k)) for k in ("time", "z", "lon", "lat", "p", "t", "q", "k",
+                                               "scal", "geo", "rad", "tau", "tp")}
+        lev = np.ascontiguousarray(b.lev_off, np.int32)
+        ray = np.ascontiguousarray(b.ray_off, np.int32)
+        s = _Batch(nobs=b.nobs, lev_off=_p(lev, _ip), ray_off=_p(ray, _ip),
+                   **{k: _p(v) for k, v in arr.items()})
+        return s, arr, (lev, ray)
+
+    def kernel_sizes(self, batch):
+        s, arr, keep = self._batch_struct(batch)
+        m = np.zeros(batch.nobs, np.int32)
+        n = np.zeros(batch.nobs, np.int32)
+        self._check(load().jgb_kernel_sizes(self.h, C.byref(s), _p(m, _ip), _p(n, _ip)))
+        return m, n
+
+    def kernel_batch(self, batch, precision: int = FP64):
+        """Finite-difference Jacobians of every observation (kernel,
+        src/jurassic.c:4004-4099).  Returns (list of K_i [m_i, n_i], Batch with
+        the unperturbed forward model)."""
+        m, n = self.kernel_sizes(batch)
+        b = batch.copy()
+        s, arr, keep = self._batch_struct(b)
+        kmat = np.zeros(int(np.sum(m.astype(np.int64) * n)))
+        self._check(load().jgb_kernel_batch(self.h, C.byref(s), _p(kmat), precision))
+        for k in ("rad", "tau", "tp", "p"):
+            setattr(b, k, arr[k])
+        out, o = [], 0
+        for mi, ni in zip(m, n):
+            out.append(kmat[o:o + mi * ni].reshape(mi, ni))
+            o += mi * ni
+        return out, b
+
+    def kernel(self, atm: Atm, obs: Obs, precision: int = FP64):
+        """Jacobian of one observation (the reference kernel())."""
+        from .synth import pack
+        K, b = self.kernel_batch(pack(self.ctl, [(atm, obs)]), precision)
+        return K[0]
+
+    def normal_equations(self, Ks, ws, dys, precision: int = MIXED):
+        """A_i = K_i^T diag(w_i^2) K_i and b_i = K_i^T diag(w_i^2) dy_i for
+        lists of K_i [m_i, n_i], w_i [m_i], dy_i [m_i]."""
+        m = np.array([k.shape[0] for k in Ks], np.int32)
+        n = np.array([k.shape[1] for k in Ks], np.int32)
+        K = _d(np.concatenate([np.ravel(k) for k in Ks]))
+        w = _d(np.concatenate(ws))
+        dy = _d(np.concatenate(dys))
+        A = np.zeros(int(np.sum(n.astype(np.int64) ** 2)))
+        b = np.zeros(int(np.sum(n)))
+        self._check(load().jgb_normal_equations(self.h, len(Ks), _p(m, _ip), _p(n, _ip), _p(K),
+                                                _p(w), _p(dy), _p(A), _p(b), precision))
+        outA, outb, oa, ob = [], [], 0, 0
+        for ni in n:
+            outA.append(A[oa:oa + ni * ni].reshape(ni, ni))
+            outb.append(b[ob:ob + ni])
+            oa += ni * ni
+            ob += ni
+        return outA, outb
+
+    def retrieve_batch(self, ret, batch, precision: int = FP64):
+        """Optimal-estimation retrievals (optimal_estimation,
+        src/retrieval.c:448-749) of every observation of a batch: the batch
+        holds the a-priori atmospheres and, in rad, the measurements.
+        Returns dict(x=[state vectors], cov=[covariances or None],
+        costs=[chi^2/m histories], iters=[...], batch=final forward model)."""
+        ctl = self.ctl
+        r = ret.sized(ctl)
+        keep = {k: _d(getattr(r, k)) for k in ("err_formod", "err_noise", "err_q", "err_q_cz",
+                                                "err_q_ch", "err_k", "err_k_cz", "err_k_ch",
+                                                "err_clk", "err_sfeps")}
+        sr = _Ret(kernel_recomp=r.kernel_recomp, conv_itmax=r.conv_itmax, err_ana=r.err_ana,
+                  conv_dmin=r.conv_dmin, err_press=r.err_press, err_press_cz=r.err_press_cz,
+                  err_press_ch=r.err_press_ch, err_temp=r.err_temp, err_temp_cz=r.err_temp_cz,
+                  err_temp_ch=r.err_temp_ch, err_clz=r.err_clz, err_cldz=r.err_cldz,
+                  err_sfz=r.err_sfz, err_sfp=r.err_sfp, err_sft=r.err_sft,
+                  **{k: _p(v) for k, v in keep.items()})
+        m, n = self.kernel_sizes(batch)
+        b = batch.copy()
+        s, arr, ks = self._batch_struct(b)
+        nx = int(np.sum(n))
+        x = np.zeros(nx)
+        cov = np.zeros(int(np.sum(n.astype(np.int64) ** 2))) if r.err_ana else None
+        ncost = r.conv_itmax + 1
+        costs = np.zeros(b.nobs * ncost)
+        iters = np.zeros(b.nobs, np.int32)
+        self._check(load().jgb_retrieve_batch(self.h, C.byref(sr), C.byref(s), _p(x),
+                                              _p(cov) if cov is not None else None, _p(costs),
+                                              _p(iters, _ip), precision))
+        for k in ("rad", "tau", "tp", "p"):
+            setattr(b, k, arr[k])
+        xs, covs, ox, oc = [], [], 0, 0
+        for ni in n:
+            xs.append(x[ox:ox + ni])
+            covs.append(cov[oc:oc + ni * ni].reshape(ni, ni) if cov is not None else None)
+            ox += ni
+            oc += ni * ni
+        cs = costs.reshape(b.nobs, ncost)
+        return dict(x=xs, cov=covs, costs=[c[np.isfinite(c)] for c in cs],
+                    iters=iters.tolist(), batch=b)

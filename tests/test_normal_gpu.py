@@ -1,0 +1,45 @@
+"""Normal-equation products A = K^T W K, b = K^T W dy (matrix_product,
+retrieval.c:403-444; gradient, retrieval.c:573-577) on the GPU.
+
+3xTF32 tensor-core path: |A - A_ref| <= 1e-5 sqrt(A_ii A_jj) (FP32 accumulation over m rows, m 2^-24; the
+inputs are recovered to FP32 by 3xTF32); b within 1e-5 of sqrt(A_jj * dy^T W dy).
+FP64 path: relative 1e-12 against numpy.
+"""
+import numpy as np
+import pytest
+
+from jurassic_gb300 import native, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _ref(K, w, dy):
+    X = K * w[:, None]
+    return X.T @ X, K.T @ (dy * w * w)
+
+
+def _ctx():
+    w = synth.config_limb_ega(n_rays=1)
+    return native.Context(w.ctl)   # no tables needed for these products
+
+
+@pytest.mark.parametrize("prec", [native.MIXED, native.FP64])
+def test_normal_equations_uneven_batch(built_lib, prec):
+    rng = np.random.default_rng(7)
+    sizes = [(150, 405), (37, 64), (300, 129), (1, 1), (65, 63)]
+    Ks = [rng.standard_normal((m, n)) * np.exp(rng.uniform(-3, 3, n))[None, :] for m, n in sizes]
+    ws = [np.exp(rng.uniform(-1, 1, m)) for m, _ in sizes]
+    dys = [rng.standard_normal(m) for m, _ in sizes]
+    ctx = _ctx()
+    As, bs = ctx.normal_equations(Ks, ws, dys, prec)
+    for K, w, dy, A, b in zip(Ks, ws, dys, As, bs):
+        Ar, br = _ref(K, w, dy)
+        d = np.sqrt(np.diag(Ar))
+        if prec == native.MIXED:
+            assert np.max(np.abs(A - Ar) / np.outer(d, d)) <= 1e-5
+            sdy = np.sqrt(np.sum((dy * w) ** 2))
+            assert np.max(np.abs(b - br) / (d * sdy)) <= 1e-5
+        else:
+            assert np.max(np.abs(A - Ar) / np.outer(d, d)) <= 1e-12
+            assert np.allclose(b, br, rtol=1e-10, atol=1e-12 * np.max(np.abs(br)))
+        assert np.array_equal(A, A.T)
