@@ -201,6 +201,72 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def serving_workload(seed=5):
+    """Retrieval serving stream: a 300-channel context (650-2400 cm^-1,
+    CO2 + H2O + O3), requests with 50-300 measured channels, 41-101 levels
+    on 0-100 km, nadir (1 ray) and limb (5 rays) alternating; T retrieved on
+    0-60 km and H2O on 0-20 km; diagonal S_a (2 K, 30 %, 3 km vertical
+    correlation length without a horizontal one, so no correlation,
+    retrieval.c:901), up to 10 LM iterations, kernel recomputed every
+    iteration, covariance and averaging-kernel analysis on."""
+    from jurassic_gb300 import synth
+    from jurassic_gb300.model import Ctl, Ret
+    ctl = Ctl(emitter=["CO2", "H2O", "O3"], nu=np.linspace(650.0, 2400.0, 300))
+    ctl.rett_zmin, ctl.rett_zmax = 0.0, 60.0
+    ctl.retq_zmin = np.array([-999.0, 0.0, -999.0])
+    ctl.retq_zmax = np.array([-999.0, 20.0, -999.0])
+    ret = Ret(kernel_recomp=1, conv_itmax=10, conv_dmin=0.1, err_ana=1,
+              err_noise=np.full(ctl.nd, 1e-4), err_formod=np.full(ctl.nd, 0.5),
+              err_temp=2.0, err_temp_cz=3.0, err_temp_ch=-999.0,
+              err_q=np.array([0.0, 30.0, 0.0]), err_q_cz=np.array([-999.0, 3.0, -999.0]),
+              err_q_ch=np.array([-999.0, -999.0, -999.0]))
+    return ctl, ret, synth.make_tables(ctl, seed + 100), synth.make_filters(ctl)
+
+
+def run_serving(args, device):
+    """Closed-loop capacity and Poisson-arrival latency of the retrieval
+    engine, mixed precision and FP64, on the serving stream."""
+    from jurassic_gb300 import native, serving, synth
+    ctl, ret, tables, filters = serving_workload()
+    ctx = native.Context(ctl, tables, filters, device=device)
+    n, m = args.serve_requests, args.serve_fp64_requests
+    rng = np.random.default_rng(55)
+    nch = rng.integers(50, 301, n)
+    reqs = synth.retrieval_requests(ctl, lambda b: ctx.formod_batch(b.fresh_outputs(), native.FP64),
+                                    n, 55, nlev=(41, 101), ztop=100.0, nch=nch, limb_rays=5)
+    out = {"workload": "retrieval stream: %d requests, 50-300 of 300 channels, 41-101 levels, "
+                       "nadir/limb(5 rays) alternating, CO2+H2O+O3, T+H2O retrieved" % n}
+
+    def engine(prec):
+        return ctx.engine(ret, prec, mem_budget=int(args.serve_budget_gb * 2**30))
+
+    def strip(r):
+        return {k: v for k, v in r.items() if k != "results"}
+
+    # warm-up (autotune, allocations) on two requests
+    serving.serve(engine(native.MIXED), ctl, reqs[:2], np.inf)
+    serving.serve(engine(native.FP64), ctl, reqs[:2], np.inf)
+    closed = serving.serve(engine(native.MIXED), ctl, reqs, np.inf)
+    rate = args.serve_load * closed["retrievals_per_s"]
+    pois = serving.serve(engine(native.MIXED), ctl, reqs, rate, seed=7)
+    sub_mixed = serving.serve(engine(native.MIXED), ctl, reqs[:m], np.inf)
+    sub_fp64 = serving.serve(engine(native.FP64), ctl, reqs[:m], np.inf)
+    dev = []
+    for a, b in zip(sub_fp64["results"], sub_mixed["results"]):
+        if a["err_total"] is not None:
+            dev.append(float(np.max(np.abs(a["x"] - b["x"]) / a["err_total"])))
+    out.update({
+        "mixed_closed_loop": strip(closed),
+        "mixed_poisson": dict(strip(pois), load=args.serve_load),
+        "fp64_closed_loop_subset": strip(sub_fp64),
+        "mixed_closed_loop_subset": strip(sub_mixed),
+        "retrievals_per_s_mixed_over_fp64": sub_mixed["retrievals_per_s"] / sub_fp64["retrievals_per_s"],
+        "mixed_vs_fp64_max_dx_over_sigma": max(dev) if dev else None,
+        "mem_budget_gb": args.serve_budget_gb})
+    ctx.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -212,6 +278,11 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=48)
+    ap.add_argument("--serve-fp64-requests", type=int, default=12)
+    ap.add_argument("--serve-load", type=float, default=0.7,
+                    help="Poisson arrival rate as a fraction of the closed-loop capacity")
+    ap.add_argument("--serve-budget-gb", type=float, default=64.0)
     args = ap.parse_args()
 
     rank, world, local, pg = dist_setup(args.gpus)
@@ -352,6 +423,8 @@ def main():
                             "mixed_p99_abs_dBT_mK": 1e3 * float(np.percentile(dbt, 99)),
                             "mixed_max_rel_rad": float(np.max(np.abs(rad_mixed[:, sl] - ref.rad) / np.abs(ref.rad))),
                             "fp64_max_rel_rad": float(np.max(rel64))}
+    if rank == 0 and args.serve_requests > 0:
+        line["serving"] = run_serving(args, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
     for p in dptr.values():

@@ -169,7 +169,8 @@ typedef struct {
 } jgb_ret;
 
 /* Optimal-estimation retrievals (optimal_estimation, retrieval.c:448-749)
-   of every observation of a batch, advancing in lockstep on the device.
+   of every observation of a batch (all submitted at once to a retrieval
+   engine and stepped until done).
    In:  b holds the a-priori atmospheres and in b->rad the measurement
         (NaN = channel not used).
    Out: x: final state vectors (atm2x of the final atmosphere, sizes n_i of
@@ -182,6 +183,65 @@ typedef struct {
    FP64 Cholesky, LM step, cost and convergence test in both modes. */
 int jgb_retrieve_batch(jgb_ctx *ctx, const jgb_ret *ret, const jgb_batch *b, double *x,
                        double *cov, double *costs, int *iters, int precision);
+
+/* ---------------------------------------------------------------------------
+   Retrieval engine (continuous batching).  Replaces the reference's
+   one-retrieval-per-process driver (retrieval.c:148-245 main loop over
+   directories calling optimal_estimation, 448-749) by a queue of independent
+   requests served on one device: requests are admitted while at most
+   max_active are in flight and their working set fits mem_budget bytes
+   (0 = unlimited; a request larger than the budget is admitted alone when
+   nothing else runs); every admitted request keeps its atmosphere, Jacobian
+   and LM state resident on the device.  jgb_engine_step advances every
+   admitted request by one LM iteration (newly admitted ones are first
+   initialised: a-priori forward model, S_a^-1, cost, Jacobian).  A request's
+   results do not depend on which other requests share its steps.  Peak
+   device memory is about twice the working set (it is rebuilt into a
+   second buffer when requests join or leave) plus the forward-model scratch
+   of the context.  Not thread-safe: one host thread per engine, and the
+   engine uses its context's stream. */
+typedef struct jgb_engine jgb_engine;
+
+typedef struct {
+  unsigned long long submitted, finished, failed, steps, rebuilds, forward_calls, lm_trials,
+      jacobians;
+  double step_ms;              /* host wall time spent in jgb_engine_step */
+  int active, queued, done;    /* requests in flight, waiting, finished and not yet collected */
+  unsigned long long used_bytes;  /* working-set bytes of the active requests */
+} jgb_engine_stats;
+
+/* Results of one request; every pointer may be NULL (not copied).
+   Sizes: n state elements, m measurement elements (jgb_engine_sizes).
+   x[n] final state (atm2x order); costs[conv_itmax+1] chi^2/m per iteration
+   (NaN after convergence); rad/tau[nd][nr], tp[3][nr], p[np] forward model
+   and pressures of the final iterate.  With err_ana (has_err_ana = 1):
+   cov[n*n] retrieval covariance, avk[n*n] averaging kernel, gain[n*m] (only
+   if the engine keeps gains), err_total/err_noise/err_formod[n] standard
+   deviations (write_stddev "total", "noise", "formod"), cont[n] and res[n]
+   as written to atm_cont.tab and atm_res.tab by analyze_avk
+   (retrieval.c:257-336), in state-vector order. */
+typedef struct {
+  double *x, *cov, *costs, *rad, *tau, *tp, *p;
+  double *gain, *avk, *err_total, *err_noise, *err_formod, *cont, *res;
+  int iters, status, has_err_ana;
+} jgb_ret_out;
+
+int jgb_engine_create(jgb_ctx *ctx, const jgb_ret *ret, int precision,
+                      unsigned long long mem_budget, int max_active, int keep_gain,
+                      jgb_engine **out);
+void jgb_engine_destroy(jgb_engine *e);
+/* Queue every observation of a host batch (a-priori atmosphere, geometry and
+   measurement in b->rad, NaN = not used) as one request; ids[nobs] out.
+   Checks of set_cov_apr/set_cov_meas are made here. */
+int jgb_engine_submit(jgb_engine *e, const jgb_batch *b, unsigned long long *ids);
+/* Admission plus one LM iteration of every admitted request. */
+int jgb_engine_step(jgb_engine *e, int *n_active, int *n_queued, int *n_done);
+/* Ids of finished requests not collected yet (ascending, up to max). */
+int jgb_engine_finished(jgb_engine *e, unsigned long long *ids, int max, int *count);
+int jgb_engine_sizes(jgb_engine *e, unsigned long long id, int *n, int *m, int *np, int *nr);
+/* Copy the results of a finished request and release it. */
+int jgb_engine_result(jgb_engine *e, unsigned long long id, jgb_ret_out *out);
+int jgb_engine_get_stats(const jgb_engine *e, jgb_engine_stats *out);
 
 int jgb_get_stats(const jgb_ctx *ctx, jgb_stats *out);
 

@@ -162,6 +162,9 @@ struct BatchDev {
   double* tau;          // [nd][nray]
   double* tp;           // [3][nray]
   const unsigned char* mask;  // [nd][nray] 1 = masked
+  // [nobs] 1 = observation not computed: its rays get no LOS and its
+  // outputs (rad, tau, tp) and pressures are left untouched (nullptr: none)
+  const unsigned char* obs_skip;
 };
 
 // Lines of sight, ray-major with per-ray offsets, SoA planes of FP64.

@@ -232,6 +232,10 @@ __device__ int walk(const CtlDev& c, const ChanDev& ch, const AtmView& a, const 
 __global__ void k_trace_count(CtlDev c, ChanDev ch, BatchDev b, LosDev L, unsigned* err) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= b.nray) return;
+  if (b.obs_skip && b.obs_skip[b.ray_obs[r]]) {
+    L.count[r] = 0;
+    return;
+  }
   const AtmView a = atm_view(c, b, b.ray_obs[r]);
   double sft;
   const int n = walk<false>(c, ch, a, b.geo, b.nray, r, L, 0, c.nlos_max, &sft, err);
@@ -241,6 +245,7 @@ __global__ void k_trace_count(CtlDev c, ChanDev ch, BatchDev b, LosDev L, unsign
 __global__ void k_trace_fill(CtlDev c, ChanDev ch, BatchDev b, LosDev L, unsigned* err) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= b.nray) return;
+  if (b.obs_skip && b.obs_skip[b.ray_obs[r]]) return;
   const AtmView a = atm_view(c, b, b.ray_obs[r]);
   const long long base = L.off[r];
   const int cap = L.count[r];
@@ -483,6 +488,7 @@ __global__ void k_path_fp64(CtlDev c, TblDev T, ChanDev ch, BatchDev b, LosDev L
   const int id = (int)(gid / nray);
   const int r = (int)(gid % nray);
   const int o = b.ray_obs[r];
+  if (b.obs_skip && b.obs_skip[o]) return;
   const int n = L.count[r];
   const long long base = L.off[r];
   const double nu = ch.nu[id];
@@ -595,6 +601,7 @@ __global__ void k_srcfunc(int nd, int id0, int nch, const int* fn_off, const dou
 __global__ void k_hydrostatic(CtlDev c, BatchDev b, double* p_out) {
   const int o = blockIdx.x * blockDim.x + threadIdx.x;
   if (o >= b.nobs || c.hydz < 0) return;
+  if (b.obs_skip && b.obs_skip[o]) return;
   const int l0 = b.lev_off[o], np = b.lev_off[o + 1] - l0;
   const double* z = b.z + l0;
   const double* t = b.t + l0;

@@ -53,10 +53,13 @@ struct CtxView {
 };
 int ctx_view(jgb_ctx* x, CtxView* out);  // fills *out; returns JGB_ERR_STATE if not ready
 
-// jgb_normal.cu: batched normal-equation products on device buffers
+// jgb_normal.cu: batched normal-equation products on device buffers.
+// Problems are concatenated (K blocks m_i x n_i, A blocks n_i x n_i, ...);
+// sel (host, nullptr = all) picks the problems computed, the others' blocks
+// are left untouched.  At most 65535 selected problems per call.
 int normal_equations_dev(int nret, const int* m, const int* n, const double* K, const double* w,
-                         const double* dy, double* A, double* b, int precision, void* desc_dev,
-                         cudaStream_t s);
+                         const double* dy, double* A, double* b, int precision, const int* sel,
+                         void* desc_dev, cudaStream_t s);
 size_t normal_desc_bytes(int nret);
 int ctx_fail(jgb_ctx* x, int code, const char* msg);
 

@@ -288,7 +288,8 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
   const int tile = blockIdx.x / nchb;
   const int id = (blockIdx.x % nchb) * 4 + warp;
   if (tile >= P.ntile || id >= c.nd) return;
-  const int r = P.perm[tile * 32 + lane];
+  int r = P.perm[tile * 32 + lane];
+  if (r >= 0 && b.obs_skip && b.obs_skip[b.ray_obs[r]]) r = -1;  // lane idle, outputs untouched
   const int n = r >= 0 ? L.count[r] : 0;
   const Fields F = fields_of(c);
   const float* base = P.data + P.toff[tile] * (long long)F.n * 32 + lane;

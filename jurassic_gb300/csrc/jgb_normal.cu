@@ -185,32 +185,43 @@ __global__ void k_normal_fp64(const NeDesc* desc, const double* Kall, const doub
 }  // namespace
 
 int normal_equations_dev(int nret, const int* m, const int* n, const double* K, const double* w,
-                         const double* dy, double* A, double* b, int precision, void* desc_dev,
-                         cudaStream_t s) {
-  // descriptors (host -> device scratch provided by the caller)
+                         const double* dy, double* A, double* b, int precision, const int* sel,
+                         void* desc_dev, cudaStream_t s) {
+  // descriptors of the selected problems (host -> device scratch provided by
+  // the caller); offsets follow the concatenation of all nret problems
   NeDesc* hd = new NeDesc[nret];
   long long ko = 0, mo = 0, ao = 0, bo = 0;
-  int maxtiles = 0, maxn = 0;
+  int maxtiles = 0, maxn = 0, nsel = 0;
   for (int i = 0; i < nret; i++) {
-    hd[i] = NeDesc{m[i], n[i], ko, mo, ao, bo};
+    if (!sel || sel[i]) {
+      hd[nsel++] = NeDesc{m[i], n[i], ko, mo, ao, bo};
+      const int nt = (n[i] + 1 + kTile - 1) / kTile;
+      maxtiles = nt * (nt + 1) / 2 > maxtiles ? nt * (nt + 1) / 2 : maxtiles;
+      maxn = n[i] > maxn ? n[i] : maxn;
+    }
     ko += (long long)m[i] * n[i];
     mo += m[i];
     ao += (long long)n[i] * n[i];
     bo += n[i];
-    const int nt = (n[i] + 1 + kTile - 1) / kTile;
-    maxtiles = nt * (nt + 1) / 2 > maxtiles ? nt * (nt + 1) / 2 : maxtiles;
-    maxn = n[i] > maxn ? n[i] : maxn;
   }
-  cudaError_t e = cudaMemcpyAsync(desc_dev, hd, sizeof(NeDesc) * nret, cudaMemcpyHostToDevice, s);
+  if (nsel == 0) {
+    delete[] hd;
+    return JGB_OK;
+  }
+  if (nsel > 65535) {
+    delete[] hd;
+    return JGB_ERR_ARG;
+  }
+  cudaError_t e = cudaMemcpyAsync(desc_dev, hd, sizeof(NeDesc) * nsel, cudaMemcpyHostToDevice, s);
   cudaStreamSynchronize(s);
   delete[] hd;
   if (e != cudaSuccess) return JGB_ERR_CUDA;
   if (precision == JGB_MIXED) {
-    dim3 grid(maxtiles, 1, nret);
+    dim3 grid(maxtiles, 1, nsel);
     k_normal_3xtf32<<<grid, 128, 0, s>>>(static_cast<const NeDesc*>(desc_dev), K, w, dy, A, b);
   } else {
     const long long nel = (long long)maxn * (maxn + 1) / 2 + maxn;
-    dim3 grid((unsigned)((nel + 127) / 128 < 4096 ? (nel + 127) / 128 : 4096), nret);
+    dim3 grid((unsigned)((nel + 127) / 128 < 4096 ? (nel + 127) / 128 : 4096), nsel);
     k_normal_fp64<<<grid, 128, 0, s>>>(static_cast<const NeDesc*>(desc_dev), K, w, dy, A, b);
   }
   return cudaGetLastError() == cudaSuccess ? JGB_OK : JGB_ERR_CUDA;
@@ -253,7 +264,7 @@ extern "C" int jgb_normal_equations(jgb_ctx* x, int nret, const int* m, const in
   cudaMemcpyAsync(dK, K, sizeof(double) * sk, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(dw, w, sizeof(double) * sm, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(ddy, dy, sizeof(double) * sm, cudaMemcpyHostToDevice, s);
-  rc = normal_equations_dev(nret, m, n, dK, dw, ddy, dA, db, precision, ddesc, s);
+  rc = normal_equations_dev(nret, m, n, dK, dw, ddy, dA, db, precision, nullptr, ddesc, s);
   if (rc == JGB_OK) {
     cudaMemcpyAsync(A, dA, sizeof(double) * sa, cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(b, db, sizeof(double) * sb, cudaMemcpyDeviceToHost, s);

@@ -1,23 +1,27 @@
 // Optimal-estimation retrieval on the device (optimal_estimation,
-// retrieval.c:448-749), batched over independent retrievals.
+// retrieval.c:448-749), batched over independent retrievals and served by a
+// continuous-batching engine (see the engine section below).
 //
-// All retrievals of a batch advance in lockstep through the Levenberg-
-// Marquardt iterations, each with its own damping parameter, inner-loop
-// state and convergence flag.  Per outer iteration: finite-difference
-// Jacobian (fd_core, one batched forward-model launch sequence for every
-// perturbation of every active retrieval), normal-equation products (3xTF32
-// tensor cores or FP64), then up to 20 damped steps, each an FP64 Cholesky
-// solve plus one batched forward model of the retrievals still trying.
-// FP64 is used for the a-priori covariance and its inverse, the Cholesky
-// solves, the cost function and the convergence test.
+// Every retrieval keeps its own Levenberg-Marquardt state (iteration count,
+// damping parameter, inner-loop trials, convergence).  Per iteration:
+// finite-difference Jacobian (fd_core, one batched forward-model launch
+// sequence for every perturbation of every retrieval that needs it),
+// normal-equation products (3xTF32 tensor cores or FP64), then up to 20
+// damped steps, each an FP64 Cholesky solve plus one forward model of the
+// retrievals still trying.  FP64 is used for the a-priori covariance and its
+// inverse, the Cholesky solves, the cost function, the convergence test and
+// the error analysis (retrieval.c:668-726).
 //
 // This translation unit is compiled without FMA contraction: the FP64 linear
 // algebra follows the textbook loop orders of the reference's helpers
 // (cost_function retrieval.c:340-369, matrix_invert 373-399, Cholesky
-// decomposition/solution as used at 588-589).
+// decomposition/solution as used at 588-589, matrix_product 403-444).
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
+#include <deque>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -62,9 +66,9 @@ __device__ inline double* elem_ptr(const AtmArrays& a, int lev0, long long o, in
 }
 
 __global__ void k_gather_state(int nret, const RetDesc* d, const int* lev_off, const int4* elems,
-                               AtmArrays a, double* xv) {
+                               const int* active, AtmArrays a, double* xv) {
   const int i = blockIdx.x;
-  if (i >= nret) return;
+  if (i >= nret || (active && !active[i])) return;
   for (int j = threadIdx.x; j < d[i].n; j += blockDim.x)
     xv[d[i].xo + j] = *elem_ptr(a, lev_off[i], i, elems[d[i].xo + j]);
 }
@@ -117,9 +121,9 @@ __global__ void k_set_iterate(int nret, const RetDesc* d, const int* lev_off, co
 
 // y_i (obs2y order) from the forward-model results of retrieval i.
 __global__ void k_gather_y(int nret, const RetDesc* d, const int* ray_off, const int2* ymap,
-                           const double* rad, long long nray, double* yv) {
+                           const int* active, const double* rad, long long nray, double* yv) {
   const int i = blockIdx.x;
-  if (i >= nret) return;
+  if (i >= nret || (active && !active[i])) return;
   for (int r = threadIdx.x; r < d[i].m; r += blockDim.x) {
     const int2 ym = ymap[d[i].yo + r];
     yv[d[i].yo + r] = rad[(long long)ym.y * nray + ray_off[i] + ym.x];
@@ -281,9 +285,10 @@ struct SaElem {
   int iq;
 };
 
-__global__ void k_build_sa(int nret, const RetDesc* d, const SaElem* el, double* S) {
+__global__ void k_build_sa(int nret, const RetDesc* d, const int* active, const SaElem* el,
+                           double* S) {
   const int i = blockIdx.y;
-  if (i >= nret) return;
+  if (i >= nret || (active && !active[i])) return;
   const RetDesc r = d[i];
   const long long nn = (long long)r.n * r.n;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
@@ -323,375 +328,1182 @@ __global__ void k_dot_state(int nret, const RetDesc* d, const int* active, const
   out[i] = s;
 }
 
-__global__ void k_add(long long n, const double* a, double* b) {
-  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e < n) b[e] += a[e];
+}  // namespace
+}  // namespace jgb
+
+
+// ===========================================================================
+// Retrieval engine: continuous batching of independent retrievals.
+//
+// Requests (one observation each) wait in a queue and are admitted while the
+// number of active requests and the device memory of their working set stay
+// within the engine's limits.  The working set is one contiguous allocation
+// holding, for every active request, its a-priori and current atmosphere,
+// geometry, measurement, forward model, state vectors, S_a^-1, K, K^T W K
+// and the LM scratch.  When requests leave or join, a new working set is
+// built in a second allocation and the iterate state of the requests that
+// stay is moved there on the device (segment copies), so no request's state
+// goes back to the host between its iterations.
+//
+// One engine step = admission, the initialisation (a-priori forward model,
+// S_a^-1, cost, first Jacobian) of newly admitted requests, then one
+// Levenberg-Marquardt iteration of every initialised request, each at its
+// own iteration count, damping parameter and kernel-recomputation phase.
+// Forward models run on the whole working set with the requests that are
+// not part of the current sub-step flagged off (no LOS, outputs untouched),
+// so every request sees exactly the arithmetic it would see alone.
+
+namespace jgb {
+namespace {
+
+// Segment copies: seg[3k] source, seg[3k+1] destination (device addresses),
+// seg[3k+2] length in doubles.  blockIdx.y strides over segments.
+__global__ void k_copy_segments(int nseg, const unsigned long long* seg) {
+  for (int k = blockIdx.y; k < nseg; k += gridDim.y) {
+    const double* src = reinterpret_cast<const double*>(seg[3 * k]);
+    double* dst = reinterpret_cast<double*>(seg[3 * k + 1]);
+    const long long nw = (long long)seg[3 * k + 2];
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nw;
+         i += (long long)gridDim.x * blockDim.x)
+      dst[i] = src[i];
+  }
+}
+
+// LOS point counts of the rays that were traced (skip flag clear).
+__global__ void k_keep_counts(int nray, const int* ray_obs, const unsigned char* skip,
+                              const int* src, int* dst) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < nray && !skip[ray_obs[r]]) dst[r] = src[r];
+}
+
+// dst = src on the n x n blocks of the selected retrievals.
+__global__ void k_select_nn(int nret, const RetDesc* d, const int* sel, const double* src,
+                            double* dst) {
+  const int i = blockIdx.y;
+  if (i >= nret || !sel[i]) return;
+  const long long nn = (long long)d[i].n * d[i].n;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
+       e += (long long)gridDim.x * blockDim.x)
+    dst[d[i].so + e] = src[d[i].so + e];
+}
+
+// b += a on the n x n blocks (gsl_matrix_add(cov, s_a_inv), retrieval.c:673)
+__global__ void k_add_nn(int nret, const RetDesc* d, const int* active, const double* a,
+                         double* b) {
+  const int i = blockIdx.y;
+  if (i >= nret || !active[i]) return;
+  const long long nn = (long long)d[i].n * d[i].n;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
+       e += (long long)gridDim.x * blockDim.x)
+    b[d[i].so + e] = b[d[i].so + e] + a[d[i].so + e];
+}
+
+// Gain G = cov K^T diag(w^2), n x m at offset ko (retrieval.c:694-701).
+__global__ void k_gain(int nret, const RetDesc* d, const int* active, const double* cov,
+                       const double* K, const double* w, double* G) {
+  const int i = blockIdx.y;
+  if (i >= nret || !active[i]) return;
+  const RetDesc r = d[i];
+  const double* C = cov + r.so;
+  const double* Ki = K + r.ko;
+  const long long nm = (long long)r.n * r.m;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < nm;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int a = (int)(e / r.m), j = (int)(e % r.m);
+    const double wj = w[r.yo + j];
+    double s = 0;
+    for (int b = 0; b < r.n; b++) s += C[(long long)a * r.n + b] * (Ki[(long long)j * r.n + b] * (wj * wj));
+    G[r.ko + e] = s;
+  }
+}
+
+// sqrt(diag(G diag(sig^2) G^T)): error propagation of noise or forward-model
+// errors (matrix_product(gain, sig, 2, a) + write_stddev, retrieval.c:705-711).
+__global__ void k_err_diag(int nret, const RetDesc* d, const int* active, const double* G,
+                           const double* sig, double* out) {
+  const int i = blockIdx.x;
+  if (i >= nret || !active[i]) return;
+  const RetDesc r = d[i];
+  for (int a = threadIdx.x; a < r.n; a += blockDim.x) {
+    double s = 0;
+    for (int j = 0; j < r.m; j++) {
+      const double v = G[r.ko + (long long)a * r.m + j] * sig[r.yo + j];
+      s += v * v;
+    }
+    out[r.xo + a] = sqrt(s);
+  }
+}
+
+__global__ void k_sqrt_diag(int nret, const RetDesc* d, const int* active, const double* S,
+                            double* out) {
+  const int i = blockIdx.x;
+  if (i >= nret || !active[i]) return;
+  for (int a = threadIdx.x; a < d[i].n; a += blockDim.x)
+    out[d[i].xo + a] = sqrt(S[d[i].so + (long long)a * d[i].n + a]);
+}
+
+// Averaging kernel A = G K, n x n (retrieval.c:714-715).
+__global__ void k_avk(int nret, const RetDesc* d, const int* active, const double* G,
+                      const double* K, double* A) {
+  const int i = blockIdx.y;
+  if (i >= nret || !active[i]) return;
+  const RetDesc r = d[i];
+  const long long nn = (long long)r.n * r.n;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int a = (int)(e / r.n), b = (int)(e % r.n);
+    double s = 0;
+    for (int j = 0; j < r.m; j++) s += G[r.ko + (long long)a * r.m + j] * K[r.ko + (long long)j * r.n + b];
+    A[r.so + e] = s;
+  }
+}
+
+// analyze_avk (retrieval.c:257-336): per state element, the row sum of the
+// averaging kernel over the elements of the same quantity (added to the
+// value copy_atm(..., init=1) leaves there: 1 for surface emissivities,
+// else 0) and the inverse diagonal.
+__global__ void k_avk_analyze(int nret, const RetDesc* d, const int* active, const double* A,
+                              const SaElem* el, int iq_sfeps, double* cont, double* res) {
+  const int i = blockIdx.x;
+  if (i >= nret || !active[i]) return;
+  const RetDesc r = d[i];
+  for (int a = threadIdx.x; a < r.n; a += blockDim.x) {
+    const int iq = el[r.xo + a].iq;
+    int n0 = -1, n1 = 0;
+    for (int j = 0; j < r.n; j++)
+      if (el[r.xo + j].iq == iq) {
+        if (n0 < 0) n0 = j;
+        n1 = j - n0 + 1;
+      }
+    double s = iq >= iq_sfeps ? 1.0 : 0.0;
+    for (int j = 0; j < n1; j++) s += A[r.so + (long long)a * r.n + n0 + j];
+    cont[r.xo + a] = s;
+    res[r.xo + a] = 1 / A[r.so + (long long)a * r.n + a];
+  }
+}
+
+// One retrieval request: its inputs, host-side LM scalars and results.
+struct Request {
+  unsigned long long id = 0;
+  int np = 0, nr = 0, n = 0, m = 0;
+  std::vector<double> lev;    // [6+ng+nw][np]: time z lon lat p t q[] k[]
+  std::vector<double> scal;   // [nscal]
+  std::vector<double> geo;    // [7][nr]
+  std::vector<double> rad;    // [nd][nr] measurement, NaN = channel not used
+  std::vector<Elem> lay;      // state layout (atm2x order)
+  std::vector<int2> ymap;     // (ray, channel) of each measurement element
+  std::vector<int4> elems;    // device form of lay
+  std::vector<SaElem> sael;   // a-priori sigma, correlation lengths, location
+  std::vector<double> ymeas, winv, sn, sf;  // y_m, 1/sigma_eps, noise, formod errors
+  bool sa_diag = true;
+  size_t bytes = 0;           // working-set bytes of this request
+  int slot = -1;              // index in the current working set
+  int state = 0;              // 0 waiting for initialisation, 1 iterating, 2 finished
+  int it = 0;                 // LM iterations done
+  double lmpar = 0.001, chisq = 0, chisq_old = 0;
+  int status = JGB_OK;
+  std::vector<double> costs;
+  // results
+  std::vector<double> x, cov, avk, gain, err_total, err_noise, err_formod, cont, res;
+  std::vector<double> rad_out, tau_out, tp_out, p_out;
+};
+
+// Contiguous device working set of the active requests.
+struct WorkSet {
+  int nret = 0;
+  long long nlev = 0, nray = 0, nx = 0, ny = 0, nss = 0, nk = 0;
+  FdLayout H;
+  std::vector<RetDesc> desc;
+  std::vector<int> mvec, nvec;
+  DevBuf mem;
+  double *apr_lev = nullptr, *cur_lev = nullptr, *apr_scal = nullptr, *cur_scal = nullptr;
+  double *geo = nullptr, *radm = nullptr, *rad = nullptr, *tau = nullptr, *tp = nullptr;
+  double *xa = nullptr, *xi = nullptr, *dx = nullptr, *bvec = nullptr, *step = nullptr, *xfin = nullptr;
+  double *e_tot = nullptr, *e_noise = nullptr, *e_formod = nullptr, *cont = nullptr, *res = nullptr;
+  double *ym = nullptr, *yi = nullptr, *dy = nullptr, *w = nullptr, *sn = nullptr, *sf = nullptr;
+  double *sainv = nullptr, *cov = nullptr, *covn = nullptr, *Amat = nullptr, *work = nullptr;
+  double *Kd = nullptr, *G = nullptr;
+  double *chisq = nullptr, *lmpar = nullptr, *disq = nullptr;
+  int4* elems = nullptr;
+  SaElem* sael = nullptr;
+  RetDesc* desc_d = nullptr;
+  int *active = nullptr, *status = nullptr, *levoff = nullptr, *rayoff = nullptr;
+  int *rayobs = nullptr, *cnt = nullptr;
+  unsigned char *skip = nullptr, *mask = nullptr;
+  int2* ymap = nullptr;
+  void* nedesc = nullptr;
+};
+
+// Device bytes of a working set with these totals (the carving below).
+size_t workset_bytes(const CtlDev& c, long long nret, long long nlev, long long nray, long long nx,
+                     long long ny, long long nss, long long nk, bool err_ana) {
+  const long long nscal = 5 + c.ncl + c.nsf, nplanes = 6 + c.ng + c.nw;
+  const size_t dbl = sizeof(double);
+  return dbl * (size_t)(nlev * nplanes * 2 + nret * nscal * 2 + 7 * nray + c.nd * nray * 3 +
+                        3 * nray + nx * 11 + ny * 6 + nss * 5 + nk * (err_ana ? 2 : 1) + nret * 3) +
+         sizeof(int4) * nx + sizeof(SaElem) * nx + sizeof(RetDesc) * nret +
+         sizeof(int) * (4 * nret + 2 + 2 * nray) + (size_t)nret + (size_t)c.nd * nray +
+         sizeof(int2) * ny + normal_desc_bytes((int)nret) + 64 * 256;
 }
 
 }  // namespace
 }  // namespace jgb
 
+struct jgb_engine {
+  jgb_ctx* x = nullptr;
+  int precision = JGB_FP64;
+  unsigned long long budget = 0;
+  int max_active = 0;
+  int keep_gain = 0;
+  jgb_ret ret{};
+  std::vector<double> v_formod, v_noise, v_q, v_qcz, v_qch, v_k, v_kcz, v_kch, v_clk, v_sfeps;
+  unsigned long long next_id = 1;
+  std::deque<jgb::Request*> queue;
+  std::vector<jgb::Request*> active;
+  std::map<unsigned long long, jgb::Request*> done;
+  jgb::WorkSet ws[2];
+  int cur = 0;
+  bool have_ws = false, dirty = true;
+  unsigned long long used = 0;
+  jgb::DevBuf segbuf, stage;
+  double* pinned = nullptr;
+  size_t pinned_n = 0;
+  jgb_engine_stats st{};
+  ~jgb_engine() {
+    for (jgb::Request* r : queue) delete r;
+    for (jgb::Request* r : active) delete r;
+    for (auto& kv : done) delete kv.second;
+    if (pinned) cudaFreeHost(pinned);
+  }
+};
+
 using namespace jgb;
 
-extern "C" int jgb_retrieve_batch(jgb_ctx* x, const jgb_ret* ret, const jgb_batch* hb,
-                                  double* x_out, double* cov_out, double* costs, int* iters,
-                                  int precision) {
-  if (!x || !ret || !hb || !x_out || hb->nobs <= 0) return ctx_error(x, JGB_ERR_ARG, "bad arguments");
-  if (ret->conv_itmax < 0 || ret->kernel_recomp <= 0) return ctx_error(x, JGB_ERR_ARG, "bad retrieval settings");
-  if (hb->nobs > 65535) return ctx_error(x, JGB_ERR_ARG, "at most 65535 retrievals per batch");
-  cudaSetDevice(x->device);
+namespace {
+
+#define ECK(call)                                                                        \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return ctx_error(E->x, JGB_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+double now_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Host-side checks and tables of one request (set_cov_apr, set_cov_meas,
+// retrieval.c:808-964; errors as the reference reports them).
+int prepare_request(jgb_engine* E, Request* q) {
+  jgb_ctx* x = E->x;
+  const CtlDev& c = x->c;
+  const jgb_ret* ret = &E->ret;
+  FdLayout H;
+  const int lev_off[2] = {0, q->np}, ray_off[2] = {0, q->nr};
+  int rc = fd_layout(x, 1, lev_off, ray_off, q->lev.data() + q->np, q->rad.data(), H);
+  if (rc) return rc;
+  q->lay = H.lay[0];
+  q->ymap = H.ymap;
+  q->n = H.ncnt[0];
+  q->m = H.mcnt[0];
+  q->ymeas.resize(q->m);
+  q->winv.resize(q->m);
+  q->sn.resize(q->m);
+  q->sf.resize(q->m);
+  for (int k = 0; k < q->m; k++) {
+    const int2 ym = q->ymap[k];
+    const double v = q->rad[(size_t)ym.y * q->nr + ym.x];
+    const double sn = ret->err_noise ? ret->err_noise[ym.y] : 0.0;
+    const double sf = fabs((ret->err_formod ? ret->err_formod[ym.y] : 0.0) / 100 * v);
+    q->ymeas[k] = v;
+    q->sn[k] = sn;
+    q->sf[k] = sf;
+    q->winv[k] = 1 / sqrt(sn * sn + sf * sf);
+    if (!(q->winv[k] > 0))
+      return ctx_error(x, JGB_ERR_ARG, "Check measurement errors (zero standard deviation)!");
+  }
+  q->elems.resize(q->n);
+  q->sael.resize(q->n);
+  const double* L = q->lev.data();
+  const size_t np = q->np;
+  for (int j = 0; j < q->n; j++) {
+    const Elem& e = q->lay[j];
+    q->elems[j] = make_int4(e.arr, e.idx, e.arr == 4 ? e.idx : e.lev, e.hkind);
+    SaElem se{};
+    double xv;
+    switch (e.arr) {
+      case 0: xv = L[4 * np + e.lev]; break;
+      case 1: xv = L[5 * np + e.lev]; break;
+      case 2: xv = L[(6 + (size_t)e.idx) * np + e.lev]; break;
+      case 3: xv = L[(6 + (size_t)c.ng + e.idx) * np + e.lev]; break;
+      default: xv = q->scal[e.idx]; break;
+    }
+    if (e.arr == 0) { se.iq = 0; se.sigma = ret->err_press / 100 * xv; se.cz = ret->err_press_cz; se.ch = ret->err_press_ch; }
+    else if (e.arr == 1) { se.iq = 1; se.sigma = ret->err_temp; se.cz = ret->err_temp_cz; se.ch = ret->err_temp_ch; }
+    else if (e.arr == 2) { se.iq = 2 + e.idx; se.sigma = ret->err_q[e.idx] / 100 * xv; se.cz = ret->err_q_cz[e.idx]; se.ch = ret->err_q_ch[e.idx]; }
+    else if (e.arr == 3) { se.iq = 2 + c.ng + e.idx; se.sigma = ret->err_k[e.idx]; se.cz = ret->err_k_cz[e.idx]; se.ch = ret->err_k_ch[e.idx]; }
+    else {
+      const int o = 2 + c.ncl;
+      se.cz = se.ch = 0;
+      if (e.idx == 0) { se.iq = 2 + c.ng + c.nw; se.sigma = ret->err_clz; }
+      else if (e.idx == 1) { se.iq = 3 + c.ng + c.nw; se.sigma = ret->err_cldz; }
+      else if (e.idx < o) { se.iq = 4 + c.ng + c.nw + (e.idx - 2); se.sigma = ret->err_clk[e.idx - 2]; }
+      else if (e.idx == o) { se.iq = 4 + c.ng + c.nw + c.ncl; se.sigma = ret->err_sfz; }
+      else if (e.idx == o + 1) { se.iq = 5 + c.ng + c.nw + c.ncl; se.sigma = ret->err_sfp; }
+      else if (e.idx == o + 2) { se.iq = 6 + c.ng + c.nw + c.ncl; se.sigma = ret->err_sft; }
+      else { se.iq = 7 + c.ng + c.nw + c.ncl + (e.idx - o - 3); se.sigma = ret->err_sfeps[e.idx - o - 3]; }
+    }
+    if (!(se.sigma * se.sigma > 0))
+      return ctx_error(x, JGB_ERR_ARG, "Check a priori data (zero standard deviation)!");
+    const int lv = e.arr == 4 ? 0 : e.lev;
+    se.lon = L[2 * np + lv];
+    se.lat = L[3 * np + lv];
+    se.z = L[1 * np + lv];
+    q->sael[j] = se;
+  }
+  // S_a is diagonal unless two elements of one quantity correlate (retrieval.c:901)
+  q->sa_diag = true;
+  for (int j = 0; j < q->n && q->sa_diag; j++) {
+    const SaElem& a = q->sael[j];
+    if (a.cz > 0 && a.ch > 0)
+      for (int k = 0; k < q->n; k++)
+        if (k != j && q->sael[k].iq == a.iq) {
+          q->sa_diag = false;
+          break;
+        }
+  }
+  const long long n = q->n, m = q->m;
+  q->bytes = workset_bytes(c, 1, q->np, q->nr, n, m, n * n, n * m, E->ret.err_ana != 0);
+  q->costs.assign(E->ret.conv_itmax + 1, NAN);
+  return JGB_OK;
+}
+
+// Grow-only pinned staging buffer for results.
+int ensure_pinned(jgb_engine* E, size_t words) {
+  if (words <= E->pinned_n) return JGB_OK;
+  if (E->pinned) cudaFreeHost(E->pinned);
+  E->pinned = nullptr;
+  E->pinned_n = 0;
+  const size_t want = words + words / 4 + 1024;
+  ECK(cudaMallocHost(reinterpret_cast<void**>(&E->pinned), want * sizeof(double)));
+  E->pinned_n = want;
+  return JGB_OK;
+}
+
+// Run segment copies (device addresses, lengths in doubles).
+int run_segments(jgb_engine* E, const std::vector<unsigned long long>& seg) {
+  if (seg.empty()) return JGB_OK;
+  cudaStream_t s = E->x->stream;
+  ECK(E->segbuf.reserve(sizeof(unsigned long long) * seg.size()));
+  ECK(cudaMemcpyAsync(E->segbuf.p, seg.data(), sizeof(unsigned long long) * seg.size(),
+                      cudaMemcpyHostToDevice, s));
+  const int nseg = (int)(seg.size() / 3);
+  dim3 grid(8, (unsigned)std::min(nseg, 65535));
+  k_copy_segments<<<grid, 256, 0, s>>>(nseg, E->segbuf.as<unsigned long long>());
+  ECK(cudaGetLastError());
+  // the host vector is reused by the caller: wait for the upload
+  ECK(cudaStreamSynchronize(s));
+  return JGB_OK;
+}
+
+// Build working set `w` for E->active; requests with slot >= 0 bring their
+// iterate state from `old`.
+int build_workset(jgb_engine* E, WorkSet& w, WorkSet* old) {
+  jgb_ctx* x = E->x;
   const CtlDev& c = x->c;
   cudaStream_t s = x->stream;
-  const int nret = hb->nobs;
-  const int nray = hb->ray_off[nret], nlev = hb->lev_off[nret];
+  const int nret = (int)E->active.size();
   const int nscal = 5 + c.ncl + c.nsf, nplanes = 6 + c.ng + c.nw;
-  // ---- layouts (host) ----
-  FdLayout H;
-  int rc = fd_layout(x, nret, hb->lev_off, hb->ray_off, hb->z, hb->rad, H);
-  if (rc) return rc;
-  std::vector<RetDesc> desc(nret);
-  long long nx = 0, ny = 0, nss = 0, nk = 0;
+  w.nret = nret;
+  FdLayout& H = w.H;
+  H.nobs = nret;
+  H.lev_off.assign(nret + 1, 0);
+  H.ray_off.assign(nret + 1, 0);
+  H.lay.assign(nret, {});
+  H.mcnt.assign(nret, 0);
+  H.ncnt.assign(nret, 0);
+  H.yoff.assign(nret + 1, 0);
+  H.kb.assign(nret + 1, 0);
+  H.ymap.clear();
+  w.desc.assign(nret, RetDesc{});
+  w.mvec.assign(nret, 0);
+  w.nvec.assign(nret, 0);
+  long long nx = 0, nss = 0;
   for (int i = 0; i < nret; i++) {
-    desc[i] = RetDesc{H.ncnt[i], H.mcnt[i], nx, (long long)H.yoff[i], nss, H.kb[i]};
-    nx += H.ncnt[i];
-    nss += (long long)H.ncnt[i] * H.ncnt[i];
-    nk += (long long)H.ncnt[i] * H.mcnt[i];
+    const Request* q = E->active[i];
+    H.lev_off[i + 1] = H.lev_off[i] + q->np;
+    H.ray_off[i + 1] = H.ray_off[i] + q->nr;
+    H.lay[i] = q->lay;
+    H.ncnt[i] = q->n;
+    H.mcnt[i] = q->m;
+    H.ymap.insert(H.ymap.end(), q->ymap.begin(), q->ymap.end());
+    H.yoff[i + 1] = H.yoff[i] + q->m;
+    H.kb[i + 1] = H.kb[i] + (long long)q->m * q->n;
+    w.desc[i] = RetDesc{q->n, q->m, nx, (long long)H.yoff[i], nss, H.kb[i]};
+    w.mvec[i] = q->m;
+    w.nvec[i] = q->n;
+    nx += q->n;
+    nss += (long long)q->n * q->n;
   }
-  ny = (long long)H.ymap.size();
-  // measured y and its errors (set_cov_meas, retrieval.c:924-964)
-  std::vector<double> ymeas(ny), winv(ny);
-  for (int i = 0; i < nret; i++)
-    for (int k = 0; k < H.mcnt[i]; k++) {
-      const int2 ym = H.ymap[H.yoff[i] + k];
-      const double v = hb->rad[(size_t)ym.y * nray + hb->ray_off[i] + ym.x];
-      const double sn = ret->err_noise ? ret->err_noise[ym.y] : 0.0;
-      const double sf = fabs((ret->err_formod ? ret->err_formod[ym.y] : 0.0) / 100 * v);
-      ymeas[H.yoff[i] + k] = v;
-      winv[H.yoff[i] + k] = 1 / sqrt(sn * sn + sf * sf);
-      if (!(winv[H.yoff[i] + k] > 0))
-        return ctx_error(x, JGB_ERR_ARG, "Check measurement errors (zero standard deviation)!");
-    }
-  // state element tables and a-priori sigmas
+  w.nlev = H.lev_off[nret];
+  w.nray = H.ray_off[nret];
+  w.nx = nx;
+  w.nss = nss;
+  w.ny = H.yoff[nret];
+  w.nk = H.kb[nret];
+  const bool err_ana = E->ret.err_ana != 0;
+  // host staging of the inputs
+  std::vector<double> lev((size_t)w.nlev * nplanes), scal((size_t)nret * nscal), geo(7 * (size_t)w.nray),
+      radm((size_t)c.nd * w.nray), yv(4 * (size_t)w.ny);
   std::vector<int4> elems(nx);
   std::vector<SaElem> sael(nx);
-  std::vector<char> sa_diag(nret, 1);
   for (int i = 0; i < nret; i++) {
-    const int l0 = hb->lev_off[i];
-    for (int j = 0; j < H.ncnt[i]; j++) {
-      const Elem& e = H.lay[i][j];
-      elems[desc[i].xo + j] = make_int4(e.arr, e.idx, e.arr == 4 ? e.idx : e.lev, e.hkind);
-      SaElem se{};
-      const double* scal = hb->scal + (size_t)i * nscal;
-      double xv = 0;
-      switch (e.arr) {
-        case 0: xv = hb->p[l0 + e.lev]; break;
-        case 1: xv = hb->t[l0 + e.lev]; break;
-        case 2: xv = hb->q[(size_t)e.idx * nlev + l0 + e.lev]; break;
-        case 3: xv = hb->k[(size_t)e.idx * nlev + l0 + e.lev]; break;
-        default: xv = scal[e.idx]; break;
-      }
-      int iq;
-      if (e.arr == 0) { iq = 0; se.sigma = ret->err_press / 100 * xv; se.cz = ret->err_press_cz; se.ch = ret->err_press_ch; }
-      else if (e.arr == 1) { iq = 1; se.sigma = ret->err_temp; se.cz = ret->err_temp_cz; se.ch = ret->err_temp_ch; }
-      else if (e.arr == 2) { iq = 2 + e.idx; se.sigma = ret->err_q[e.idx] / 100 * xv; se.cz = ret->err_q_cz[e.idx]; se.ch = ret->err_q_ch[e.idx]; }
-      else if (e.arr == 3) { iq = 2 + c.ng + e.idx; se.sigma = ret->err_k[e.idx]; se.cz = ret->err_k_cz[e.idx]; se.ch = ret->err_k_ch[e.idx]; }
-      else {
-        const int o = 2 + c.ncl;
-        se.cz = se.ch = 0;
-        if (e.idx == 0) { iq = 2 + c.ng + c.nw; se.sigma = ret->err_clz; }
-        else if (e.idx == 1) { iq = 3 + c.ng + c.nw; se.sigma = ret->err_cldz; }
-        else if (e.idx < o) { iq = 4 + c.ng + c.nw + (e.idx - 2); se.sigma = ret->err_clk[e.idx - 2]; }
-        else if (e.idx == o) { iq = 4 + c.ng + c.nw + c.ncl; se.sigma = ret->err_sfz; }
-        else if (e.idx == o + 1) { iq = 5 + c.ng + c.nw + c.ncl; se.sigma = ret->err_sfp; }
-        else if (e.idx == o + 2) { iq = 6 + c.ng + c.nw + c.ncl; se.sigma = ret->err_sft; }
-        else { iq = 7 + c.ng + c.nw + c.ncl + (e.idx - o - 3); se.sigma = ret->err_sfeps[e.idx - o - 3]; }
-      }
-      if (!(se.sigma * se.sigma > 0))
-        return ctx_error(x, JGB_ERR_ARG, "Check a priori data (zero standard deviation)!");
-      se.iq = iq;
-      const int lv = e.arr == 4 ? 0 : e.lev;
-      se.lon = hb->lon[l0 + lv];
-      se.lat = hb->lat[l0 + lv];
-      se.z = hb->z[l0 + lv];
-      sael[desc[i].xo + j] = se;
-    }
-    // diagonal iff no pair of the same quantity has both correlation lengths > 0
-    for (int j = 0; j < H.ncnt[i] && sa_diag[i]; j++) {
-      const SaElem& a = sael[desc[i].xo + j];
-      if (a.cz > 0 && a.ch > 0)
-        for (int k = 0; k < H.ncnt[i]; k++)
-          if (k != j && sael[desc[i].xo + k].iq == a.iq) { sa_diag[i] = 0; break; }
-    }
+    const Request* q = E->active[i];
+    const int l0 = H.lev_off[i], r0 = H.ray_off[i];
+    for (int k = 0; k < nplanes; k++)
+      std::memcpy(&lev[(size_t)k * w.nlev + l0], &q->lev[(size_t)k * q->np], sizeof(double) * q->np);
+    std::memcpy(&scal[(size_t)i * nscal], q->scal.data(), sizeof(double) * nscal);
+    for (int k = 0; k < 7; k++)
+      std::memcpy(&geo[(size_t)k * w.nray + r0], &q->geo[(size_t)k * q->nr], sizeof(double) * q->nr);
+    for (int k = 0; k < c.nd; k++)
+      std::memcpy(&radm[(size_t)k * w.nray + r0], &q->rad[(size_t)k * q->nr], sizeof(double) * q->nr);
+    const size_t yo = H.yoff[i];
+    std::memcpy(&yv[yo], q->ymeas.data(), sizeof(double) * q->m);
+    std::memcpy(&yv[w.ny + yo], q->winv.data(), sizeof(double) * q->m);
+    std::memcpy(&yv[2 * w.ny + yo], q->sn.data(), sizeof(double) * q->m);
+    std::memcpy(&yv[3 * w.ny + yo], q->sf.data(), sizeof(double) * q->m);
+    std::copy(q->elems.begin(), q->elems.end(), elems.begin() + w.desc[i].xo);
+    std::copy(q->sael.begin(), q->sael.end(), sael.begin() + w.desc[i].xo);
   }
-  // ---- device buffers ----
-  DevBuf mem;
-  const size_t dbl = sizeof(double);
-  const size_t bytes = dbl * ((size_t)nlev * nplanes * 2 + (size_t)nret * nscal * 2 + 7 * (size_t)nray +
-                              (size_t)c.nd * nray * 4 + (size_t)nx * 8 + (size_t)ny * 4 + (size_t)nss * 5 +
-                              (size_t)nk + (size_t)nret * 4) +
-                       sizeof(int4) * nx + sizeof(SaElem) * nx + sizeof(RetDesc) * nret +
-                       sizeof(int) * (4 * (size_t)nret + 4) + sizeof(int2) * ny + normal_desc_bytes(nret) +
-                       64 * 256;  // alignment padding of the sub-arrays carved below (< 64 of them)
-  RCK(mem.reserve(bytes));
-  char* mp = mem.as<char>();
+  const size_t bytes = workset_bytes(c, nret, w.nlev, w.nray, nx, w.ny, nss, w.nk, err_ana);
+  ECK(w.mem.reserve(bytes));
+  char* mp = w.mem.as<char>();
   auto take = [&](size_t nbytes) {
     char* p = mp;
     mp += (nbytes + 255) & ~size_t(255);
     return p;
   };
-  double* apr_lev = (double*)take(dbl * (size_t)nlev * nplanes);
-  double* cur_lev = (double*)take(dbl * (size_t)nlev * nplanes);
-  double* apr_scal = (double*)take(dbl * (size_t)nret * nscal);
-  double* cur_scal = (double*)take(dbl * (size_t)nret * nscal);
-  double* geo = (double*)take(dbl * 7 * (size_t)nray);
-  double* radm = (double*)take(dbl * (size_t)c.nd * nray);
-  double* rad = (double*)take(dbl * (size_t)c.nd * nray);
-  double* tau = (double*)take(dbl * (size_t)c.nd * nray);
-  double* tp = (double*)take(dbl * 3 * (size_t)nray);
-  double* xa = (double*)take(dbl * nx);
-  double* xi = (double*)take(dbl * nx);
-  double* dx = (double*)take(dbl * nx);
-  double* bvec = (double*)take(dbl * nx);
-  double* step = (double*)take(dbl * nx);
-  double* xfin = (double*)take(dbl * nx);
-  double* ym_d = (double*)take(dbl * ny);
-  double* yi = (double*)take(dbl * ny);
-  double* dy = (double*)take(dbl * ny);
-  double* w_d = (double*)take(dbl * ny);
-  double* sainv = (double*)take(dbl * nss);
-  double* cov = (double*)take(dbl * nss);
-  double* Amat = (double*)take(dbl * nss);
-  double* work = (double*)take(dbl * nss);
-  double* Kd = (double*)take(dbl * std::max(nk, 1LL));
-  double* chisq_d = (double*)take(dbl * nret);
-  double* lmpar_d = (double*)take(dbl * nret);
-  double* disq_d = (double*)take(dbl * nret);
-  int4* elems_d = (int4*)take(sizeof(int4) * nx);
-  SaElem* sael_d = (SaElem*)take(sizeof(SaElem) * nx);
-  RetDesc* desc_d = (RetDesc*)take(sizeof(RetDesc) * nret);
-  int* active_d = (int*)take(sizeof(int) * nret);
-  int* status_d = (int*)take(sizeof(int) * nret);
-  int* levoff_d = (int*)take(sizeof(int) * (nret + 1));
-  int* rayoff_d = (int*)take(sizeof(int) * (nret + 1));
-  int2* ymap_d = (int2*)take(sizeof(int2) * ny);
-  void* nedesc_d = take(normal_desc_bytes(nret));
-  // upload
-  const size_t L = (size_t)nlev * dbl;
-  const double* src_lev[6] = {hb->time, hb->z, hb->lon, hb->lat, hb->p, hb->t};
-  for (int k = 0; k < 6; k++) RCK(cudaMemcpyAsync(apr_lev + (size_t)k * nlev, src_lev[k], L, cudaMemcpyHostToDevice, s));
-  if (c.ng) RCK(cudaMemcpyAsync(apr_lev + 6 * (size_t)nlev, hb->q, L * c.ng, cudaMemcpyHostToDevice, s));
-  if (c.nw) RCK(cudaMemcpyAsync(apr_lev + (6 + (size_t)c.ng) * nlev, hb->k, L * c.nw, cudaMemcpyHostToDevice, s));
-  RCK(cudaMemcpyAsync(apr_scal, hb->scal, dbl * (size_t)nret * nscal, cudaMemcpyHostToDevice, s));
-  RCK(cudaMemcpyAsync(geo, hb->geo, dbl * 7 * (size_t)nray, cudaMemcpyHostToDevice, s));
-  RCK(cudaMemcpyAsync(radm, hb->rad, dbl * (size_t)c.nd * nray, cudaMemcpyHostToDevice, s));
-  RCK(cudaMemcpyAsync(ym_d, ymeas.data(), dbl * ny, cudaMemcpyHostToDevice, s));
-  RCK(cudaMemcpyAsync(w_d, winv.data(), dbl * ny, cudaMemcpyHostToDevice, s));
-  RCK(cudaMemcpyAsync(elems_d, elems.data(), sizeof(int4) * nx, cudaMemcpyHostToDevice, s));
-  RCK(cudaMemcpyAsync(sael_d, sael.data(), sizeof(SaElem) * nx, cudaMemcpyHostToDevice, s));
-  RCK(cudaMemcpyAsync(desc_d, desc.data(), sizeof(RetDesc) * nret, cudaMemcpyHostToDevice, s));
-  RCK(cudaMemcpyAsync(levoff_d, hb->lev_off, sizeof(int) * (nret + 1), cudaMemcpyHostToDevice, s));
-  RCK(cudaMemcpyAsync(rayoff_d, hb->ray_off, sizeof(int) * (nret + 1), cudaMemcpyHostToDevice, s));
-  RCK(cudaMemcpyAsync(ymap_d, H.ymap.data(), sizeof(int2) * ny, cudaMemcpyHostToDevice, s));
-  RCK(cudaMemcpyAsync(cur_lev, apr_lev, dbl * (size_t)nlev * nplanes, cudaMemcpyDeviceToDevice, s));
-  RCK(cudaMemcpyAsync(cur_scal, apr_scal, dbl * (size_t)nret * nscal, cudaMemcpyDeviceToDevice, s));
-  RCK(cudaMemsetAsync(status_d, 0, sizeof(int) * nret, s));
-  std::vector<int> active(nret, 1), trying(nret, 0), converged(nret, 0);
-  std::vector<double> lmpar(nret, 0.001), chisq(nret), chisq_old(nret), disq(nret);
-  std::vector<int> niter(nret, 0);
-  const int ncost = ret->conv_itmax + 1;
-  if (costs)
-    for (long long k = 0; k < (long long)nret * ncost; k++) costs[k] = NAN;
-  auto put_active = [&](const std::vector<int>& a) {
-    return cudaMemcpyAsync(active_d, a.data(), sizeof(int) * nret, cudaMemcpyHostToDevice, s);
+  const size_t dbl = sizeof(double);
+  w.apr_lev = (double*)take(dbl * (size_t)w.nlev * nplanes);
+  w.cur_lev = (double*)take(dbl * (size_t)w.nlev * nplanes);
+  w.apr_scal = (double*)take(dbl * (size_t)nret * nscal);
+  w.cur_scal = (double*)take(dbl * (size_t)nret * nscal);
+  w.geo = (double*)take(dbl * 7 * (size_t)w.nray);
+  w.radm = (double*)take(dbl * (size_t)c.nd * w.nray);
+  w.rad = (double*)take(dbl * (size_t)c.nd * w.nray);
+  w.tau = (double*)take(dbl * (size_t)c.nd * w.nray);
+  w.tp = (double*)take(dbl * 3 * (size_t)w.nray);
+  double** xs[11] = {&w.xa, &w.xi, &w.dx, &w.bvec, &w.step, &w.xfin, &w.e_tot, &w.e_noise, &w.e_formod, &w.cont, &w.res};
+  for (double** p : xs) *p = (double*)take(dbl * nx);
+  w.ym = (double*)take(dbl * 4 * w.ny);
+  w.w = w.ym + w.ny;
+  w.sn = w.ym + 2 * w.ny;
+  w.sf = w.ym + 3 * w.ny;
+  w.yi = (double*)take(dbl * w.ny);
+  w.dy = (double*)take(dbl * w.ny);
+  double** ss[5] = {&w.sainv, &w.cov, &w.covn, &w.Amat, &w.work};
+  for (double** p : ss) *p = (double*)take(dbl * nss);
+  w.Kd = (double*)take(dbl * std::max(w.nk, 1LL));
+  w.G = err_ana ? (double*)take(dbl * std::max(w.nk, 1LL)) : nullptr;
+  w.chisq = (double*)take(dbl * nret);
+  w.lmpar = (double*)take(dbl * nret);
+  w.disq = (double*)take(dbl * nret);
+  w.elems = (int4*)take(sizeof(int4) * nx);
+  w.sael = (SaElem*)take(sizeof(SaElem) * nx);
+  w.desc_d = (RetDesc*)take(sizeof(RetDesc) * nret);
+  w.active = (int*)take(sizeof(int) * nret);
+  w.status = (int*)take(sizeof(int) * nret);
+  w.levoff = (int*)take(sizeof(int) * (nret + 1));
+  w.rayoff = (int*)take(sizeof(int) * (nret + 1));
+  w.rayobs = (int*)take(sizeof(int) * w.nray);
+  w.cnt = (int*)take(sizeof(int) * w.nray);
+  w.skip = (unsigned char*)take(nret);
+  w.mask = (unsigned char*)take((size_t)c.nd * w.nray);
+  w.ymap = (int2*)take(sizeof(int2) * w.ny);
+  w.nedesc = take(normal_desc_bytes(nret));
+  if ((size_t)(mp - w.mem.as<char>()) > w.mem.n)
+    return ctx_error(x, JGB_ERR_CUDA, "retrieval working set overflow");
+  ECK(cudaMemcpyAsync(w.apr_lev, lev.data(), dbl * lev.size(), cudaMemcpyHostToDevice, s));
+  ECK(cudaMemcpyAsync(w.apr_scal, scal.data(), dbl * scal.size(), cudaMemcpyHostToDevice, s));
+  ECK(cudaMemcpyAsync(w.geo, geo.data(), dbl * geo.size(), cudaMemcpyHostToDevice, s));
+  ECK(cudaMemcpyAsync(w.radm, radm.data(), dbl * radm.size(), cudaMemcpyHostToDevice, s));
+  ECK(cudaMemcpyAsync(w.ym, yv.data(), dbl * yv.size(), cudaMemcpyHostToDevice, s));
+  ECK(cudaMemcpyAsync(w.elems, elems.data(), sizeof(int4) * nx, cudaMemcpyHostToDevice, s));
+  ECK(cudaMemcpyAsync(w.sael, sael.data(), sizeof(SaElem) * nx, cudaMemcpyHostToDevice, s));
+  ECK(cudaMemcpyAsync(w.desc_d, w.desc.data(), sizeof(RetDesc) * nret, cudaMemcpyHostToDevice, s));
+  ECK(cudaMemcpyAsync(w.levoff, H.lev_off.data(), sizeof(int) * (nret + 1), cudaMemcpyHostToDevice, s));
+  ECK(cudaMemcpyAsync(w.rayoff, H.ray_off.data(), sizeof(int) * (nret + 1), cudaMemcpyHostToDevice, s));
+  ECK(cudaMemcpyAsync(w.ymap, H.ymap.data(), sizeof(int2) * w.ny, cudaMemcpyHostToDevice, s));
+  ECK(cudaMemsetAsync(w.status, 0, sizeof(int) * nret, s));
+  ECK(cudaMemsetAsync(w.cnt, 0, sizeof(int) * w.nray, s));
+  launch_ray_obs_mask(nret, w.rayoff, w.rayobs, (long long)c.nd * w.nray, w.radm, w.mask, s);
+  ECK(cudaGetLastError());
+  // fresh requests start from the a priori
+  ECK(cudaMemcpyAsync(w.cur_lev, w.apr_lev, dbl * lev.size(), cudaMemcpyDeviceToDevice, s));
+  ECK(cudaMemcpyAsync(w.cur_scal, w.apr_scal, dbl * scal.size(), cudaMemcpyDeviceToDevice, s));
+  // requests that stay bring their iterate state
+  std::vector<unsigned long long> seg;
+  auto add = [&](const double* src, double* dst, long long nwords) {
+    if (nwords <= 0) return;
+    seg.push_back((unsigned long long)src);
+    seg.push_back((unsigned long long)dst);
+    seg.push_back((unsigned long long)nwords);
   };
-  AtmArrays apr{apr_lev, apr_scal, nlev, nscal, c.ng};
-  AtmArrays cur{cur_lev, cur_scal, nlev, nscal, c.ng};
+  std::vector<int> cnt_keep;
+  if (old)
+    for (int i = 0; i < nret; i++) {
+      const Request* q = E->active[i];
+      const int j = q->slot;
+      if (j < 0 || q->state == 0) continue;
+      const long long ol = old->H.lev_off[j], orr = old->H.ray_off[j];
+      const long long nl = H.lev_off[i], nr = H.ray_off[i];
+      for (int k = 0; k < nplanes; k++) add(old->cur_lev + k * old->nlev + ol, w.cur_lev + k * w.nlev + nl, q->np);
+      add(old->cur_scal + (long long)j * nscal, w.cur_scal + (long long)i * nscal, nscal);
+      for (int k = 0; k < c.nd; k++) {
+        add(old->rad + k * old->nray + orr, w.rad + k * w.nray + nr, q->nr);
+        add(old->tau + k * old->nray + orr, w.tau + k * w.nray + nr, q->nr);
+      }
+      for (int k = 0; k < 3; k++) add(old->tp + k * old->nray + orr, w.tp + k * w.nray + nr, q->nr);
+      const RetDesc& od = old->desc[j];
+      const RetDesc& nd = w.desc[i];
+      add(old->xa + od.xo, w.xa + nd.xo, od.n);
+      add(old->xi + od.xo, w.xi + nd.xo, od.n);
+      add(old->dx + od.xo, w.dx + nd.xo, od.n);
+      add(old->yi + od.yo, w.yi + nd.yo, od.m);
+      add(old->dy + od.yo, w.dy + nd.yo, od.m);
+      add(old->sainv + od.so, w.sainv + nd.so, (long long)od.n * od.n);
+      // K and K^T W K are reused unless the next iteration recomputes them
+      const int nit = q->it + 1;
+      if (!(nit == 1 || nit % E->ret.kernel_recomp == 0)) {
+        add(old->cov + od.so, w.cov + nd.so, (long long)od.n * od.n);
+        add(old->Kd + od.ko, w.Kd + nd.ko, (long long)od.n * od.m);
+      }
+      // LOS point counts (ints) travel as pairs packed in doubles where
+      // aligned; simpler to copy them through the host below
+      cnt_keep.push_back(i);
+    }
+  int rc = run_segments(E, seg);
+  if (rc) return rc;
+  if (!cnt_keep.empty()) {
+    std::vector<int> oc(old->nray), nc(w.nray, 0);
+    ECK(cudaMemcpy(oc.data(), old->cnt, sizeof(int) * old->nray, cudaMemcpyDeviceToHost));
+    for (int i : cnt_keep) {
+      const int j = E->active[i]->slot;
+      std::memcpy(&nc[H.ray_off[i]], &oc[old->H.ray_off[j]], sizeof(int) * E->active[i]->nr);
+    }
+    ECK(cudaMemcpyAsync(w.cnt, nc.data(), sizeof(int) * w.nray, cudaMemcpyHostToDevice, s));
+    ECK(cudaStreamSynchronize(s));
+  }
+  for (int i = 0; i < nret; i++) E->active[i]->slot = i;
+  return JGB_OK;
+}
+
+int put_flags(jgb_engine* E, WorkSet& w, const std::vector<int>& f) {
+  ECK(cudaMemcpyAsync(w.active, f.data(), sizeof(int) * w.nret, cudaMemcpyHostToDevice, E->x->stream));
+  return JGB_OK;
+}
+
+AtmArrays apr_arrays(const jgb_engine* E, const WorkSet& w) {
+  const CtlDev& c = E->x->c;
+  return AtmArrays{w.apr_lev, w.apr_scal, w.nlev, 5 + c.ncl + c.nsf, c.ng};
+}
+AtmArrays cur_arrays(const jgb_engine* E, const WorkSet& w) {
+  const CtlDev& c = E->x->c;
+  return AtmArrays{w.cur_lev, w.cur_scal, w.nlev, 5 + c.ncl + c.nsf, c.ng};
+}
+
+// Forward model of the flagged requests of the working set; y_i gathered.
+// Leaves w.active = flags.
+int forward(jgb_engine* E, WorkSet& w, const std::vector<int>& flags) {
+  jgb_ctx* x = E->x;
+  const CtlDev& c = x->c;
+  cudaStream_t s = x->stream;
+  const int nret = w.nret;
+  std::vector<unsigned char> skip(nret);
+  for (int i = 0; i < nret; i++) skip[i] = flags[i] ? 0 : 1;
+  ECK(cudaMemcpyAsync(w.skip, skip.data(), nret, cudaMemcpyHostToDevice, s));
+  int rc = put_flags(E, w, flags);
+  if (rc) return rc;
   BatchDev bd{};
   bd.nobs = nret;
-  bd.nlev = nlev;
-  bd.nray = nray;
-  bd.nscal = nscal;
-  bd.lev_off = levoff_d;
-  bd.time = cur_lev;
-  bd.z = cur_lev + nlev;
-  bd.lon = cur_lev + 2 * (size_t)nlev;
-  bd.lat = cur_lev + 3 * (size_t)nlev;
-  bd.p = cur_lev + 4 * (size_t)nlev;
-  bd.t = cur_lev + 5 * (size_t)nlev;
-  bd.q = cur_lev + 6 * (size_t)nlev;
-  bd.k = cur_lev + (6 + (size_t)c.ng) * nlev;
-  bd.scal = cur_scal;
-  bd.geo = geo;
-  bd.rad = rad;
-  bd.tau = tau;
-  bd.tp = tp;
-  RCK(x->b_rayobs.reserve(sizeof(int) * nray));
-  RCK(x->b_mask.reserve((size_t)c.nd * nray));
-  bd.ray_obs = x->b_rayobs.as<int>();
-  bd.mask = x->b_mask.as<unsigned char>();
-  std::vector<int> cnt(nray);
-  // forward model of the current iterates: results in rad, y_i gathered
-  auto forward = [&]() -> int {
-    RCK(cudaMemcpyAsync(rad, radm, dbl * (size_t)c.nd * nray, cudaMemcpyDeviceToDevice, s));
-    launch_ray_obs_mask(nret, rayoff_d, const_cast<int*>(bd.ray_obs), (long long)c.nd * nray, rad,
-                        const_cast<unsigned char*>(bd.mask), s);
-    const int r2 = run_core(x, bd, precision, false);
-    if (r2) return r2;
-    k_gather_y<<<nret, 128, 0, s>>>(nret, desc_d, rayoff_d, ymap_d, rad, nray, yi);
-    RCK(cudaGetLastError());
-    return JGB_OK;
-  };
-  auto jacobian = [&](const std::vector<int>& list) -> int {
-    RCK(cudaMemcpy(cnt.data(), x->los_cnt.p, sizeof(int) * nray, cudaMemcpyDeviceToHost));
-    FdInput in{cur_lev, cur_scal, geo, radm, levoff_d, rayoff_d, rad, cnt.data()};
-    return fd_core(x, H, in, list, Kd, precision);
-  };
-  auto normal = [&](const std::vector<int>& a) -> int {
-    // cov = K^T W K and bvec = K^T W dy for the listed retrievals (all
-    // retrievals are computed; inactive ones are recomputed harmlessly)
-    std::vector<int> m(nret), n(nret);
-    for (int i = 0; i < nret; i++) {
-      m[i] = H.mcnt[i];
-      n[i] = H.ncnt[i];
-    }
-    (void)a;
-    return normal_equations_dev(nret, m.data(), n.data(), Kd, w_d, dy, cov, bvec, precision, nedesc_d, s);
-  };
-
-  // ---- initialisation (retrieval.c:503-556) ----
-  rc = forward();
+  bd.nlev = (int)w.nlev;
+  bd.nray = (int)w.nray;
+  bd.nscal = 5 + c.ncl + c.nsf;
+  bd.lev_off = w.levoff;
+  bd.ray_obs = w.rayobs;
+  bd.time = w.cur_lev;
+  bd.z = w.cur_lev + w.nlev;
+  bd.lon = w.cur_lev + 2 * w.nlev;
+  bd.lat = w.cur_lev + 3 * w.nlev;
+  bd.p = w.cur_lev + 4 * w.nlev;
+  bd.t = w.cur_lev + 5 * w.nlev;
+  bd.q = w.cur_lev + 6 * w.nlev;
+  bd.k = w.cur_lev + (6 + (long long)c.ng) * w.nlev;
+  bd.scal = w.cur_scal;
+  bd.geo = w.geo;
+  bd.rad = w.rad;
+  bd.tau = w.tau;
+  bd.tp = w.tp;
+  bd.mask = w.mask;
+  bd.obs_skip = w.skip;
+  rc = run_core(x, bd, E->precision, false);
   if (rc) return rc;
-  RCK(put_active(active));
-  k_gather_state<<<nret, 128, 0, s>>>(nret, desc_d, levoff_d, elems_d, apr, xa);
-  k_gather_state<<<nret, 128, 0, s>>>(nret, desc_d, levoff_d, elems_d, cur, xi);
-  {
-    dim3 g(64, nret);
-    k_build_sa<<<g, 256, 0, s>>>(nret, desc_d, sael_d, sainv);
-  }
-  std::vector<int> nondiag(nret), diag(nret);
-  bool any_nondiag = false;
-  for (int i = 0; i < nret; i++) {
-    nondiag[i] = !sa_diag[i];
-    diag[i] = sa_diag[i];
-    any_nondiag |= !sa_diag[i];
-  }
-  RCK(put_active(diag));
-  k_diag_inverse<<<nret, 128, 0, s>>>(nret, desc_d, active_d, sainv);
-  if (any_nondiag) {
-    RCK(put_active(nondiag));
-    RCK(cudaMemcpyAsync(work, sainv, dbl * nss, cudaMemcpyDeviceToDevice, s));
-    k_chol_factor<<<nret, 256, 0, s>>>(nret, desc_d, active_d, work, status_d);
-    k_chol_inverse<<<nret, 128, 0, s>>>(nret, desc_d, active_d, work, Amat, sainv);
-  }
-  RCK(put_active(active));
-  k_residuals<<<nret, 128, 0, s>>>(nret, desc_d, active_d, xi, xa, ym_d, yi, dx, dy);
-  k_cost<<<(nret + 63) / 64, 64, 0, s>>>(nret, desc_d, active_d, dx, dy, sainv, w_d, chisq_d);
-  RCK(cudaMemcpyAsync(chisq.data(), chisq_d, dbl * nret, cudaMemcpyDeviceToHost, s));
-  RCK(cudaStreamSynchronize(s));
-  for (int i = 0; i < nret; i++)
-    if (costs) costs[(size_t)i * ncost] = chisq[i];
-  {
-    std::vector<int> all(nret);
-    for (int i = 0; i < nret; i++) all[i] = i;
-    rc = jacobian(all);
-    if (rc) return rc;
-  }
-  // ---- Levenberg-Marquardt (retrieval.c:559-652) ----
-  for (int it = 1; it <= ret->conv_itmax; it++) {
-    std::vector<int> act;
-    for (int i = 0; i < nret; i++)
-      if (active[i]) act.push_back(i);
-    if (act.empty()) break;
-    chisq_old = chisq;
-    if (it > 1 && it % ret->kernel_recomp == 0) {
-      rc = jacobian(act);
-      if (rc) return rc;
-    }
-    RCK(put_active(active));
-    if (it == 1 || it % ret->kernel_recomp == 0) {
-      rc = normal(active);
-      if (rc) return rc;
-    } else {
-      // b needs K^T W dy with the current dy even when cov is kept
-      RCK(cudaMemcpyAsync(work, cov, dbl * nss, cudaMemcpyDeviceToDevice, s));
-      rc = normal(active);
-      if (rc) return rc;
-      RCK(cudaMemcpyAsync(cov, work, dbl * nss, cudaMemcpyDeviceToDevice, s));
-    }
-    k_gradient<<<nret, 128, 0, s>>>(nret, desc_d, active_d, sainv, dx, bvec);
-    trying = active;
-    for (int it2 = 0; it2 < 20; it2++) {
-      bool any = false;
-      for (int i = 0; i < nret; i++) any |= trying[i] != 0;
-      if (!any) break;
-      RCK(put_active(trying));
-      RCK(cudaMemcpyAsync(lmpar_d, lmpar.data(), dbl * nret, cudaMemcpyHostToDevice, s));
-      {
-        dim3 g(64, nret);
-        k_lm_matrix<<<g, 256, 0, s>>>(nret, desc_d, active_d, lmpar_d, sainv, cov, Amat);
-      }
-      k_chol_factor<<<nret, 256, 0, s>>>(nret, desc_d, active_d, Amat, status_d);
-      k_chol_solve<<<(nret + 63) / 64, 64, 0, s>>>(nret, desc_d, active_d, Amat, bvec, step);
-      k_axpy_state<<<nret, 128, 0, s>>>(nret, desc_d, active_d, +1.0, step, xi);
-      k_set_iterate<<<nret, 256, 0, s>>>(nret, desc_d, levoff_d, elems_d, active_d, apr, cur, xi,
-                                          c.nw, c.ncl, c.nsf);
-      rc = forward();
-      if (rc) return rc;
-      k_residuals<<<nret, 128, 0, s>>>(nret, desc_d, active_d, xi, xa, ym_d, yi, dx, dy);
-      k_cost<<<(nret + 63) / 64, 64, 0, s>>>(nret, desc_d, active_d, dx, dy, sainv, w_d, chisq_d);
-      std::vector<double> cnew(nret);
-      std::vector<int> st(nret);
-      RCK(cudaMemcpyAsync(cnew.data(), chisq_d, dbl * nret, cudaMemcpyDeviceToHost, s));
-      RCK(cudaMemcpyAsync(st.data(), status_d, sizeof(int) * nret, cudaMemcpyDeviceToHost, s));
-      RCK(cudaStreamSynchronize(s));
-      std::vector<int> reject(nret, 0);
-      for (int i = 0; i < nret; i++) {
-        if (!trying[i]) continue;
-        if (st[i]) return ctx_error(x, JGB_ERR_NUMERIC, "normal matrix is not positive definite");
-        chisq[i] = cnew[i];
-        if (chisq[i] > chisq_old[i]) {
-          lmpar[i] *= 10;
-          reject[i] = 1;
-        } else {
-          lmpar[i] /= 10;
-          trying[i] = 0;
-        }
-      }
-      RCK(put_active(reject));
-      k_axpy_state<<<nret, 128, 0, s>>>(nret, desc_d, active_d, -1.0, step, xi);
-      for (int i = 0; i < nret; i++)
-        if (!reject[i]) trying[i] = 0;
-    }
-    RCK(put_active(active));
-    k_dot_state<<<(nret + 63) / 64, 64, 0, s>>>(nret, desc_d, active_d, step, bvec, disq_d);
-    RCK(cudaMemcpyAsync(disq.data(), disq_d, dbl * nret, cudaMemcpyDeviceToHost, s));
-    RCK(cudaStreamSynchronize(s));
-    for (int i : act) {
-      if (costs) costs[(size_t)i * ncost + it] = chisq[i];
-      niter[i] = it;
-      const double dq = disq[i] / (double)H.ncnt[i];
-      if ((it == 1 || it % ret->kernel_recomp == 0) && dq < ret->conv_dmin) active[i] = 0;
-    }
-  }
-  // ---- results (retrieval.c:658-661, 668-684) ----
-  std::vector<int> all(nret, 1);
-  RCK(put_active(all));
-  k_gather_state<<<nret, 128, 0, s>>>(nret, desc_d, levoff_d, elems_d, cur, xfin);
-  RCK(cudaMemcpyAsync(x_out, xfin, dbl * nx, cudaMemcpyDeviceToHost, s));
-  RCK(cudaMemcpyAsync(hb->rad, rad, dbl * (size_t)c.nd * nray, cudaMemcpyDeviceToHost, s));
-  RCK(cudaMemcpyAsync(hb->tau, tau, dbl * (size_t)c.nd * nray, cudaMemcpyDeviceToHost, s));
-  RCK(cudaMemcpyAsync(hb->tp, tp, dbl * 3 * (size_t)nray, cudaMemcpyDeviceToHost, s));
-  RCK(cudaMemcpyAsync(hb->p, cur_lev + 4 * (size_t)nlev, L, cudaMemcpyDeviceToHost, s));
-  if (ret->err_ana && cov_out) {
-    rc = normal(all);
-    if (rc) return rc;
-    k_add<<<(unsigned)((nss + 255) / 256), 256, 0, s>>>(nss, sainv, cov);
-    k_chol_factor<<<nret, 256, 0, s>>>(nret, desc_d, active_d, cov, status_d);
-    k_chol_inverse<<<nret, 128, 0, s>>>(nret, desc_d, active_d, cov, work, Amat);
-    RCK(cudaMemcpyAsync(cov_out, Amat, dbl * nss, cudaMemcpyDeviceToHost, s));
-  }
-  RCK(cudaStreamSynchronize(s));
-  if (iters)
-    for (int i = 0; i < nret; i++) iters[i] = niter[i];
+  E->st.forward_calls++;
+  k_keep_counts<<<(unsigned)((w.nray + 255) / 256), 256, 0, s>>>((int)w.nray, w.rayobs, w.skip,
+                                                                  x->los_cnt.as<int>(), w.cnt);
+  k_gather_y<<<nret, 128, 0, s>>>(nret, w.desc_d, w.rayoff, w.ymap, w.active, w.rad, w.nray, w.yi);
+  ECK(cudaGetLastError());
   return JGB_OK;
+}
+
+int jacobian(jgb_engine* E, WorkSet& w, const std::vector<int>& flags) {
+  std::vector<int> list;
+  for (int i = 0; i < w.nret; i++)
+    if (flags[i]) list.push_back(i);
+  if (list.empty()) return JGB_OK;
+  std::vector<int> cnt(w.nray);
+  ECK(cudaMemcpyAsync(cnt.data(), w.cnt, sizeof(int) * w.nray, cudaMemcpyDeviceToHost, E->x->stream));
+  ECK(cudaStreamSynchronize(E->x->stream));
+  FdInput in{w.cur_lev, w.cur_scal, w.geo, w.radm, w.levoff, w.rayoff, w.rad, cnt.data()};
+  E->st.jacobians += list.size();
+  return fd_core(E->x, w.H, in, list, w.Kd, E->precision);
+}
+
+// Initialisation of the flagged requests (retrieval.c:503-556).
+int init_requests(jgb_engine* E, WorkSet& w, const std::vector<int>& F) {
+  jgb_ctx* x = E->x;
+  cudaStream_t s = x->stream;
+  const int nret = w.nret;
+  int rc = forward(E, w, F);
+  if (rc) return rc;
+  k_gather_state<<<nret, 128, 0, s>>>(nret, w.desc_d, w.levoff, w.elems, w.active, apr_arrays(E, w), w.xa);
+  k_gather_state<<<nret, 128, 0, s>>>(nret, w.desc_d, w.levoff, w.elems, w.active, cur_arrays(E, w), w.xi);
+  k_build_sa<<<dim3(64, nret), 256, 0, s>>>(nret, w.desc_d, w.active, w.sael, w.sainv);
+  std::vector<int> diag(nret, 0), nondiag(nret, 0);
+  bool any_nd = false;
+  for (int i = 0; i < nret; i++) {
+    if (!F[i]) continue;
+    if (E->active[i]->sa_diag) diag[i] = 1;
+    else nondiag[i] = 1, any_nd = true;
+  }
+  rc = put_flags(E, w, diag);
+  if (rc) return rc;
+  k_diag_inverse<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, w.sainv);
+  if (any_nd) {
+    rc = put_flags(E, w, nondiag);
+    if (rc) return rc;
+    k_select_nn<<<dim3(16, nret), 256, 0, s>>>(nret, w.desc_d, w.active, w.sainv, w.work);
+    k_chol_factor<<<nret, 256, 0, s>>>(nret, w.desc_d, w.active, w.work, w.status);
+    k_chol_inverse<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, w.work, w.Amat, w.sainv);
+  }
+  rc = put_flags(E, w, F);
+  if (rc) return rc;
+  k_residuals<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, w.xi, w.xa, w.ym, w.yi, w.dx, w.dy);
+  k_cost<<<(nret + 63) / 64, 64, 0, s>>>(nret, w.desc_d, w.active, w.dx, w.dy, w.sainv, w.w, w.chisq);
+  std::vector<double> chisq(nret);
+  std::vector<int> st(nret);
+  ECK(cudaMemcpyAsync(chisq.data(), w.chisq, sizeof(double) * nret, cudaMemcpyDeviceToHost, s));
+  ECK(cudaMemcpyAsync(st.data(), w.status, sizeof(int) * nret, cudaMemcpyDeviceToHost, s));
+  ECK(cudaStreamSynchronize(s));
+  std::vector<int> J(nret, 0);
+  for (int i = 0; i < nret; i++) {
+    if (!F[i]) continue;
+    Request* q = E->active[i];
+    q->chisq = chisq[i];
+    q->costs[0] = chisq[i];
+    q->state = 1;
+    if (st[i]) {
+      q->status = JGB_ERR_NUMERIC;
+      q->state = 2;
+    } else if (E->ret.conv_itmax == 0) {
+      q->state = 2;
+    }
+    J[i] = q->state == 1;
+  }
+  return jacobian(E, w, J);
+}
+
+// One LM iteration (retrieval.c:559-652) of every iterating request.
+int lm_iteration(jgb_engine* E, WorkSet& w) {
+  jgb_ctx* x = E->x;
+  cudaStream_t s = x->stream;
+  const int nret = w.nret;
+  const int kr = E->ret.kernel_recomp;
+  std::vector<int> A(nret, 0), J(nret, 0), N(nret, 0);
+  bool any = false;
+  for (int i = 0; i < nret; i++) {
+    Request* q = E->active[i];
+    if (q->state != 1) continue;
+    const int it = q->it + 1;
+    A[i] = 1;
+    any = true;
+    J[i] = it > 1 && it % kr == 0;
+    N[i] = it == 1 || it % kr == 0;
+    q->chisq_old = q->chisq;
+  }
+  if (!any) return JGB_OK;
+  int rc = jacobian(E, w, J);
+  if (rc) return rc;
+  // K^T W K into covn and K^T W dy into bvec; covn replaces cov where the
+  // kernel was (re)computed for this iteration
+  rc = normal_equations_dev(nret, w.mvec.data(), w.nvec.data(), w.Kd, w.w, w.dy, w.covn, w.bvec,
+                            E->precision, A.data(), w.nedesc, s);
+  if (rc) return ctx_error(x, rc, "normal-equation kernel failed");
+  rc = put_flags(E, w, N);
+  if (rc) return rc;
+  k_select_nn<<<dim3(16, nret), 256, 0, s>>>(nret, w.desc_d, w.active, w.covn, w.cov);
+  rc = put_flags(E, w, A);
+  if (rc) return rc;
+  k_gradient<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, w.sainv, w.dx, w.bvec);
+  std::vector<int> trying = A;
+  std::vector<double> lmpar(nret, 0), cnew(nret);
+  std::vector<int> st(nret), reject(nret);
+  for (int it2 = 0; it2 < 20; it2++) {
+    bool anyt = false;
+    for (int i = 0; i < nret; i++) anyt |= trying[i] != 0;
+    if (!anyt) break;
+    for (int i = 0; i < nret; i++) lmpar[i] = E->active[i]->lmpar;
+    rc = put_flags(E, w, trying);
+    if (rc) return rc;
+    ECK(cudaMemcpyAsync(w.lmpar, lmpar.data(), sizeof(double) * nret, cudaMemcpyHostToDevice, s));
+    k_lm_matrix<<<dim3(64, nret), 256, 0, s>>>(nret, w.desc_d, w.active, w.lmpar, w.sainv, w.cov, w.Amat);
+    k_chol_factor<<<nret, 256, 0, s>>>(nret, w.desc_d, w.active, w.Amat, w.status);
+    k_chol_solve<<<(nret + 63) / 64, 64, 0, s>>>(nret, w.desc_d, w.active, w.Amat, w.bvec, w.step);
+    k_axpy_state<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, +1.0, w.step, w.xi);
+    const CtlDev& c = x->c;
+    k_set_iterate<<<nret, 256, 0, s>>>(nret, w.desc_d, w.levoff, w.elems, w.active, apr_arrays(E, w),
+                                        cur_arrays(E, w), w.xi, c.nw, c.ncl, c.nsf);
+    ECK(cudaGetLastError());
+    rc = forward(E, w, trying);
+    if (rc) return rc;
+    k_residuals<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, w.xi, w.xa, w.ym, w.yi, w.dx, w.dy);
+    k_cost<<<(nret + 63) / 64, 64, 0, s>>>(nret, w.desc_d, w.active, w.dx, w.dy, w.sainv, w.w, w.chisq);
+    ECK(cudaMemcpyAsync(cnew.data(), w.chisq, sizeof(double) * nret, cudaMemcpyDeviceToHost, s));
+    ECK(cudaMemcpyAsync(st.data(), w.status, sizeof(int) * nret, cudaMemcpyDeviceToHost, s));
+    ECK(cudaStreamSynchronize(s));
+    E->st.lm_trials++;
+    for (int i = 0; i < nret; i++) {
+      reject[i] = 0;
+      if (!trying[i]) continue;
+      Request* q = E->active[i];
+      if (st[i]) {  // normal matrix not positive definite: the request fails
+        q->status = JGB_ERR_NUMERIC;
+        q->state = 2;
+        trying[i] = 0;
+        A[i] = 0;
+        continue;
+      }
+      q->chisq = cnew[i];
+      if (q->chisq > q->chisq_old) {
+        q->lmpar *= 10;
+        reject[i] = 1;
+      } else {
+        q->lmpar /= 10;
+      }
+    }
+    rc = put_flags(E, w, reject);
+    if (rc) return rc;
+    k_axpy_state<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, -1.0, w.step, w.xi);
+    for (int i = 0; i < nret; i++) trying[i] = reject[i];
+  }
+  rc = put_flags(E, w, A);
+  if (rc) return rc;
+  k_dot_state<<<(nret + 63) / 64, 64, 0, s>>>(nret, w.desc_d, w.active, w.step, w.bvec, w.disq);
+  std::vector<double> disq(nret);
+  ECK(cudaMemcpyAsync(disq.data(), w.disq, sizeof(double) * nret, cudaMemcpyDeviceToHost, s));
+  ECK(cudaStreamSynchronize(s));
+  for (int i = 0; i < nret; i++) {
+    if (!A[i]) continue;
+    Request* q = E->active[i];
+    q->it++;
+    q->costs[q->it] = q->chisq;
+    const double dq = disq[i] / (double)q->n;
+    if ((q->it == 1 || q->it % kr == 0) && dq < E->ret.conv_dmin) q->state = 2;
+    if (q->it >= E->ret.conv_itmax) q->state = 2;
+  }
+  return JGB_OK;
+}
+
+// Results of the finished requests: final state, forward model, error
+// analysis (retrieval.c:658-726), moved to the host in one staged copy.
+int finish_requests(jgb_engine* E, WorkSet& w) {
+  jgb_ctx* x = E->x;
+  const CtlDev& c = x->c;
+  cudaStream_t s = x->stream;
+  const int nret = w.nret;
+  std::vector<int> Fin(nret, 0), ok(nret, 0);
+  bool any = false, any_ok = false;
+  for (int i = 0; i < nret; i++) {
+    const Request* q = E->active[i];
+    if (q->state != 2) continue;
+    Fin[i] = 1;
+    any = true;
+    ok[i] = q->status == JGB_OK;
+    any_ok |= ok[i] != 0;
+  }
+  if (!any) return JGB_OK;
+  const bool err_ana = E->ret.err_ana != 0;
+  int rc = put_flags(E, w, Fin);
+  if (rc) return rc;
+  k_gather_state<<<nret, 128, 0, s>>>(nret, w.desc_d, w.levoff, w.elems, w.active, cur_arrays(E, w), w.xfin);
+  std::vector<int> st(nret, 0);
+  if (err_ana && any_ok) {
+    rc = normal_equations_dev(nret, w.mvec.data(), w.nvec.data(), w.Kd, w.w, w.dy, w.covn, w.bvec,
+                              E->precision, ok.data(), w.nedesc, s);
+    if (rc) return ctx_error(x, rc, "normal-equation kernel failed");
+    rc = put_flags(E, w, ok);
+    if (rc) return rc;
+    ECK(cudaMemsetAsync(w.status, 0, sizeof(int) * nret, s));
+    k_add_nn<<<dim3(16, nret), 256, 0, s>>>(nret, w.desc_d, w.active, w.sainv, w.covn);
+    k_chol_factor<<<nret, 256, 0, s>>>(nret, w.desc_d, w.active, w.covn, w.status);
+    k_chol_inverse<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, w.covn, w.work, w.Amat);
+    k_gain<<<dim3(64, nret), 256, 0, s>>>(nret, w.desc_d, w.active, w.Amat, w.Kd, w.w, w.G);
+    k_sqrt_diag<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, w.Amat, w.e_tot);
+    k_err_diag<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, w.G, w.sn, w.e_noise);
+    k_err_diag<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, w.G, w.sf, w.e_formod);
+    k_avk<<<dim3(64, nret), 256, 0, s>>>(nret, w.desc_d, w.active, w.G, w.Kd, w.work);
+    k_avk_analyze<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, w.work, w.sael,
+                                        7 + c.ng + c.nw + c.ncl, w.cont, w.res);
+    ECK(cudaGetLastError());
+    ECK(cudaMemcpyAsync(st.data(), w.status, sizeof(int) * nret, cudaMemcpyDeviceToHost, s));
+  }
+  // stage every result of every finished request into one device buffer
+  std::vector<unsigned long long> seg;
+  size_t words = 0;
+  struct Dst {
+    std::vector<double>* v;
+    size_t off, len;
+  };
+  std::vector<Dst> dst;
+  auto add = [&](const double* src, long long len, std::vector<double>* v, size_t voff) {
+    if (len <= 0) return;
+    seg.push_back((unsigned long long)src);
+    seg.push_back(words);  // relocated to the staging address below
+    seg.push_back((unsigned long long)len);
+    dst.push_back(Dst{v, voff, (size_t)len});
+    words += (size_t)len;
+  };
+  for (int i = 0; i < nret; i++) {
+    if (!Fin[i]) continue;
+    Request* q = E->active[i];
+    const RetDesc& d = w.desc[i];
+    const long long n = q->n, nr = q->nr, r0 = w.H.ray_off[i];
+    q->x.assign(n, 0);
+    q->rad_out.assign((size_t)c.nd * nr, 0);
+    q->tau_out.assign((size_t)c.nd * nr, 0);
+    q->tp_out.assign(3 * (size_t)nr, 0);
+    q->p_out.assign(q->np, 0);
+    add(w.xfin + d.xo, n, &q->x, 0);
+    for (int k = 0; k < c.nd; k++) {
+      add(w.rad + k * w.nray + r0, nr, &q->rad_out, (size_t)k * nr);
+      add(w.tau + k * w.nray + r0, nr, &q->tau_out, (size_t)k * nr);
+    }
+    for (int k = 0; k < 3; k++) add(w.tp + k * w.nray + r0, nr, &q->tp_out, (size_t)k * nr);
+    add(w.cur_lev + 4 * w.nlev + w.H.lev_off[i], q->np, &q->p_out, 0);
+    if (err_ana && ok[i] && !st[i]) {
+      q->cov.assign(n * n, 0);
+      q->avk.assign(n * n, 0);
+      q->err_total.assign(n, 0);
+      q->err_noise.assign(n, 0);
+      q->err_formod.assign(n, 0);
+      q->cont.assign(n, 0);
+      q->res.assign(n, 0);
+      add(w.Amat + d.so, n * n, &q->cov, 0);
+      add(w.work + d.so, n * n, &q->avk, 0);
+      add(w.e_tot + d.xo, n, &q->err_total, 0);
+      add(w.e_noise + d.xo, n, &q->err_noise, 0);
+      add(w.e_formod + d.xo, n, &q->err_formod, 0);
+      add(w.cont + d.xo, n, &q->cont, 0);
+      add(w.res + d.xo, n, &q->res, 0);
+      if (E->keep_gain) {
+        q->gain.assign(n * q->m, 0);
+        add(w.G + d.ko, n * q->m, &q->gain, 0);
+      }
+    } else if (err_ana && ok[i] && st[i]) {
+      q->status = JGB_ERR_NUMERIC;
+    }
+  }
+  ECK(E->stage.reserve(sizeof(double) * std::max(words, (size_t)1)));
+  double* sd = E->stage.as<double>();
+  for (size_t k = 0; k < seg.size(); k += 3) seg[k + 1] = (unsigned long long)(sd + seg[k + 1]);
+  rc = run_segments(E, seg);
+  if (rc) return rc;
+  rc = ensure_pinned(E, words);
+  if (rc) return rc;
+  ECK(cudaMemcpyAsync(E->pinned, sd, sizeof(double) * words, cudaMemcpyDeviceToHost, s));
+  ECK(cudaStreamSynchronize(s));
+  size_t o = 0;
+  for (const Dst& d : dst) {
+    std::memcpy(d.v->data() + d.off, E->pinned + o, sizeof(double) * d.len);
+    o += d.len;
+  }
+  // retire
+  std::vector<Request*> keep;
+  for (int i = 0; i < nret; i++) {
+    Request* q = E->active[i];
+    if (Fin[i]) {
+      E->used -= q->bytes;
+      E->done[q->id] = q;
+      E->st.finished++;
+      if (q->status) E->st.failed++;
+    } else {
+      keep.push_back(q);
+    }
+  }
+  E->active.swap(keep);
+  E->dirty = true;
+  return JGB_OK;
+}
+
+int engine_step(jgb_engine* E) {
+  jgb_ctx* x = E->x;
+  cudaSetDevice(x->device);
+  const double t0 = now_ms();
+  // admission by slots and working-set bytes
+  while (!E->queue.empty() && (int)E->active.size() < E->max_active) {
+    Request* q = E->queue.front();
+    if (!E->active.empty() && E->used + q->bytes > E->budget) break;
+    E->queue.pop_front();
+    q->slot = -1;
+    E->active.push_back(q);
+    E->used += q->bytes;
+    E->dirty = true;
+  }
+  if (E->active.empty()) return JGB_OK;
+  if (E->dirty) {
+    WorkSet& nw = E->ws[1 - E->cur];
+    int rc = build_workset(E, nw, E->have_ws ? &E->ws[E->cur] : nullptr);
+    if (rc) return rc;
+    E->cur = 1 - E->cur;
+    E->have_ws = true;
+    E->dirty = false;
+    E->st.rebuilds++;
+  }
+  WorkSet& w = E->ws[E->cur];
+  std::vector<int> F(w.nret, 0);
+  bool anyf = false;
+  for (int i = 0; i < w.nret; i++) {
+    F[i] = E->active[i]->state == 0;
+    anyf |= F[i] != 0;
+  }
+  int rc = JGB_OK;
+  if (anyf) rc = init_requests(E, w, F);
+  if (!rc) rc = lm_iteration(E, w);
+  if (!rc) rc = finish_requests(E, w);
+  E->st.steps++;
+  E->st.step_ms += now_ms() - t0;
+  return rc;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI of the engine
+
+extern "C" int jgb_engine_create(jgb_ctx* x, const jgb_ret* ret, int precision,
+                                 unsigned long long mem_budget, int max_active, int keep_gain,
+                                 jgb_engine** out) {
+  if (!x || !ret || !out) return ctx_error(x, JGB_ERR_ARG, "bad arguments");
+  *out = nullptr;
+  if (ret->conv_itmax < 0 || ret->kernel_recomp <= 0) return ctx_error(x, JGB_ERR_ARG, "bad retrieval settings");
+  if (precision != JGB_FP64 && precision != JGB_MIXED) return ctx_error(x, JGB_ERR_ARG, "bad precision");
+  CtxView v;
+  int rc = ctx_view(x, &v);
+  if (rc) return rc;
+  const CtlDev& c = x->c;
+  jgb_engine* E = new jgb_engine();
+  E->x = x;
+  E->precision = precision;
+  E->budget = mem_budget ? mem_budget : ~0ULL;
+  E->max_active = max_active > 0 ? std::min(max_active, 65535) : 65535;
+  E->keep_gain = keep_gain;
+  E->ret = *ret;
+  auto cp = [](std::vector<double>& v, const double* p, int n) -> const double* {
+    if (!p || n <= 0) return nullptr;
+    v.assign(p, p + n);
+    return v.data();
+  };
+  E->ret.err_formod = cp(E->v_formod, ret->err_formod, c.nd);
+  E->ret.err_noise = cp(E->v_noise, ret->err_noise, c.nd);
+  E->ret.err_q = cp(E->v_q, ret->err_q, c.ng);
+  E->ret.err_q_cz = cp(E->v_qcz, ret->err_q_cz, c.ng);
+  E->ret.err_q_ch = cp(E->v_qch, ret->err_q_ch, c.ng);
+  E->ret.err_k = cp(E->v_k, ret->err_k, c.nw);
+  E->ret.err_k_cz = cp(E->v_kcz, ret->err_k_cz, c.nw);
+  E->ret.err_k_ch = cp(E->v_kch, ret->err_k_ch, c.nw);
+  E->ret.err_clk = cp(E->v_clk, ret->err_clk, c.ncl);
+  E->ret.err_sfeps = cp(E->v_sfeps, ret->err_sfeps, c.nsf);
+  *out = E;
+  return JGB_OK;
+}
+
+extern "C" void jgb_engine_destroy(jgb_engine* E) {
+  if (!E) return;
+  cudaSetDevice(E->x->device);
+  cudaStreamSynchronize(E->x->stream);
+  delete E;
+}
+
+extern "C" int jgb_engine_submit(jgb_engine* E, const jgb_batch* hb, unsigned long long* ids) {
+  if (!E || !hb || hb->nobs <= 0) return ctx_error(E ? E->x : nullptr, JGB_ERR_ARG, "bad arguments");
+  jgb_ctx* x = E->x;
+  const CtlDev& c = x->c;
+  const int nobs = hb->nobs;
+  const int nlev = hb->lev_off[nobs], nray = hb->ray_off[nobs];
+  const int nscal = 5 + c.ncl + c.nsf;
+  std::vector<Request*> made;
+  for (int i = 0; i < nobs; i++) {
+    Request* q = new Request();
+    const int l0 = hb->lev_off[i], r0 = hb->ray_off[i];
+    q->np = hb->lev_off[i + 1] - l0;
+    q->nr = hb->ray_off[i + 1] - r0;
+    int rc = JGB_OK;
+    if (q->np < 1 || q->nr < 1) rc = ctx_error(x, JGB_ERR_ARG, "empty observation");
+    if (!rc) {
+      const int nplanes = 6 + c.ng + c.nw;
+      q->lev.resize((size_t)nplanes * q->np);
+      const double* src[6] = {hb->time, hb->z, hb->lon, hb->lat, hb->p, hb->t};
+      for (int k = 0; k < 6; k++) std::memcpy(&q->lev[(size_t)k * q->np], src[k] + l0, sizeof(double) * q->np);
+      for (int g = 0; g < c.ng; g++)
+        std::memcpy(&q->lev[(size_t)(6 + g) * q->np], hb->q + (size_t)g * nlev + l0, sizeof(double) * q->np);
+      for (int k = 0; k < c.nw; k++)
+        std::memcpy(&q->lev[(size_t)(6 + c.ng + k) * q->np], hb->k + (size_t)k * nlev + l0, sizeof(double) * q->np);
+      q->scal.assign(hb->scal + (size_t)i * nscal, hb->scal + (size_t)(i + 1) * nscal);
+      q->geo.resize(7 * (size_t)q->nr);
+      for (int k = 0; k < 7; k++)
+        std::memcpy(&q->geo[(size_t)k * q->nr], hb->geo + (size_t)k * nray + r0, sizeof(double) * q->nr);
+      q->rad.resize((size_t)c.nd * q->nr);
+      for (int k = 0; k < c.nd; k++)
+        std::memcpy(&q->rad[(size_t)k * q->nr], hb->rad + (size_t)k * nray + r0, sizeof(double) * q->nr);
+      rc = prepare_request(E, q);
+    }
+    if (rc) {
+      delete q;
+      for (Request* r : made) delete r;
+      return rc;
+    }
+    made.push_back(q);
+  }
+  for (size_t i = 0; i < made.size(); i++) {
+    made[i]->id = E->next_id++;
+    if (ids) ids[i] = made[i]->id;
+    E->queue.push_back(made[i]);
+  }
+  E->st.submitted += made.size();
+  return JGB_OK;
+}
+
+extern "C" int jgb_engine_step(jgb_engine* E, int* n_active, int* n_queued, int* n_done) {
+  if (!E) return JGB_ERR_ARG;
+  const int rc = engine_step(E);
+  if (n_active) *n_active = (int)E->active.size();
+  if (n_queued) *n_queued = (int)E->queue.size();
+  if (n_done) *n_done = (int)E->done.size();
+  return rc;
+}
+
+extern "C" int jgb_engine_finished(jgb_engine* E, unsigned long long* ids, int max, int* count) {
+  if (!E || !count) return JGB_ERR_ARG;
+  int k = 0;
+  for (auto it = E->done.begin(); it != E->done.end() && k < max; ++it) ids[k++] = it->first;
+  *count = k;
+  return JGB_OK;
+}
+
+extern "C" int jgb_engine_sizes(jgb_engine* E, unsigned long long id, int* n, int* m, int* np, int* nr) {
+  if (!E) return JGB_ERR_ARG;
+  auto it = E->done.find(id);
+  if (it == E->done.end()) return ctx_error(E->x, JGB_ERR_ARG, "unknown or unfinished request");
+  const Request* q = it->second;
+  if (n) *n = q->n;
+  if (m) *m = q->m;
+  if (np) *np = q->np;
+  if (nr) *nr = q->nr;
+  return JGB_OK;
+}
+
+extern "C" int jgb_engine_result(jgb_engine* E, unsigned long long id, jgb_ret_out* o) {
+  if (!E || !o) return JGB_ERR_ARG;
+  auto it = E->done.find(id);
+  if (it == E->done.end()) return ctx_error(E->x, JGB_ERR_ARG, "unknown or unfinished request");
+  Request* q = it->second;
+  auto put = [](double* dst, const std::vector<double>& v) {
+    if (dst && !v.empty()) std::memcpy(dst, v.data(), sizeof(double) * v.size());
+  };
+  put(o->x, q->x);
+  put(o->cov, q->cov);
+  put(o->costs, q->costs);
+  put(o->rad, q->rad_out);
+  put(o->tau, q->tau_out);
+  put(o->tp, q->tp_out);
+  put(o->p, q->p_out);
+  put(o->gain, q->gain);
+  put(o->avk, q->avk);
+  put(o->err_total, q->err_total);
+  put(o->err_noise, q->err_noise);
+  put(o->err_formod, q->err_formod);
+  put(o->cont, q->cont);
+  put(o->res, q->res);
+  o->iters = q->it;
+  o->status = q->status;
+  o->has_err_ana = q->cov.empty() ? 0 : 1;
+  E->done.erase(it);
+  delete q;
+  return JGB_OK;
+}
+
+extern "C" int jgb_engine_get_stats(const jgb_engine* E, jgb_engine_stats* out) {
+  if (!E || !out) return JGB_ERR_ARG;
+  *out = E->st;
+  out->active = (int)E->active.size();
+  out->queued = (int)E->queue.size();
+  out->done = (int)E->done.size();
+  out->used_bytes = E->used;
+  return JGB_OK;
+}
+
+// Lockstep-free batch retrieval on top of the engine: every observation is a
+// request, all are admitted at once and stepped until done.
+extern "C" int jgb_retrieve_batch(jgb_ctx* x, const jgb_ret* ret, const jgb_batch* hb,
+                                  double* x_out, double* cov_out, double* costs, int* iters,
+                                  int precision) {
+  if (!x || !ret || !hb || !x_out || hb->nobs <= 0) return ctx_error(x, JGB_ERR_ARG, "bad arguments");
+  if (hb->nobs > 65535) return ctx_error(x, JGB_ERR_ARG, "at most 65535 retrievals per batch");
+  const CtlDev& c = x->c;
+  jgb_engine* E = nullptr;
+  int rc = jgb_engine_create(x, ret, precision, 0, hb->nobs, 0, &E);
+  if (rc) return rc;
+  const int nret = hb->nobs;
+  std::vector<unsigned long long> ids(nret);
+  rc = jgb_engine_submit(E, hb, ids.data());
+  while (!rc && (int)E->done.size() < nret) rc = engine_step(E);
+  if (rc) {
+    jgb_engine_destroy(E);
+    return rc;
+  }
+  const int nray = hb->ray_off[nret];
+  const int ncost = ret->conv_itmax + 1;
+  int first_err = JGB_OK;
+  long long xo = 0, so = 0;
+  for (int i = 0; i < nret; i++) {
+    Request* q = E->done[ids[i]];
+    std::memcpy(x_out + xo, q->x.data(), sizeof(double) * q->n);
+    if (cov_out && !q->cov.empty()) std::memcpy(cov_out + so, q->cov.data(), sizeof(double) * q->cov.size());
+    if (costs) std::memcpy(costs + (size_t)i * ncost, q->costs.data(), sizeof(double) * ncost);
+    if (iters) iters[i] = q->it;
+    const int r0 = hb->ray_off[i];
+    for (int k = 0; k < c.nd; k++) {
+      std::memcpy(hb->rad + (size_t)k * nray + r0, &q->rad_out[(size_t)k * q->nr], sizeof(double) * q->nr);
+      std::memcpy(hb->tau + (size_t)k * nray + r0, &q->tau_out[(size_t)k * q->nr], sizeof(double) * q->nr);
+    }
+    for (int k = 0; k < 3; k++)
+      std::memcpy(hb->tp + (size_t)k * nray + r0, &q->tp_out[(size_t)k * q->nr], sizeof(double) * q->nr);
+    std::memcpy(hb->p + hb->lev_off[i], q->p_out.data(), sizeof(double) * q->np);
+    if (q->status && !first_err) first_err = q->status;
+    xo += q->n;
+    so += (long long)q->n * q->n;
+  }
+  jgb_engine_destroy(E);
+  if (first_err == JGB_ERR_NUMERIC) return ctx_error(x, first_err, "normal matrix is not positive definite");
+  return first_err;
 }

@@ -80,6 +80,23 @@ class Stats(C.Structure):
         return d
 
 
+class EngineStats(C.Structure):
+    _fields_ = [("submitted", C.c_ulonglong), ("finished", C.c_ulonglong),
+                ("failed", C.c_ulonglong), ("steps", C.c_ulonglong), ("rebuilds", C.c_ulonglong),
+                ("forward_calls", C.c_ulonglong), ("lm_trials", C.c_ulonglong),
+                ("jacobians", C.c_ulonglong), ("step_ms", C.c_double), ("active", C.c_int),
+                ("queued", C.c_int), ("done", C.c_int), ("used_bytes", C.c_ulonglong)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class _RetOut(C.Structure):
+    _fields_ = [(k, _dp) for k in ("x", "cov", "costs", "rad", "tau", "tp", "p", "gain", "avk",
+                                   "err_total", "err_noise", "err_formod", "cont", "res")] + \
+               [("iters", C.c_int), ("status", C.c_int), ("has_err_ana", C.c_int)]
+
+
 # exported symbols and their signatures (the contract of include/jurassic_gb300.h)
 SIGNATURES = {
     "jgb_create": (C.c_int, [C.POINTER(_Ctl), C.c_int, C.POINTER(C.c_void_p)]),
@@ -102,6 +119,15 @@ SIGNATURES = {
     "jgb_retrieve_batch": (C.c_int, [C.c_void_p, C.POINTER(_Ret), C.POINTER(_Batch), _dp, _dp,
                                      _dp, _ip, C.c_int]),
     "jgb_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    "jgb_engine_create": (C.c_int, [C.c_void_p, C.POINTER(_Ret), C.c_int, C.c_ulonglong, C.c_int,
+                                    C.c_int, C.POINTER(C.c_void_p)]),
+    "jgb_engine_destroy": (None, [C.c_void_p]),
+    "jgb_engine_submit": (C.c_int, [C.c_void_p, C.POINTER(_Batch), C.POINTER(C.c_ulonglong)]),
+    "jgb_engine_step": (C.c_int, [C.c_void_p, _ip, _ip, _ip]),
+    "jgb_engine_finished": (C.c_int, [C.c_void_p, C.POINTER(C.c_ulonglong), C.c_int, _ip]),
+    "jgb_engine_sizes": (C.c_int, [C.c_void_p, C.c_ulonglong, _ip, _ip, _ip, _ip]),
+    "jgb_engine_result": (C.c_int, [C.c_void_p, C.c_ulonglong, C.POINTER(_RetOut)]),
+    "jgb_engine_get_stats": (C.c_int, [C.c_void_p, C.POINTER(EngineStats)]),
     "jgb_formod_batch_dev_noalloc": (C.c_int, [C.c_void_p, C.POINTER(_Batch)]),
     "jgb_host_alloc": (C.c_void_p, [C.c_ulonglong]),
     "jgb_host_free": (None, [C.c_void_p]),
@@ -331,6 +357,24 @@ class Context:
             ob += ni
         return outA, outb
 
+    def _ret_struct(self, ret):
+        r = ret.sized(self.ctl)
+        keep = {k: _d(getattr(r, k)) for k in ("err_formod", "err_noise", "err_q", "err_q_cz",
+                                                "err_q_ch", "err_k", "err_k_cz", "err_k_ch",
+                                                "err_clk", "err_sfeps")}
+        sr = _Ret(kernel_recomp=r.kernel_recomp, conv_itmax=r.conv_itmax, err_ana=r.err_ana,
+                  conv_dmin=r.conv_dmin, err_press=r.err_press, err_press_cz=r.err_press_cz,
+                  err_press_ch=r.err_press_ch, err_temp=r.err_temp, err_temp_cz=r.err_temp_cz,
+                  err_temp_ch=r.err_temp_ch, err_clz=r.err_clz, err_cldz=r.err_cldz,
+                  err_sfz=r.err_sfz, err_sfp=r.err_sfp, err_sft=r.err_sft,
+                  **{k: _p(v) for k, v in keep.items()})
+        return r, sr, keep
+
+    def engine(self, ret, precision: int = FP64, mem_budget: int = 0, max_active: int = 0,
+               keep_gain: bool = False) -> "Engine":
+        """Continuous-batching retrieval engine on this context."""
+        return Engine(self, ret, precision, mem_budget, max_active, keep_gain)
+
     def retrieve_batch(self, ret, batch, precision: int = FP64):
         """Optimal-estimation retrievals (optimal_estimation,
         src/retrieval.c:448-749) of every observation of a batch: the batch
@@ -371,3 +415,93 @@ class Context:
         cs = costs.reshape(b.nobs, ncost)
         return dict(x=xs, cov=covs, costs=[c[np.isfinite(c)] for c in cs],
                     iters=iters.tolist(), batch=b)
+
+
+class Engine:
+    """Continuous-batching retrieval engine (jgb_engine_*): submit
+    observations as requests, step, collect results per request id.
+
+    Results are dicts with x, costs (finite entries), iters, status, rad,
+    tau, tp, p and, with error analysis, cov, avk, gain (if kept),
+    err_total, err_noise, err_formod, cont, res."""
+
+    def __init__(self, ctx: Context, ret, precision: int = FP64, mem_budget: int = 0,
+                 max_active: int = 0, keep_gain: bool = False):
+        self.ctx = ctx
+        self.keep_gain = bool(keep_gain)
+        self.r, sr, self._keep = ctx._ret_struct(ret)
+        h = C.c_void_p()
+        ctx._check(load().jgb_engine_create(ctx.h, C.byref(sr), precision, int(mem_budget),
+                                            int(max_active), int(keep_gain), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().jgb_engine_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, batch) -> list:
+        s, arr, keep = self.ctx._batch_struct(batch)
+        ids = (C.c_ulonglong * batch.nobs)()
+        self.ctx._check(load().jgb_engine_submit(self.h, C.byref(s), ids))
+        return list(ids)
+
+    def step(self):
+        a, q, d = C.c_int(), C.c_int(), C.c_int()
+        self.ctx._check(load().jgb_engine_step(self.h, C.byref(a), C.byref(q), C.byref(d)))
+        return a.value, q.value, d.value
+
+    def finished(self, max_ids: int = 65536) -> list:
+        ids = (C.c_ulonglong * max_ids)()
+        n = C.c_int()
+        self.ctx._check(load().jgb_engine_finished(self.h, ids, max_ids, C.byref(n)))
+        return list(ids[:n.value])
+
+    def stats(self) -> dict:
+        st = EngineStats()
+        load().jgb_engine_get_stats(self.h, C.byref(st))
+        return st.as_dict()
+
+    def result(self, rid: int) -> dict:
+        n, m, npl, nr = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        L = load()
+        self.ctx._check(L.jgb_engine_sizes(self.h, rid, C.byref(n), C.byref(m), C.byref(npl),
+                                           C.byref(nr)))
+        n, m, npl, nr = n.value, m.value, npl.value, nr.value
+        nd = self.ctx.ctl.nd
+        ana = bool(self.r.err_ana)
+        out = dict(x=np.zeros(n), costs=np.zeros(self.r.conv_itmax + 1), rad=np.zeros((nd, nr)),
+                   tau=np.zeros((nd, nr)), tp=np.zeros((3, nr)), p=np.zeros(npl))
+        if ana:
+            out.update(cov=np.zeros((n, n)), avk=np.zeros((n, n)), gain=np.zeros((n, m)),
+                       err_total=np.zeros(n), err_noise=np.zeros(n), err_formod=np.zeros(n),
+                       cont=np.zeros(n), res=np.zeros(n))
+        ro = _RetOut(**{k: _p(v) for k, v in out.items()})
+        self.ctx._check(L.jgb_engine_result(self.h, rid, C.byref(ro)))
+        out["costs"] = out["costs"][np.isfinite(out["costs"])]
+        out["iters"] = ro.iters
+        out["status"] = ro.status
+        if ana and not ro.has_err_ana:
+            for k in ("cov", "avk", "gain", "err_total", "err_noise", "err_formod", "cont", "res"):
+                out[k] = None
+        if ana and not self.keep_gain:
+            out["gain"] = None
+        return out
+
+    def run(self, batch) -> list:
+        """Submit a batch, step until all of it is done, results in order."""
+        ids = self.submit(batch)
+        want = set(ids)
+        res = {}
+        while want - set(res):
+            self.step()
+            for rid in self.finished():
+                if rid in want:
+                    res[rid] = self.result(rid)
+        return [res[i] for i in ids]

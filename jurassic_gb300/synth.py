@@ -330,3 +330,43 @@ def config_limb_cga(nobs, seed=3, nd=32, emitters=("CO2", "H2O", "O3"), raydz=0.
         items.append((atm, obs))
     return Workload("limb_cga_%dobs_%dch_%dgas" % (nobs, nd, ctl.ng), ctl,
                     make_tables(ctl, seed + 100), make_filters(ctl), pack(ctl, items))
+
+
+def retrieval_requests(ctl: Ctl, forward, n, seed, nlev=(21, 31), ztop=60.0,
+                       kinds=("nadir", "limb"), nch=None, limb_rays=3, noise=2e-3,
+                       dt=3.0, dq=0.2):
+    """Retrieval requests of uneven size: (a-priori Atm, measured Obs) pairs.
+
+    Request i has a level count uniform on ``nlev`` (0-ztop km), is nadir (one
+    ray) or limb (``limb_rays`` tangent heights on 8-30 km) in turn from
+    ``kinds``, and measures the first ``nch[i]`` channels (others NaN, all if
+    ``nch`` is None).  The truth is the standard atmosphere with a seeded
+    temperature offset (+-dt K) and gas factors (+-dq); the measurement is
+    ``forward(truth batch)`` with multiplicative noise; the a priori is the
+    unperturbed standard atmosphere."""
+    rng = np.random.default_rng(seed)
+    truths, obss, aprs = [], [], []
+    for i in range(n):
+        nl = int(rng.integers(nlev[0], nlev[1] + 1))
+        z = np.linspace(0.0, ztop, nl)
+        lat = float(rng.uniform(-60, 60))
+        lon = float(rng.uniform(-180, 180))
+        truths.append(profile(ctl.emitter, z, dt=float(rng.uniform(-dt, dt)),
+                              dq=1 + rng.uniform(-dq, dq, ctl.ng), nw=ctl.nw, time=float(i),
+                              lon=lon, lat=lat))
+        aprs.append(profile(ctl.emitter, z, nw=ctl.nw, time=float(i), lon=lon, lat=lat))
+        if kinds[i % len(kinds)] == "nadir":
+            obs = nadir_obs(ctl.nd, [lat], time=float(i), lon=lon)
+        else:
+            obs = limb_obs(ctl.nd, np.sort(rng.uniform(8.0, 30.0, limb_rays)), time=float(i),
+                           lon=lon, lat=lat)
+        obss.append(obs)
+    fw = forward(pack(ctl, list(zip(truths, obss))))
+    items = []
+    for i in range(n):
+        _, o = fw.item(ctl, i)
+        o.rad = o.rad * (1 + noise * rng.standard_normal(o.rad.shape))
+        if nch is not None:
+            o.rad[int(nch[i]):, :] = np.nan
+        items.append((aprs[i], o))
+    return items
