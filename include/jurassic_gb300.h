@@ -206,6 +206,10 @@ typedef struct {
   unsigned long long submitted, finished, failed, steps, rebuilds, forward_calls, lm_trials,
       jacobians;
   double step_ms;              /* host wall time spent in jgb_engine_step */
+  /* of which (stream synchronised at each phase end): working-set rebuilds,
+     initialisation forward models + S_a, Jacobians, normal equations +
+     gradient, damped trials (Cholesky + forward model + cost), results */
+  double rebuild_ms, init_ms, jacobian_ms, normal_ms, trial_ms, finish_ms;
   int active, queued, done;    /* requests in flight, waiting, finished and not yet collected */
   unsigned long long used_bytes;  /* working-set bytes of the active requests */
 } jgb_engine_stats;

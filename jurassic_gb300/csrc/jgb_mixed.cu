@@ -124,48 +124,74 @@ __device__ __forceinline__ int bisect_f(const float* g, int lo, int hi, float x)
   return lo;
 }
 
-// Bracket of x on an ascending row of n entries with g[0] <= x <= g[n-1],
-// starting from hint h (locate_tbl semantics, jurassic.c:4152-4170).
-__device__ __forceinline__ int hunt_f(const float* g, int n, float x, int h) {
+// Bracket i of x on an ascending row of n entries with g[0] <= x <= g[n-1],
+// starting from hint h (locate_tbl semantics, jurassic.c:4152-4170), with
+// the grid values g[i], g[i+1] (reused from the probe loads on a hit).
+struct Bracket {
+  int i;
+  float a, b;
+};
+
+__device__ __forceinline__ Bracket hunt_f(const float* g, int n, float x, int h) {
   h = h < 0 ? 0 : (h > n - 2 ? n - 2 : h);
   const float a = __ldg(g + h), b = __ldg(g + h + 1);
   const float c = (h + 2 <= n - 1) ? __ldg(g + h + 2) : b;
+  int i;
   if (a <= x) {
-    if (x < b) return h;
-    if (h + 1 >= n - 1) return n - 2;
-    if (x < c) return h + 1;
-    if (h + 2 >= n - 1) return n - 2;
-    return bisect_f(g, h + 2, n - 1, x);
+    if (x < b || h + 1 >= n - 1) return Bracket{h, a, b};          // h == n-2 on the right end
+    if (x < c || h + 2 >= n - 1) return Bracket{h + 1, b, c};      // h + 1 == n-2 on the right end
+    i = bisect_f(g, h + 2, n - 1, x);
+  } else {
+    i = bisect_f(g, 0, h, x);
   }
-  return bisect_f(g, 0, h, x);
+  return Bracket{i, __ldg(g + i), __ldg(g + i + 1)};
 }
 
-// Emissivity at column u (intpol_tbl_eps) in float; *hint holds the bracket.
-__device__ __forceinline__ float rowf_eps(const RowF& r, float u, int* hint) {
-  if (u < r.u0) return r.e0 / r.u0 * u;
-  if (u > r.un) {
-    const float a = log1pf(-r.en) / r.un;
-    return -expm1f(a * u);
+// Emissivity of one table row (corner of the p-T cell) for the extended
+// path: EGA u = intpol_tbl_u(e_path) + du, CGA u = ucg; then
+// intpol_tbl_eps(u) (jurassic.c:3799-3891, 3895-3967).  In EGA the bracket
+// that inverts e_path also brackets u_eq in the column row (the rows are
+// monotone), and u_eq + du usually stays inside it: then the emissivity is
+// interpolated from the four entries already loaded, with no second search.
+// The bracket is the same either way, so the value is too.
+__device__ __forceinline__ float corner_eps(const RowF& r, bool cga, float e_path, float du,
+                                            float ucg, unsigned short& hu, unsigned short& he) {
+  float uq;
+  int ib = -1;
+  float u_lo = 0.f, u_hi = 0.f, e_lo = 0.f, e_hi = 0.f;
+  if (cga) {
+    uq = ucg;
+  } else {
+    if (e_path < r.e0) {
+      uq = r.u0 / r.e0 * e_path;
+    } else if (e_path > r.en) {
+      const float a = log1pf(-r.en) / r.un;
+      uq = log1pf(-e_path) / a;
+    } else {
+      const Bracket k = hunt_f(r.e, r.n, e_path, he);
+      he = (unsigned short)k.i;
+      ib = k.i;
+      e_lo = k.a;
+      e_hi = k.b;
+      u_lo = __ldg(r.u + k.i);
+      u_hi = __ldg(r.u + k.i + 1);
+      uq = u_lo + (u_hi - u_lo) / (e_hi - e_lo) * (e_path - e_lo);
+    }
+    uq = uq + du;
   }
-  const int i = hunt_f(r.u, r.n, u, *hint);
-  *hint = i;
-  const float xa = __ldg(r.u + i), xb = __ldg(r.u + i + 1);
-  const float ya = __ldg(r.e + i), yb = __ldg(r.e + i + 1);
-  return ya + (yb - ya) / (xb - xa) * (u - xa);
-}
-
-// Column at emissivity e (intpol_tbl_u) in float; *hint holds the bracket.
-__device__ __forceinline__ float rowf_u(const RowF& r, float e, int* hint) {
-  if (e < r.e0) return r.u0 / r.e0 * e;
-  if (e > r.en) {
+  if (uq < r.u0) return r.e0 / r.u0 * uq;
+  if (uq > r.un) {
     const float a = log1pf(-r.en) / r.un;
-    return log1pf(-e) / a;
+    return -expm1f(a * uq);
   }
-  const int i = hunt_f(r.e, r.n, e, *hint);
-  *hint = i;
-  const float xa = __ldg(r.e + i), xb = __ldg(r.e + i + 1);
-  const float ya = __ldg(r.u + i), yb = __ldg(r.u + i + 1);
-  return ya + (yb - ya) / (xb - xa) * (e - xa);
+  if (ib >= 0 && uq >= u_lo && uq < u_hi) {
+    hu = (unsigned short)ib;
+    return e_lo + (e_hi - e_lo) / (u_hi - u_lo) * (uq - u_lo);
+  }
+  const Bracket k = hunt_f(r.u, r.n, uq, ib >= 0 ? ib : (int)hu);
+  hu = (unsigned short)k.i;
+  const float ya = __ldg(r.e + k.i), yb = __ldg(r.e + k.i + 1);
+  return ya + (yb - ya) / (k.b - k.a) * (uq - k.a);
 }
 
 __device__ __forceinline__ int bracket_regf(const float* g, int n, float x) {
@@ -187,16 +213,18 @@ __device__ __forceinline__ int bracket_irrf(const float* g, int n, float x) {
 }
 
 // Pressure bracket with a hint: keeps ipr while p lies inside its interval
-// (or beyond the grid end it is clamped to), else bisects.
-__device__ __forceinline__ int pbracket_f(const float* g, int n, float x, int ipr) {
+// (or beyond the grid end it is clamped to), else bisects; with the grid
+// values at ipr and ipr + 1.
+__device__ __forceinline__ Bracket pbracket_f(const float* g, int n, float x, int ipr) {
   if (ipr >= 0) {
     const float a = __ldg(g + ipr), b = __ldg(g + ipr + 1);
     const float lo = fminf(a, b), hi = fmaxf(a, b);
     const bool low_end = (ipr == 0) && ((a < b) ? (x < a) : (x > a));
     const bool high_end = (ipr == n - 2) && ((a < b) ? (x >= b) : (x <= b));
-    if ((x >= lo && x < hi) || low_end || high_end) return ipr;
+    if ((x >= lo && x < hi) || low_end || high_end) return Bracket{ipr, a, b};
   }
-  return bracket_irrf(g, n, x);
+  const int i = bracket_irrf(g, n, x);
+  return Bracket{i, __ldg(g + i), __ldg(g + i + 1)};
 }
 
 constexpr int kStateWords = 7;  // t, e, ipr, 2 words of u hints, 2 of eps hints
@@ -226,10 +254,9 @@ __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, bool c
   }
   const float* pg = T.pf + dg * T.tp;
   const int* ntg = T.nt + dg * T.tp;
-  const int ipr = pbracket_f(pg, np, pq, s.ipr);
-  if (ipr != s.ipr) {
-    s.ipr = ipr;
-  }
+  const Bracket pb_ = pbracket_f(pg, np, pq, s.ipr);
+  const int ipr = pb_.i;
+  s.ipr = ipr;
   const int nt0 = __ldg(ntg + ipr), nt1 = __ldg(ntg + ipr + 1);
   if (nt0 < 2 || nt1 < 2) return 0.f;
   const float* t0g = T.tf + (dg * T.tp + ipr) * T.tt;
@@ -239,22 +266,15 @@ __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, bool c
   const RowF r00 = rowf_at(T, dg, ipr, it0), r01 = rowf_at(T, dg, ipr, it0 + 1);
   const RowF r10 = rowf_at(T, dg, ipr + 1, it1), r11 = rowf_at(T, dg, ipr + 1, it1 + 1);
   if (r00.n < 2 || r01.n < 2 || r10.n < 2 || r11.n < 2) return 0.f;
-  float ec[4];
-  const RowF* rows[4] = {&r00, &r01, &r10, &r11};
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    int hu = s.hu[k], he = s.he[k];
-    const float uq = cga ? ucg : rowf_u(*rows[k], s.e, &he) + du;
-    ec[k] = rowf_eps(*rows[k], uq, &hu);
-    s.hu[k] = (unsigned short)hu;
-    s.he[k] = (unsigned short)he;
-  }
-  const float e00 = ec[0], e01 = ec[1], e10 = ec[2], e11 = ec[3];
+  const float e00 = corner_eps(r00, cga, s.e, du, ucg, s.hu[0], s.he[0]);
+  const float e01 = corner_eps(r01, cga, s.e, du, ucg, s.hu[1], s.he[1]);
+  const float e10 = corner_eps(r10, cga, s.e, du, ucg, s.hu[2], s.he[2]);
+  const float e11 = corner_eps(r11, cga, s.e, du, ucg, s.hu[3], s.he[3]);
   const float ta = __ldg(t0g + it0), tb = __ldg(t0g + it0 + 1);
   const float tc = __ldg(t1g + it1), td = __ldg(t1g + it1 + 1);
   const float ea = e00 + (e01 - e00) / (tb - ta) * (tq - ta);
   const float eb = e10 + (e11 - e10) / (td - tc) * (tq - tc);
-  const float pa = __ldg(pg + ipr), pb = __ldg(pg + ipr + 1);
+  const float pa = pb_.a, pb = pb_.b;
   float w;
   if (cga && pq / pa > 0.f && pb / pa > 0.f)
     w = __logf(pq / pa) / __logf(pb / pa);

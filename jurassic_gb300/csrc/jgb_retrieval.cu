@@ -966,7 +966,10 @@ int jacobian(jgb_engine* E, WorkSet& w, const std::vector<int>& flags) {
   ECK(cudaStreamSynchronize(E->x->stream));
   FdInput in{w.cur_lev, w.cur_scal, w.geo, w.radm, w.levoff, w.rayoff, w.rad, cnt.data()};
   E->st.jacobians += list.size();
-  return fd_core(E->x, w.H, in, list, w.Kd, E->precision);
+  const double t0 = now_ms();
+  const int rc = fd_core(E->x, w.H, in, list, w.Kd, E->precision);
+  E->st.jacobian_ms += now_ms() - t0;
+  return rc;
 }
 
 // Initialisation of the flagged requests (retrieval.c:503-556).
@@ -1044,6 +1047,7 @@ int lm_iteration(jgb_engine* E, WorkSet& w) {
   if (!any) return JGB_OK;
   int rc = jacobian(E, w, J);
   if (rc) return rc;
+  double t0 = now_ms();
   // K^T W K into covn and K^T W dy into bvec; covn replaces cov where the
   // kernel was (re)computed for this iteration
   rc = normal_equations_dev(nret, w.mvec.data(), w.nvec.data(), w.Kd, w.w, w.dy, w.covn, w.bvec,
@@ -1055,6 +1059,9 @@ int lm_iteration(jgb_engine* E, WorkSet& w) {
   rc = put_flags(E, w, A);
   if (rc) return rc;
   k_gradient<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, w.sainv, w.dx, w.bvec);
+  ECK(cudaStreamSynchronize(s));
+  E->st.normal_ms += now_ms() - t0;
+  t0 = now_ms();
   std::vector<int> trying = A;
   std::vector<double> lmpar(nret, 0), cnew(nret);
   std::vector<int> st(nret), reject(nret);
@@ -1106,6 +1113,7 @@ int lm_iteration(jgb_engine* E, WorkSet& w) {
     k_axpy_state<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, -1.0, w.step, w.xi);
     for (int i = 0; i < nret; i++) trying[i] = reject[i];
   }
+  E->st.trial_ms += now_ms() - t0;
   rc = put_flags(E, w, A);
   if (rc) return rc;
   k_dot_state<<<(nret + 63) / 64, 64, 0, s>>>(nret, w.desc_d, w.active, w.step, w.bvec, w.disq);
@@ -1148,8 +1156,9 @@ int finish_requests(jgb_engine* E, WorkSet& w) {
   k_gather_state<<<nret, 128, 0, s>>>(nret, w.desc_d, w.levoff, w.elems, w.active, cur_arrays(E, w), w.xfin);
   std::vector<int> st(nret, 0);
   if (err_ana && any_ok) {
+    // the final covariance is FP64 in both precision modes
     rc = normal_equations_dev(nret, w.mvec.data(), w.nvec.data(), w.Kd, w.w, w.dy, w.covn, w.bvec,
-                              E->precision, ok.data(), w.nedesc, s);
+                              JGB_FP64, ok.data(), w.nedesc, s);
     if (rc) return ctx_error(x, rc, "normal-equation kernel failed");
     rc = put_flags(E, w, ok);
     if (rc) return rc;
@@ -1271,9 +1280,12 @@ int engine_step(jgb_engine* E) {
   }
   if (E->active.empty()) return JGB_OK;
   if (E->dirty) {
+    const double tb = now_ms();
     WorkSet& nw = E->ws[1 - E->cur];
     int rc = build_workset(E, nw, E->have_ws ? &E->ws[E->cur] : nullptr);
     if (rc) return rc;
+    ECK(cudaStreamSynchronize(x->stream));
+    E->st.rebuild_ms += now_ms() - tb;
     E->cur = 1 - E->cur;
     E->have_ws = true;
     E->dirty = false;
@@ -1287,9 +1299,17 @@ int engine_step(jgb_engine* E) {
     anyf |= F[i] != 0;
   }
   int rc = JGB_OK;
-  if (anyf) rc = init_requests(E, w, F);
+  if (anyf) {
+    const double ti = now_ms(), j0 = E->st.jacobian_ms;
+    rc = init_requests(E, w, F);
+    E->st.init_ms += now_ms() - ti - (E->st.jacobian_ms - j0);
+  }
   if (!rc) rc = lm_iteration(E, w);
-  if (!rc) rc = finish_requests(E, w);
+  if (!rc) {
+    const double tf = now_ms();
+    rc = finish_requests(E, w);
+    E->st.finish_ms += now_ms() - tf;
+  }
   E->st.steps++;
   E->st.step_ms += now_ms() - t0;
   return rc;

@@ -84,7 +84,10 @@ class EngineStats(C.Structure):
     _fields_ = [("submitted", C.c_ulonglong), ("finished", C.c_ulonglong),
                 ("failed", C.c_ulonglong), ("steps", C.c_ulonglong), ("rebuilds", C.c_ulonglong),
                 ("forward_calls", C.c_ulonglong), ("lm_trials", C.c_ulonglong),
-                ("jacobians", C.c_ulonglong), ("step_ms", C.c_double), ("active", C.c_int),
+                ("jacobians", C.c_ulonglong), ("step_ms", C.c_double),
+                ("rebuild_ms", C.c_double), ("init_ms", C.c_double), ("jacobian_ms", C.c_double),
+                ("normal_ms", C.c_double), ("trial_ms", C.c_double), ("finish_ms", C.c_double),
+                ("active", C.c_int),
                 ("queued", C.c_int), ("done", C.c_int), ("used_bytes", C.c_ulonglong)]
 
     def as_dict(self):

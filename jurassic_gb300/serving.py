@@ -62,9 +62,15 @@ def serve(engine, ctl, requests: Sequence, rate_hz: float, seed: int = 0,
             latency[j] = (clock() - t0) - arrival_of.pop(rid)
             done += 1
     wall = clock() - t0
+    est = engine.stats()
     lat_ms = latency * 1e3
     return dict(n=n, wall_s=wall, retrievals_per_s=n / wall,
                 p50_ms=float(np.percentile(lat_ms, 50)), p99_ms=float(np.percentile(lat_ms, 99)),
                 mean_ms=float(np.mean(lat_ms)), rate_hz=float(rate_hz), steps=steps,
                 iters_mean=float(np.mean([r["iters"] for r in results])),
-                failed=int(sum(1 for r in results if r["status"])), results=results)
+                failed=int(sum(1 for r in results if r["status"])),
+                engine={k: est[k] for k in ("steps", "rebuilds", "forward_calls", "lm_trials",
+                                            "jacobians", "step_ms", "rebuild_ms", "init_ms",
+                                            "jacobian_ms", "normal_ms", "trial_ms",
+                                            "finish_ms")},
+                results=results)

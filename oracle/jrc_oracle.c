@@ -1502,6 +1502,70 @@ int jrc_retrieval(jrc_ctx *c, const jrc_ret *ret, const jrc_atm *atm_apr,
                   const jrc_obs *obs_meas, double *x_final, double *y_final,
                   double *cov_out, double *costs, int maxcost, int *info,
                   int nthreads) {
+  return jrc_retrieval_ex(c, ret, atm_apr, obs_meas, x_final, y_final, cov_out, costs,
+                          maxcost, info, nthreads, NULL);
+}
+
+/* Error analysis after the covariance (retrieval.c:686-726): gain
+   G = cov K^T diag(sig_inv^2) (dgemm in k order), noise and forward-model
+   error standard deviations sqrt(diag(G diag(sig^2) G^T)) (matrix_product
+   with transpose == 2, write_stddev), averaging kernel A = G K and
+   analyze_avk (257-336): per element the row sum over its quantity's block
+   on top of copy_atm's init value (1 for surface emissivities, else 0) and
+   1/A_ii. */
+static void error_analysis(const jrc_ctx *c, const double *cov, const double *kk,
+                           const double *sig_inv, const double *sig_noise,
+                           const double *sig_fm, const int *iqa, int m, int n,
+                           jrc_ana *ana) {
+  double *G = malloc((size_t) n * (size_t) m * sizeof(double));
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < m; j++) {
+      double s = 0;
+      for (int k = 0; k < n; k++)
+        s += cov[(size_t) i * n + k] * (kk[(size_t) j * n + k] * sq(sig_inv[j]));
+      G[(size_t) i * m + j] = s;
+    }
+  for (int i = 0; i < n; i++) {
+    double sn = 0, sf = 0;
+    for (int j = 0; j < m; j++) {
+      sn += sq(G[(size_t) i * m + j] * sig_noise[j]);
+      sf += sq(G[(size_t) i * m + j] * sig_fm[j]);
+    }
+    if (ana->err_total) ana->err_total[i] = sqrt(cov[(size_t) i * n + i]);
+    if (ana->err_noise) ana->err_noise[i] = sqrt(sn);
+    if (ana->err_formod) ana->err_formod[i] = sqrt(sf);
+  }
+  double *A = malloc((size_t) n * (size_t) n * sizeof(double));
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) {
+      double s = 0;
+      for (int k = 0; k < m; k++)
+        s += G[(size_t) i * m + k] * kk[(size_t) k * n + j];
+      A[(size_t) i * n + j] = s;
+    }
+  for (int i = 0; i < n; i++) {
+    int n0 = -1, n1 = 0;
+    for (int j = 0; j < n; j++)
+      if (iqa[j] == iqa[i]) {
+        if (n0 < 0) n0 = j;
+        n1 = j - n0 + 1;
+      }
+    double s = iqa[i] >= Q_SFEPS(c, 0) ? 1.0 : 0.0;
+    for (int j = 0; j < n1; j++)
+      s += A[(size_t) i * n + n0 + j];
+    if (ana->cont) ana->cont[i] = s;
+    if (ana->res) ana->res[i] = 1 / A[(size_t) i * n + i];
+  }
+  if (ana->gain) memcpy(ana->gain, G, (size_t) n * (size_t) m * sizeof(double));
+  if (ana->avk) memcpy(ana->avk, A, (size_t) n * (size_t) n * sizeof(double));
+  free(G);
+  free(A);
+}
+
+int jrc_retrieval_ex(jrc_ctx *c, const jrc_ret *ret, const jrc_atm *atm_apr,
+                     const jrc_obs *obs_meas, double *x_final, double *y_final,
+                     double *cov_out, double *costs, int maxcost, int *info,
+                     int nthreads, jrc_ana *ana) {
   const int nd = c->nd, np = atm_apr->np, nr = obs_meas->nr;
   int m, n;
   jrc_sizes(c, atm_apr, obs_meas, &m, &n);
@@ -1731,6 +1795,8 @@ int jrc_retrieval(jrc_ctx *c, const jrc_ret *ret, const jrc_atm *atm_apr,
       goto done;
     }
     memcpy(cov_out, cov, (size_t) n * (size_t) n * sizeof(double));
+    if (ana)
+      error_analysis(c, cov, kk, sig_inv, sig_noise, sig_fm, iqa, m, n, ana);
   }
   info[0] = n;
   info[1] = m;

@@ -134,6 +134,19 @@ int jrc_retrieval(jrc_ctx *c, const jrc_ret *ret, const jrc_atm *atm_apr,
                   double *cov, double *costs, int maxcost, int *info,
                   int nthreads);
 
+/* Error analysis outputs (retrieval.c:668-726), any pointer may be NULL:
+   gain[n][m], avk[n][n], standard deviations err_total/err_noise/err_formod[n]
+   and analyze_avk's cont/res[n], all in state-vector order. */
+typedef struct {
+  double *gain, *avk, *err_total, *err_noise, *err_formod, *cont, *res;
+} jrc_ana;
+
+/* jrc_retrieval plus the error analysis (needs err_ana and cov != NULL). */
+int jrc_retrieval_ex(jrc_ctx *c, const jrc_ret *ret, const jrc_atm *atm_apr,
+                     const jrc_obs *obs_meas, double *x_final, double *y_final,
+                     double *cov, double *costs, int maxcost, int *info,
+                     int nthreads, jrc_ana *ana);
+
 #ifdef __cplusplus
 }
 #endif

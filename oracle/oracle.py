@@ -70,6 +70,11 @@ class _Ret(C.Structure):
                 ("err_sfp", C.c_double), ("err_sft", C.c_double), ("err_sfeps", _dp)]
 
 
+class _Ana(C.Structure):
+    _fields_ = [(k, _dp) for k in ("gain", "avk", "err_total", "err_noise", "err_formod", "cont",
+                                   "res")]
+
+
 def _d(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
@@ -106,6 +111,9 @@ def lib():
         L.jrc_kernel.argtypes = [C.c_void_p, C.POINTER(_Atm), C.POINTER(_Obs), _dp, C.c_int]
         L.jrc_retrieval.argtypes = [C.c_void_p, C.POINTER(_Ret), C.POINTER(_Atm),
                                     C.POINTER(_Obs), _dp, _dp, _dp, _dp, C.c_int, _ip, C.c_int]
+        L.jrc_retrieval_ex.argtypes = [C.c_void_p, C.POINTER(_Ret), C.POINTER(_Atm),
+                                       C.POINTER(_Obs), _dp, _dp, _dp, _dp, C.c_int, _ip, C.c_int,
+                                       C.POINTER(_Ana)]
         _lib = L
     return _lib
 
@@ -279,8 +287,15 @@ class Oracle:
         cov = np.zeros((n, n))
         costs = np.zeros(maxcost)
         info = np.zeros(4, np.int32)
-        self._check(lib().jrc_retrieval(self.h, C.byref(sr), C.byref(sa), C.byref(so), _ptr(x),
-                                        _ptr(y), _ptr(cov), _ptr(costs), maxcost,
-                                        _ptr(info, _ip), nthreads))
-        return dict(x=x, y=y, cov=cov if r.err_ana else None, costs=costs[:info[2]],
-                    n=int(info[0]), m=int(info[1]), iters=int(info[3]))
+        ana = dict(gain=np.zeros((n, m)), avk=np.zeros((n, n)), err_total=np.zeros(n),
+                   err_noise=np.zeros(n), err_formod=np.zeros(n), cont=np.zeros(n),
+                   res=np.zeros(n))
+        sana = _Ana(**{k: _ptr(v) for k, v in ana.items()})
+        self._check(lib().jrc_retrieval_ex(self.h, C.byref(sr), C.byref(sa), C.byref(so),
+                                           _ptr(x), _ptr(y), _ptr(cov), _ptr(costs), maxcost,
+                                           _ptr(info, _ip), nthreads, C.byref(sana)))
+        out = dict(x=x, y=y, cov=cov if r.err_ana else None, costs=costs[:info[2]],
+                   n=int(info[0]), m=int(info[1]), iters=int(info[3]))
+        if r.err_ana:
+            out.update(ana)
+        return out

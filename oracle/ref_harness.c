@@ -238,12 +238,44 @@ static int g_cap_have_atm;
 static double *g_cap_cov;
 static size_t g_cap_cov_n;
 
+/* error analysis (retrieval.c:668-726): gain [n][m], averaging kernel
+   [n][n] and the state-vector form (atm2x) of the atm_err_{total,noise,
+   formod}.tab, atm_cont.tab and atm_res.tab files */
+static double *g_cap_gain, *g_cap_avk;
+static size_t g_cap_gain_n, g_cap_gain_m, g_cap_avk_n;
+static const char *g_ana_files[5] = {"atm_err_total.tab", "atm_err_noise.tab",
+                                     "atm_err_formod.tab", "atm_cont.tab", "atm_res.tab"};
+static double *g_cap_ana[5];
+static size_t g_cap_ana_n[5];
+
+static void cap_matrix(const gsl_matrix *m, double **dst, size_t *n1, size_t *n2) {
+  free(*dst);
+  *n1 = m->size1;
+  if (n2) *n2 = m->size2;
+  *dst = (double *) malloc(m->size1 * m->size2 * sizeof(double));
+  for (size_t i = 0; i < m->size1; i++)
+    for (size_t j = 0; j < m->size2; j++)
+      (*dst)[i * m->size2 + j] = gsl_matrix_get(m, i, j);
+}
+
 void jref_hook_write_atm(const char *dirname, const char *filename,
                          const ctl_t * ctl, const atm_t * atm) {
   if (strcmp(filename, "atm_final.tab") == 0) {
     copy_atm(ctl, &g_cap_atm_final, atm, 0);
     g_cap_have_atm = 1;
   }
+  for (int k = 0; k < 5; k++)
+    if (strcmp(filename, g_ana_files[k]) == 0) {
+      const size_t n = atm2x(ctl, atm, NULL, NULL, NULL);
+      gsl_vector *v = gsl_vector_alloc(n);
+      atm2x(ctl, atm, v, NULL, NULL);
+      free(g_cap_ana[k]);
+      g_cap_ana[k] = (double *) malloc(n * sizeof(double));
+      for (size_t i = 0; i < n; i++)
+        g_cap_ana[k][i] = gsl_vector_get(v, i);
+      g_cap_ana_n[k] = n;
+      gsl_vector_free(v);
+    }
   write_atm(dirname, filename, ctl, atm);
 }
 
@@ -264,6 +296,10 @@ void jref_hook_write_matrix(const char *dirname, const char *filename,
   (void) rowspace;
   (void) colspace;
   (void) sort;
+  if (strcmp(filename, "matrix_gain.tab") == 0)
+    cap_matrix(matrix, &g_cap_gain, &g_cap_gain_n, &g_cap_gain_m);
+  if (strcmp(filename, "matrix_avk.tab") == 0)
+    cap_matrix(matrix, &g_cap_avk, &g_cap_avk_n, NULL);
   if (strcmp(filename, "matrix_cov_ret.tab") == 0) {
     free(g_cap_cov);
     g_cap_cov_n = matrix->size1;
@@ -286,6 +322,9 @@ int jref_retrieval(const char *dir, double *x_final, int maxn, double *cov,
   snprintf(g_ret.dir, LEN, "%s", dir);
   g_cap_have_atm = 0;
   g_cap_cov_n = 0;
+  g_cap_gain_n = g_cap_gain_m = g_cap_avk_n = 0;
+  for (int k = 0; k < 5; k++)
+    g_cap_ana_n[k] = 0;
   optimal_estimation(&g_ret, &g_ctl, &g_obs, &obs_i, &g_atm, &atm_i);
   gsl_vector *x = gsl_vector_alloc((size_t) maxn);
   const size_t n = atm2x(&g_ctl, &atm_i, NULL, NULL, NULL);
@@ -318,5 +357,22 @@ int jref_retrieval(const char *dir, double *x_final, int maxn, double *cov,
     fclose(in);
   }
   info[2] = nc;
+  return 0;
+}
+
+/* Error-analysis outputs of the last jref_retrieval (ERR_ANA): gain[n*m],
+   avk[n*n], ana[5*n] = err_total, err_noise, err_formod, cont, res in
+   state-vector order.  Returns 0, or -1 if they were not written. */
+int jref_retrieval_ana(double *gain, double *avk, double *ana, int maxn, int maxm) {
+  const size_t n = g_cap_avk_n;
+  if (n == 0 || g_cap_gain_n != n || (int) n > maxn || (int) g_cap_gain_m > maxm)
+    return -1;
+  for (int k = 0; k < 5; k++)
+    if (g_cap_ana_n[k] != n)
+      return -1;
+  memcpy(gain, g_cap_gain, n * g_cap_gain_m * sizeof(double));
+  memcpy(avk, g_cap_avk, n * n * sizeof(double));
+  for (int k = 0; k < 5; k++)
+    memcpy(ana + k * n, g_cap_ana[k], n * sizeof(double));
   return 0;
 }

@@ -119,9 +119,17 @@ def _child(args):
                                   info.ctypes.data_as(C.POINTER(C.c_int)))
             if rc:
                 raise RuntimeError("jref_retrieval failed")
-            n = int(info[0])
-            out.append(dict(x=x[:n], cov=cov[:n * n].reshape(n, n) if info[3] else None,
-                            costs=costs[:info[2]], n=n, m=int(info[1])))
+            n, m = int(info[0]), int(info[1])
+            r = dict(x=x[:n], cov=cov[:n * n].reshape(n, n) if info[3] else None,
+                     costs=costs[:info[2]], n=n, m=m)
+            gain, avk, ana = np.zeros(n * m), np.zeros(n * n), np.zeros(5 * n)
+            if hasattr(L, "jref_retrieval_ana") and L.jref_retrieval_ana(
+                    gain.ctypes.data_as(dp), avk.ctypes.data_as(dp), ana.ctypes.data_as(dp),
+                    n, m) == 0:
+                r.update(gain=gain.reshape(n, m), avk=avk.reshape(n, n),
+                         **{k: ana[i * n:(i + 1) * n] for i, k in enumerate(
+                             ("err_total", "err_noise", "err_formod", "cont", "res"))})
+            out.append(r)
         else:
             raise ValueError(kind)
     return out

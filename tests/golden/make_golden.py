@@ -171,8 +171,10 @@ def retrieval_case():
     r = refimpl.run(ctl, tbl, filters, [("retrieval", apr, obs_meas, {"maxn": 256})],
                     ret=ret)[0]
     rj = {k: (v.tolist() if isinstance(v, np.ndarray) else v) for k, v in ret.sized(ctl).__dict__.items()}
+    ana = {k: r[k] for k in ("gain", "avk", "err_total", "err_noise", "err_formod", "cont",
+                             "res")}
     save("ref_retrieval.npz", ctl=ctl_json(ctl), ret=json.dumps(rj), x=r["x"], cov=r["cov"],
-         costs=r["costs"], **table_arrays(tbl, filters), **atm_arrays("atm_", ctl, apr),
+         costs=r["costs"], **ana, **table_arrays(tbl, filters), **atm_arrays("atm_", ctl, apr),
          **obs_arrays("obs_", obs_meas))
 
 

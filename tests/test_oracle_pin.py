@@ -117,6 +117,11 @@ def test_retrieval_vs_reference(built_oracle):
     # costs.tab is written with %g by the reference
     assert np.allclose(r["costs"], f["costs"], rtol=1e-5)
     assert np.max(np.abs(r["cov"] - f["cov"])) <= 1e-8 * np.max(np.abs(f["cov"]))
+    # error analysis (retrieval.c:668-726): gain, averaging kernel, error
+    # standard deviations and analyze_avk's contribution/resolution
+    for k in ("gain", "avk", "err_total", "err_noise", "err_formod", "cont", "res"):
+        assert r[k].shape == f[k].shape, k
+        assert np.max(np.abs(r[k] - f[k])) <= 1e-8 * np.max(np.abs(f[k])), k
 
 
 def test_oracle_direct_vs_reference_build(built_oracle):

@@ -43,6 +43,21 @@ def test_retrieval_golden_fp64(built_lib, built_oracle):
     assert np.max(np.abs(cov - f["cov"])) <= 1e-6 * np.max(np.abs(f["cov"]))
 
 
+def test_error_analysis_golden_fp64(built_lib, built_oracle):
+    """Gain, averaging kernel, noise/formod/total error and analyze_avk
+    outputs of the engine against the reference's own files
+    (matrix_gain.tab, matrix_avk.tab, atm_err_*.tab, atm_cont.tab,
+    atm_res.tab, retrieval.c:668-726), within 1e-6 of each output's largest
+    entry."""
+    f, ctl, ret, tbl, filt, apr, meas = _golden()
+    ctx = native.Context(ctl, tbl, filt)
+    r = ctx.engine(ret, native.FP64, keep_gain=True).run(synth.pack(ctl, [(apr, meas)]))[0]
+    assert r["status"] == 0
+    for k in ("gain", "avk", "err_total", "err_noise", "err_formod", "cont", "res"):
+        assert r[k].shape == f[k].shape, k
+        assert np.max(np.abs(r[k] - f[k])) <= 1e-6 * np.max(np.abs(f[k])), k
+
+
 def _nadir_retrievals(nobs=3):
     w = synth.config_nadir(nobs, nd=8, nlev=31, ztop=60.0, emitters=("CO2", "H2O"),
                            numin=660.0, numax=1600.0)
