@@ -272,6 +272,25 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
       x->srf_stale = false;
     }
     if (x->meta_stale) {
+      // emitters whose (float) p and T grids are identical for all channels:
+      // their brackets are found once per LOS point in the tile packing
+      x->grid_mask = 0;
+      if (x->tp <= 1023 && x->tt <= 1023)
+        for (int g = 0; g < c.ng; g++) {
+          bool same = x->h_np[g] >= 30;
+          for (int id = 1; id < c.nd && same; id++) {
+            const size_t a = (size_t)g, b = (size_t)id * c.ng + g;
+            same = x->h_np[b] == x->h_np[a] &&
+                   std::equal(x->h_nt.begin() + a * x->tp, x->h_nt.begin() + (a + 1) * x->tp,
+                              x->h_nt.begin() + b * x->tp) &&
+                   std::equal(x->h_pf.begin() + a * x->tp, x->h_pf.begin() + (a + 1) * x->tp,
+                              x->h_pf.begin() + b * x->tp) &&
+                   std::equal(x->h_tf.begin() + a * x->tp * x->tt,
+                              x->h_tf.begin() + (a + 1) * x->tp * x->tt,
+                              x->h_tf.begin() + b * x->tp * x->tt);
+          }
+          if (same) x->grid_mask |= 1u << g;
+        }
       launch_rowmeta((long long)c.nd * c.ng * x->tp * x->tt, x->tu, x->t_nu.as<int>(),
                      x->t_u.as<float>(), x->t_eps.as<float>(), x->t_meta.as<float4>(), s);
       x->meta_stale = false;
@@ -311,10 +330,11 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
     long long tile_points = 0;
     CK(cudaMemcpyAsync(&tile_points, toff + ntile, sizeof(long long), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    Pm.nfield = mixed_nfield(c);
+    Pm.brmask = x->grid_mask;
+    Pm.nfield = mixed_nfield(c, Pm.brmask);
     CK(x->tiles_data.reserve(sizeof(float) * 32 * (size_t)std::max(tile_points, 1LL) * Pm.nfield));
     Pm.data = x->tiles_data.as<float>();
-    launch_pack_tiles_n(c, L, Pm, tile_points, s);
+    launch_pack_tiles_n(c, tbl_view(x), L, Pm, tile_points, s);
     CK(cudaGetLastError());
     float* refl = nullptr;
     if (need_refl) {
@@ -833,6 +853,9 @@ int jgb_tables_init(jgb_ctx* x, int tp, int tt, int tu) {
   x->tt = tt;
   x->tu = tu;
   x->h_np.assign(ndg, -1);
+  x->h_nt.assign(ndg * tp, 0);
+  x->h_pf.assign(ndg * tp, 0.f);
+  x->h_tf.assign(ndg * tp * tt, 0.f);
   CK(x->t_np.reserve(sizeof(int) * std::max<size_t>(ndg, 1)));
   CK(x->t_p.reserve(sizeof(double) * std::max<size_t>(ndg * tp, 1)));
   CK(x->t_nt.reserve(sizeof(int) * std::max<size_t>(ndg * tp, 1)));
@@ -882,6 +905,9 @@ int jgb_set_table(jgb_ctx* x, int id, int ig, int np, const double* p, const int
       nuv[(size_t)ip * x->tt + it] = n;
     }
   }
+  std::copy(ntv.begin(), ntv.end(), x->h_nt.begin() + dg * x->tp);
+  std::copy(pf.begin(), pf.end(), x->h_pf.begin() + dg * x->tp);
+  std::copy(tf.begin(), tf.end(), x->h_tf.begin() + dg * x->tp * x->tt);
   CK(cudaMemcpy(x->t_p.as<double>() + dg * x->tp, pv.data(), sizeof(double) * x->tp, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(x->t_pf.as<float>() + dg * x->tp, pf.data(), sizeof(float) * x->tp, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(x->t_nt.as<int>() + dg * x->tp, ntv.data(), sizeof(int) * x->tp, cudaMemcpyHostToDevice));

@@ -53,6 +53,11 @@ struct jgb_ctx {
   int tp = 0, tt = 0, tu = 0;
   bool tables_init = false;
   std::vector<int> h_np;
+  // host copies of the float grids of the mixed path (padded like the device
+  // arrays) and the emitters whose grids are the same for every channel
+  std::vector<int> h_nt;
+  std::vector<float> h_pf, h_tf;
+  unsigned grid_mask = 0;
   jgb::DevBuf t_np, t_p, t_nt, t_t, t_nu, t_u, t_eps, t_pf, t_tf, t_meta;
   bool meta_stale = true;
   // source function

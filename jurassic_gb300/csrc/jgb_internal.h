@@ -28,9 +28,10 @@ struct MixedPlan {
   int* tlen;            // [ntile]
   float* data;          // tile planes
   int nfield;
+  unsigned brmask;      // emitters with p-T brackets precomputed per LOS point
 };
-int mixed_nfield(const CtlDev& c);
-void launch_pack_tiles_n(const CtlDev& c, const LosDev& L, const MixedPlan& P,
+int mixed_nfield(const CtlDev& c, unsigned brmask);
+void launch_pack_tiles_n(const CtlDev& c, const TblDev& T, const LosDev& L, const MixedPlan& P,
                          long long total_tile_points, cudaStream_t s);
 int path_mixed_variants();
 void launch_path_mixed(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,

@@ -20,12 +20,15 @@
 
 namespace jgb {
 
-// Field indices of a tile plane.
+// Field indices of a tile plane.  br0..br0+ng-1 hold, for emitters whose
+// p-T grids are shared by all channels, the packed bracket of the point
+// (ipr | it0 << 10 | it1 << 20; kNoBracket: no table, kNoBracket | 2: no
+// temperature rows at that pressure).
 struct Fields {
-  int p, t, ds, qh2o, aux, kw0, u0, cgp0, cgt0, cgu0, n;
+  int p, t, ds, qh2o, aux, kw0, u0, cgp0, cgt0, cgu0, br0, n;
 };
 
-__host__ __device__ inline Fields fields_of(const CtlDev& c) {
+__host__ __device__ inline Fields fields_of(const CtlDev& c, unsigned brmask) {
   Fields f;
   f.p = 0;
   f.t = 1;
@@ -37,48 +40,14 @@ __host__ __device__ inline Fields fields_of(const CtlDev& c) {
   f.cgp0 = f.u0 + c.ng;
   f.cgt0 = f.cgp0 + c.ng;
   f.cgu0 = f.cgt0 + c.ng;
-  f.n = c.formod == 0 ? f.cgu0 + c.ng : f.u0 + c.ng;
+  f.br0 = c.formod == 0 ? f.cgu0 + c.ng : f.u0 + c.ng;
+  f.n = f.br0 + (brmask ? c.ng : 0);
   return f;
 }
 
-int mixed_nfield(const CtlDev& c) { return fields_of(c).n; }
+int mixed_nfield(const CtlDev& c, unsigned brmask) { return fields_of(c, brmask).n; }
 
-// One thread per (tile, point, lane) converts the FP64 LOS to float tiles.
-__global__ void k_pack_tiles(CtlDev c, LosDev L, MixedPlan P, long long total) {
-  const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= total * 32) return;
-  const int lane = (int)(gid & 31);
-  const long long tp = gid >> 5;  // tile-point
-  // locate the tile by binary search over tile offsets
-  int lo = 0, hi = P.ntile;
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (P.toff[mid] <= tp) lo = mid; else hi = mid;
-  }
-  const int tile = lo;
-  const int ip = (int)(tp - P.toff[tile]);
-  const int r = P.perm[tile * 32 + lane];
-  const Fields F = fields_of(c);
-  float* out = P.data + tp * (long long)F.n * 32 + lane;
-  if (r < 0 || ip >= L.count[r]) {
-    for (int f = 0; f < F.n; f++) out[f * 32] = 0.f;
-    return;
-  }
-  const long long q = L.off[r] + ip;
-  out[F.p * 32] = (float)L.p[q];
-  out[F.t * 32] = (float)L.t[q];
-  out[F.ds * 32] = (float)L.ds[q];
-  out[F.qh2o * 32] = c.ig_h2o >= 0 ? (float)L.qh2o[q] : 0.f;
-  out[F.aux * 32] = (float)L.aux[q];
-  for (int w = 0; w < c.nw; w++) out[(F.kw0 + w) * 32] = (float)L.kw[w * L.cap + q];
-  for (int g = 0; g < c.ng; g++) out[(F.u0 + g) * 32] = (float)L.u[g * L.cap + q];
-  if (c.formod == 0)
-    for (int g = 0; g < c.ng; g++) {
-      out[(F.cgp0 + g) * 32] = (float)L.cgp[g * L.cap + q];
-      out[(F.cgt0 + g) * 32] = (float)L.cgt[g * L.cap + q];
-      out[(F.cgu0 + g) * 32] = (float)L.cgu[g * L.cap + q];
-    }
-}
+constexpr unsigned kNoBracket = 0x80000000u;
 
 // ---------------------------------------------------------------------------
 // float table access with hinted searches
@@ -212,6 +181,63 @@ __device__ __forceinline__ int bracket_irrf(const float* g, int n, float x) {
   return lo;
 }
 
+// One thread per (tile, point, lane) converts the FP64 LOS to float tiles.
+__global__ void k_pack_tiles(CtlDev c, TblDev T, LosDev L, MixedPlan P, long long total) {
+  const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= total * 32) return;
+  const int lane = (int)(gid & 31);
+  const long long tp = gid >> 5;  // tile-point
+  // locate the tile by binary search over tile offsets
+  int lo = 0, hi = P.ntile;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (P.toff[mid] <= tp) lo = mid; else hi = mid;
+  }
+  const int tile = lo;
+  const int ip = (int)(tp - P.toff[tile]);
+  const int r = P.perm[tile * 32 + lane];
+  const Fields F = fields_of(c, P.brmask);
+  float* out = P.data + tp * (long long)F.n * 32 + lane;
+  if (r < 0 || ip >= L.count[r]) {
+    for (int f = 0; f < F.n; f++) out[f * 32] = 0.f;
+    return;
+  }
+  const long long q = L.off[r] + ip;
+  out[F.p * 32] = (float)L.p[q];
+  out[F.t * 32] = (float)L.t[q];
+  out[F.ds * 32] = (float)L.ds[q];
+  out[F.qh2o * 32] = c.ig_h2o >= 0 ? (float)L.qh2o[q] : 0.f;
+  out[F.aux * 32] = (float)L.aux[q];
+  for (int w = 0; w < c.nw; w++) out[(F.kw0 + w) * 32] = (float)L.kw[w * L.cap + q];
+  for (int g = 0; g < c.ng; g++) out[(F.u0 + g) * 32] = (float)L.u[g * L.cap + q];
+  if (c.formod == 0)
+    for (int g = 0; g < c.ng; g++) {
+      out[(F.cgp0 + g) * 32] = (float)L.cgp[g * L.cap + q];
+      out[(F.cgt0 + g) * 32] = (float)L.cgt[g * L.cap + q];
+      out[(F.cgu0 + g) * 32] = (float)L.cgu[g * L.cap + q];
+    }
+  // p-T brackets on the grids of channel 0 (identical for every channel)
+  for (int g = 0; P.brmask && g < c.ng; g++) {
+    unsigned wd = kNoBracket;  // no table (np < 30)
+    const int np = __ldg(T.np + g);
+    if (((P.brmask >> g) & 1u) && np >= 30) {
+      const float pq = c.formod == 0 ? (float)L.cgp[g * L.cap + q] : (float)L.p[q];
+      const float tq = c.formod == 0 ? (float)L.cgt[g * L.cap + q] : (float)L.t[q];
+      const int ipr = bracket_irrf(T.pf + (long long)g * T.tp, np, pq);
+      const int nt0 = __ldg(T.nt + (long long)g * T.tp + ipr);
+      const int nt1 = __ldg(T.nt + (long long)g * T.tp + ipr + 1);
+      wd = kNoBracket | 2u;      // temperature rows missing at this pressure
+      if (nt0 >= 2 && nt1 >= 2) {
+        const float* t0g = T.tf + ((long long)g * T.tp + ipr) * T.tt;
+        const int it0 = bracket_regf(t0g, nt0, tq);
+        const int it1 = bracket_regf(t0g + T.tt, nt1, tq);
+        wd = (unsigned)ipr | ((unsigned)it0 << 10) | ((unsigned)it1 << 20);
+      }
+    }
+    out[(F.br0 + g) * 32] = __uint_as_float(wd);
+  }
+}
+
 // Pressure bracket with a hint: keeps ipr while p lies inside its interval
 // (or beyond the grid end it is clamped to), else bisects; with the grid
 // values at ipr and ipr + 1.
@@ -241,28 +267,48 @@ struct GasState {
 // One (channel, emitter) at one LOS point (intpol_tbl_ega / intpol_tbl_cga,
 // jurassic.c:3710-3891).  Returns the segment emissivity; *sat is set where
 // the reference's segment transmittance becomes zero.
+// brw: packed bracket precomputed for the LOS point (grids shared by all
+// channels), or kNoBracket | 1 to search here.
 __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, bool cga, float pq,
-                                           float tq, float du, float ucg, GasState& s,
-                                           bool& sat) {
-  const int np = __ldg(T.np + dg);
-  if (np < 30) return 0.f;
+                                           float tq, float du, float ucg, unsigned brw,
+                                           GasState& s, bool& sat) {
+  const bool pre = brw != (kNoBracket | 1u);
+  if (pre && brw == kNoBracket) return 0.f;   // np < 30
+  const float* pg = T.pf + dg * T.tp;
+  int np = 0;
+  if (!pre) {
+    np = __ldg(T.np + dg);
+    if (np < 30) return 0.f;
+  }
   if (s.t < 1e-9f) {
     s.t = 0.f;
     s.e = 1.f;
     sat = true;
     return 1.f;
   }
-  const float* pg = T.pf + dg * T.tp;
-  const int* ntg = T.nt + dg * T.tp;
-  const Bracket pb_ = pbracket_f(pg, np, pq, s.ipr);
-  const int ipr = pb_.i;
-  s.ipr = ipr;
-  const int nt0 = __ldg(ntg + ipr), nt1 = __ldg(ntg + ipr + 1);
-  if (nt0 < 2 || nt1 < 2) return 0.f;
+  int ipr, it0, it1;
+  float pa, pb;
+  if (pre) {
+    if (brw & kNoBracket) return 0.f;         // nt < 2 at this pressure
+    ipr = (int)(brw & 1023u);
+    it0 = (int)((brw >> 10) & 1023u);
+    it1 = (int)((brw >> 20) & 1023u);
+    pa = __ldg(pg + ipr);
+    pb = __ldg(pg + ipr + 1);
+  } else {
+    const int* ntg = T.nt + dg * T.tp;
+    const Bracket pb_ = pbracket_f(pg, np, pq, s.ipr);
+    ipr = pb_.i;
+    s.ipr = ipr;
+    pa = pb_.a;
+    pb = pb_.b;
+    const int nt0 = __ldg(ntg + ipr), nt1 = __ldg(ntg + ipr + 1);
+    if (nt0 < 2 || nt1 < 2) return 0.f;
+    it0 = bracket_regf(T.tf + (dg * T.tp + ipr) * T.tt, nt0, tq);
+    it1 = bracket_regf(T.tf + (dg * T.tp + ipr + 1) * T.tt, nt1, tq);
+  }
   const float* t0g = T.tf + (dg * T.tp + ipr) * T.tt;
   const float* t1g = t0g + T.tt;
-  const int it0 = bracket_regf(t0g, nt0, tq);
-  const int it1 = bracket_regf(t1g, nt1, tq);
   const RowF r00 = rowf_at(T, dg, ipr, it0), r01 = rowf_at(T, dg, ipr, it0 + 1);
   const RowF r10 = rowf_at(T, dg, ipr + 1, it1), r11 = rowf_at(T, dg, ipr + 1, it1 + 1);
   if (r00.n < 2 || r01.n < 2 || r10.n < 2 || r11.n < 2) return 0.f;
@@ -274,7 +320,6 @@ __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, bool c
   const float tc = __ldg(t1g + it1), td = __ldg(t1g + it1 + 1);
   const float ea = e00 + (e01 - e00) / (tb - ta) * (tq - ta);
   const float eb = e10 + (e11 - e10) / (td - tc) * (tq - tc);
-  const float pa = pb_.a, pb = pb_.b;
   float w;
   if (cga && pq / pa > 0.f && pb / pa > 0.f)
     w = __logf(pq / pa) / __logf(pb / pa);
@@ -311,7 +356,7 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
   int r = P.perm[tile * 32 + lane];
   if (r >= 0 && b.obs_skip && b.obs_skip[b.ray_obs[r]]) r = -1;  // lane idle, outputs untouched
   const int n = r >= 0 ? L.count[r] : 0;
-  const Fields F = fields_of(c);
+  const Fields F = fields_of(c, P.brmask);
   const float* base = P.data + P.toff[tile] * (long long)F.n * 32 + lane;
   const bool cga = c.formod == 0;
   const double nud = ch.nu[id];
@@ -406,8 +451,10 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
       const float pq = cga ? f[(F.cgp0 + g) * 32] : p;
       const float tq = cga ? f[(F.cgt0 + g) * 32] : t;
       const float ucg = cga ? f[(F.cgu0 + g) * 32] : 0.f;
+      const unsigned brw = ((P.brmask >> g) & 1u) ? __float_as_uint(f[(F.br0 + g) * 32])
+                                                   : (kNoBracket | 1u);
       GasState st = sload(g);
-      const float eg = gas_eps_f(T, dg0 + g, cga, pq, tq, du, ucg, st, sat);
+      const float eg = gas_eps_f(T, dg0 + g, cga, pq, tq, du, ucg, brw, st, sat);
       sstore(g, st);
       E = E + (1.f - E) * eg;
     }
@@ -549,11 +596,11 @@ __global__ void k_to_float(long long n, const double* src, float* dst) {
   if (i < n) dst[i] = (float)src[i];
 }
 
-void launch_pack_tiles_n(const CtlDev& c, const LosDev& L, const MixedPlan& P,
+void launch_pack_tiles_n(const CtlDev& c, const TblDev& T, const LosDev& L, const MixedPlan& P,
                          long long total_tile_points, cudaStream_t s) {
   const long long nth = total_tile_points * 32;
   const int bs = 256;
-  k_pack_tiles<<<(unsigned)((nth + bs - 1) / bs), bs, 0, s>>>(c, L, P, total_tile_points);
+  k_pack_tiles<<<(unsigned)((nth + bs - 1) / bs), bs, 0, s>>>(c, T, L, P, total_tile_points);
 }
 
 int path_mixed_variants() { return 4; }
