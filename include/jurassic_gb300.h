@@ -153,6 +153,16 @@ int jgb_normal_equations(jgb_ctx *ctx, int nret, const int *m, const int *n, con
                          const double *w, const double *dy, double *A, double *b,
                          int precision);
 
+/* Emitter contributions (TASK c, formod.c:200-249) of every observation of a
+   host batch: continua off; variant g < ng keeps only emitter g (all other
+   mixing ratios and all extinction zero), variant ng ("EXTINCT") has all
+   mixing ratios zero and the extinction kept.  The batch holds the
+   atmosphere as after formod (pressures after hydrostatic equilibrium) and
+   in rad the mask (NaN = not computed).
+   Out: rad[ng+1][nd][nray], tau[ng+1][nd][nray] (tau may be NULL). */
+int jgb_formod_contrib(jgb_ctx *ctx, const jgb_batch *b, double *rad, double *tau,
+                       int precision);
+
 /* Retrieval settings (ret_t, retrieval.c:32-112; read_ret, 753-804). */
 typedef struct {
   int kernel_recomp, conv_itmax, err_ana;

@@ -30,6 +30,7 @@ UNITS = {
     "jgb_noalloc.cu": [],
     "jgb_normal.cu": ["-fmad=false"],
     "jgb_retrieval.cu": ["-fmad=false"],
+    "jgb_trace_mixed.cu": ["-fmad=false"],
 }
 
 

@@ -215,7 +215,10 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
   L.nw = c.nw;
   L.cga = c.formod == 0;
   ChanDev ch = chan_view(x);
-  launch_trace_count(c, ch, b, L, d_err, s);
+  if (precision == JGB_MIXED)
+    launch_trace_count_mixed(c, b, L, d_err, s);
+  else
+    launch_trace_count(c, ch, b, L, d_err, s);
   CK(cudaGetLastError());
   long long* cnt64 = x->los_cnt64.as<long long>();
   k_widen<<<(nray + 255) / 256, 256, 0, s>>>(nray, L.count, cnt64);
@@ -249,7 +252,10 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
   L.cgp = L.kw + (long long)c.nw * cap;
   L.cgt = L.cgp + (long long)c.ng * cap;
   L.cgu = L.cgt + (long long)c.ng * cap;
-  launch_trace_fill(c, ch, b, L, d_err, s);
+  if (precision == JGB_MIXED)
+    launch_trace_fill_mixed(c, b, L, d_err, s);
+  else
+    launch_trace_fill(c, ch, b, L, d_err, s);
   CK(cudaGetLastError());
   CK(cudaEventRecord(x->ev[3], s));
 
@@ -1235,3 +1241,78 @@ int jgb_memcpy_d2h(void* dst, const void* src, unsigned long long bytes) {
 }
 
 }  // extern "C"
+
+// Emitter contributions (TASK c, formod.c:200-249): with the continua
+// switched off, one forward model per emitter with every other emitter's
+// volume mixing ratio and all extinction set to zero, then one with all
+// mixing ratios zero and the extinction kept ("EXTINCT").  All ng + 1
+// variants of every observation run as one batch.
+extern "C" int jgb_formod_contrib(jgb_ctx* x, const jgb_batch* hb, double* rad_out,
+                                  double* tau_out, int precision) {
+  if (!x || !hb || hb->nobs <= 0 || !rad_out) return fail(x, JGB_ERR_ARG, "bad arguments");
+  const CtlDev c = x->c;
+  const int nobs = hb->nobs, ng = c.ng, nw = c.nw, nv = ng + 1;
+  const long long nlev = hb->lev_off[nobs], nray = hb->ray_off[nobs];
+  const int nscal = 5 + c.ncl + c.nsf;
+  if ((long long)nobs * nv > 0x7fffffffLL || nlev * nv > 0x7fffffffLL || nray * nv > 0x7fffffffLL)
+    return fail(x, JGB_ERR_ARG, "batch too large");
+  const long long NL = nlev * nv, NR = nray * nv;
+  std::vector<int> lo(nobs * nv + 1, 0), ro(nobs * nv + 1, 0);
+  std::vector<double> time(NL), z(NL), lon(NL), lat(NL), p(NL), t(NL), q((size_t)ng * NL),
+      k((size_t)nw * NL), scal((size_t)nobs * nv * nscal), geo(7 * (size_t)NR),
+      rad((size_t)c.nd * NR), tau((size_t)c.nd * NR), tp(3 * (size_t)NR);
+  // variant v of observation o is batch entry v * nobs + o
+  for (int v = 0; v < nv; v++)
+    for (int o = 0; o < nobs; o++) {
+      const int e = v * nobs + o;
+      lo[e + 1] = lo[e] + (hb->lev_off[o + 1] - hb->lev_off[o]);
+      ro[e + 1] = ro[e] + (hb->ray_off[o + 1] - hb->ray_off[o]);
+    }
+  for (int v = 0; v < nv; v++) {
+    const long long l0 = v * nlev, r0 = v * nray;
+    std::memcpy(&time[l0], hb->time, sizeof(double) * nlev);
+    std::memcpy(&z[l0], hb->z, sizeof(double) * nlev);
+    std::memcpy(&lon[l0], hb->lon, sizeof(double) * nlev);
+    std::memcpy(&lat[l0], hb->lat, sizeof(double) * nlev);
+    std::memcpy(&p[l0], hb->p, sizeof(double) * nlev);
+    std::memcpy(&t[l0], hb->t, sizeof(double) * nlev);
+    for (int g = 0; g < ng; g++)
+      if (v == g) std::memcpy(&q[(size_t)g * NL + l0], hb->q + (size_t)g * nlev, sizeof(double) * nlev);
+    for (int w = 0; w < nw; w++)
+      if (v == ng) std::memcpy(&k[(size_t)w * NL + l0], hb->k + (size_t)w * nlev, sizeof(double) * nlev);
+    std::memcpy(&scal[(size_t)v * nobs * nscal], hb->scal, sizeof(double) * nobs * nscal);
+    for (int f = 0; f < 7; f++) std::memcpy(&geo[f * NR + r0], hb->geo + f * nray, sizeof(double) * nray);
+    for (int id = 0; id < c.nd; id++)
+      std::memcpy(&rad[id * NR + r0], hb->rad + id * nray, sizeof(double) * nray);
+  }
+  jgb_batch eb{};
+  eb.nobs = nobs * nv;
+  eb.lev_off = lo.data();
+  eb.time = time.data();
+  eb.z = z.data();
+  eb.lon = lon.data();
+  eb.lat = lat.data();
+  eb.p = p.data();
+  eb.t = t.data();
+  eb.q = q.data();
+  eb.k = k.data();
+  eb.scal = scal.data();
+  eb.ray_off = ro.data();
+  eb.geo = geo.data();
+  eb.rad = rad.data();
+  eb.tau = tau.data();
+  eb.tp = tp.data();
+  // continua off for these runs (formod.c:203-207)
+  x->c.ctm_co2 = x->c.ctm_h2o = x->c.ctm_n2 = x->c.ctm_o2 = 0;
+  const int rc = jgb_formod_batch(x, &eb, precision);
+  x->c = c;
+  if (rc) return rc;
+  // rad/tau are [nd][nv*nray]; reorder to [nv][nd][nray]
+  for (int v = 0; v < nv; v++)
+    for (int id = 0; id < c.nd; id++) {
+      std::memcpy(rad_out + ((size_t)v * c.nd + id) * nray, &rad[id * NR + v * nray], sizeof(double) * nray);
+      if (tau_out)
+        std::memcpy(tau_out + ((size_t)v * c.nd + id) * nray, &tau[id * NR + v * nray], sizeof(double) * nray);
+    }
+  return JGB_OK;
+}

@@ -12,6 +12,11 @@ namespace jgb {
 // jgb_fp64.cu
 void launch_trace_count(const CtlDev& c, const ChanDev& ch, const BatchDev& b, const LosDev& L,
                         unsigned* err, cudaStream_t s);
+// jgb_trace_mixed.cu: ray tracing of the mixed-precision forward model
+void launch_trace_count_mixed(const CtlDev& c, const BatchDev& b, const LosDev& L, unsigned* err,
+                              cudaStream_t s);
+void launch_trace_fill_mixed(const CtlDev& c, const BatchDev& b, const LosDev& L, unsigned* err,
+                             cudaStream_t s);
 void launch_trace_fill(const CtlDev& c, const ChanDev& ch, const BatchDev& b, const LosDev& L,
                        unsigned* err, cudaStream_t s);
 void launch_path_fp64(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,

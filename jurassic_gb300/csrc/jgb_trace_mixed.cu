@@ -1,0 +1,460 @@
+// Ray tracing for the mixed-precision forward model.
+//
+// Same algorithm, step rule, refraction scheme and clipping as raytrace
+// (jurassic.c:4201-4438, restated in FP64 in jgb_fp64.cu), with numerics
+// chosen for GB300, whose FP64 pipe is ~64x narrower than FP32:
+//  * the position x stays FP64 (three adds per step), but the altitude is
+//    carried as z (FP64) plus exact FP32 increments
+//      dz = (2 r (xhat . d) + |d|^2) / (r + sqrt(r^2 + 2 r (xhat . d) + |d|^2))
+//    (no cancellation, relative error ~1e-7 of the step), so no FP64 square
+//    roots, divisions or cart2geo per step;
+//  * atmosphere interpolation (log-linear p, linear T, q, k; intpol_atm,
+//    jurassic.c:3685-3706) runs in FP32 with per-level constants;
+//  * the refractivity finite difference of the reference,
+//    (N(xh + h e_k) - N(xh)) / h with N = 7.753e-5 p / T and h = 20 m,
+//    is evaluated without cancellation:
+//      N(z + dl) - N(z) = c p / (T T') (T expm1(s_p dl) - s_T dl)
+//    inside one level (split at a level boundary), where N itself would only
+//    carry ~7 significant digits in FP32;
+//  * longitude and latitude are computed only at the points that use them
+//    (first, last and the neighbours of the lowest point, for the tangent
+//    point and the solar geometry);
+//  * trapezoid lengths, column densities and Curtis-Godson sums in FP32
+//    (compensated sums).
+// The count and fill passes share the walk, so they agree on the point count.
+#include "jgb_common.cuh"
+#include "jgb_internal.h"
+
+namespace jgb {
+namespace {
+
+constexpr float kRefracC = 7.753e-05f;
+
+struct AtmM {
+  int np;
+  long long stride;
+  const double *z, *p, *t, *q, *k;
+  double clz, cldz, sfz, sfp, sft;
+};
+
+__device__ inline AtmM atm_m(const BatchDev& b, const CtlDev& c, int o) {
+  AtmM a;
+  const int l0 = b.lev_off[o];
+  a.np = b.lev_off[o + 1] - l0;
+  a.stride = b.nlev;
+  a.z = b.z + l0;
+  a.p = b.p + l0;
+  a.t = b.t + l0;
+  a.q = b.q + l0;
+  a.k = b.k + l0;
+  const double* s = b.scal + (long long)o * b.nscal;
+  a.clz = s[0];
+  a.cldz = s[1];
+  a.sfz = s[2 + c.ncl];
+  a.sfp = s[3 + c.ncl];
+  a.sft = s[4 + c.ncl];
+  return a;
+}
+
+// One level interval [z_i, z_i+1] of the profile in FP32 form.
+struct Lev {
+  int i;
+  double z0;        // z_i
+  float dz;         // z_i+1 - z_i
+  float p0, p1, t0, t1;
+  float sp;         // log(p1/p0)/dz (log-linear p) or (p1-p0)/dz (linear fallback)
+  float st;         // (t1-t0)/dz
+  bool plog;
+};
+
+__device__ inline void lev_load(const AtmM& a, int i, Lev& L) {
+  L.i = i;
+  L.z0 = a.z[i];
+  L.dz = (float)(a.z[i + 1] - a.z[i]);
+  L.p0 = (float)a.p[i];
+  L.p1 = (float)a.p[i + 1];
+  L.t0 = (float)a.t[i];
+  L.t1 = (float)a.t[i + 1];
+  L.plog = (a.p[i + 1] / a.p[i]) > 0;
+  L.sp = L.plog ? logf(L.p1 / L.p0) / L.dz : (L.p1 - L.p0) / L.dz;
+  L.st = (L.t1 - L.t0) / L.dz;
+}
+
+// Interval of z (locate_irr semantics: 0 below, np-2 above the grid) with
+// the cached interval as hint.
+__device__ inline void lev_find(const AtmM& a, double z, Lev& L) {
+  const int i = L.i;
+  if (i >= 0) {
+    const bool in = a.z[i] <= z && z < a.z[i + 1];
+    const bool below = i == 0 && z < a.z[0];
+    const bool above = i == a.np - 2 && z >= a.z[a.np - 1];
+    if (in || below || above) return;
+  }
+  lev_load(a, bracket_irr(a.z, a.np, z), L);
+}
+
+__device__ inline void lev_pt(const Lev& L, double z, float* p, float* t) {
+  const float dl = (float)(z - L.z0);
+  *p = L.plog ? L.p0 * expf(L.sp * dl) : L.p0 + L.sp * dl;
+  *t = L.t0 + L.st * dl;
+}
+
+// N(z + dl) - N(z) inside one level, from p, T at z (no cancellation).
+__device__ inline float dN_in(const Lev& L, float p, float t, float dl) {
+  const float t2 = t + L.st * dl;
+  if (L.plog) return kRefracC * p / (t * t2) * (t * expm1f(L.sp * dl) - L.st * dl);
+  return kRefracC * dl * (L.sp * t - p * L.st) / (t * t2);
+}
+
+// Altitude increment of a displacement d from a point at radius r with
+// radial unit vector xh.
+__device__ inline float dz_of(const float* xh, float r, const float* d) {
+  const float u = xh[0] * d[0] + xh[1] * d[1] + xh[2] * d[2];
+  const float dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+  const float num = 2.f * r * u + dd;
+  return num / (r + sqrtf(r * r + num));
+}
+
+// Lon/lat bookkeeping of the fill pass.
+struct GeoKeep {
+  double x_first[3], x_prev[3], x_m1[3], x_p1[3], x_last[3];
+  double zmin_seen;
+  int imin;
+  bool want_p1;
+};
+
+template <bool STORE>
+__device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long nray, int r,
+                      const LosDev& L, long long base, int cap, double* sft_out, GeoKeep* gk,
+                      unsigned* err) {
+  const float h = 0.02f;
+  const double zrefrac = 60;
+  *sft_out = -999;
+  const double obsz = g[1 * nray + r], obslon = g[2 * nray + r], obslat = g[3 * nray + r];
+  const double vpz = g[4 * nray + r], vplon = g[5 * nray + r], vplat = g[6 * nray + r];
+  double zmin = a.z[0], zmax = a.z[0];
+  for (int i = 0; i < a.np; i++) {
+    zmin = a.z[i] < zmin ? a.z[i] : zmin;
+    zmax = a.z[i] > zmax ? a.z[i] : zmax;
+  }
+  if (c.nsf > 0) {
+    zmin = a.sfz > zmin ? a.sfz : zmin;
+    if (a.sfp > 0) {
+      const int i = bracket_irr(a.p, a.np, a.sfp);
+      const double zs = lin(log(a.p[i]), a.z[i], log(a.p[i + 1]), a.z[i + 1], log(a.sfp));
+      zmin = zs > zmin ? zs : zmin;
+    }
+  }
+  if (obsz < zmin) {
+    atomicOr(err, kErrObserverBelowSurface);
+    return -1;
+  }
+  if (vpz > zmax) return 0;
+
+  double x[3], xobs[3], xvp[3];
+  to_cart(obsz, obslon, obslat, xobs);
+  to_cart(vpz, vplon, vplat, xvp);
+  // the direction stays FP64: renormalising an FP32 unit vector every step
+  // would random-walk it by ~1e-7 rad per step (metres over a limb path)
+  double ex0[3];
+  for (int i = 0; i < 3; i++) ex0[i] = xvp[i] - xobs[i];
+  const double norm = sqrt(ex0[0] * ex0[0] + ex0[1] * ex0[1] + ex0[2] * ex0[2]);
+  for (int i = 0; i < 3; i++) {
+    ex0[i] /= norm;
+    x[i] = xobs[i];
+  }
+  double z = obsz;
+  if (obsz > zmax) {  // entry into the atmosphere: bisection on the line of sight (FP64, once)
+    double dmax = norm, dmin = 0;
+    for (int guard = 0; fabs(dmin - dmax) > 0.001 && guard < 200; guard++) {
+      const double d = (dmax + dmin) / 2;
+      for (int i = 0; i < 3; i++) x[i] = xobs[i] + d * ex0[i];
+      z = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]) - kRE;
+      if (z <= zmax && z > zmax - 0.001) break;
+      if (z < zmax - 0.0005) dmax = d; else dmin = d;
+    }
+  }
+  z = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]) - kRE;
+
+  Lev lv;
+  lv.i = -1;
+  int n = 0, stop = 0;
+  double last_z = 0, x_last[3] = {0, 0, 0};
+  const float rayds = (float)c.rayds, raydz = (float)c.raydz;
+  for (;;) {
+    // radial unit vector and radius at x
+    const double rr = z + kRE;
+    const float rf = (float)rr, rinv = 1.f / rf;
+    float xh[3] = {(float)x[0] * rinv, (float)x[1] * rinv, (float)x[2] * rinv};
+    const float ef[3] = {(float)ex0[0], (float)ex0[1], (float)ex0[2]};
+    // step length from this point (jurassic.c:4278-4287)
+    float step = rayds;
+    if (raydz > 0) {
+      const float cosa = fabsf(ef[0] * xh[0] + ef[1] * xh[1] + ef[2] * xh[2]);
+      if (cosa != 0) step = rayds < raydz / cosa ? rayds : raydz / cosa;
+    }
+    // ground or top of the atmosphere: clip the last segment (4292-4306;
+    // the previous point's step becomes this point's step times frac)
+    if ((z < zmin || z > zmax) && n > 0) {
+      if (!STORE) {
+        if (n >= cap) {
+          atomicOr(err, kErrLosOverflow);
+          return -1;
+        }
+        return n + 1;
+      }
+      stop = (z < zmin ? 2 : 1);
+      const double frac = ((z < zmin ? zmin : zmax) - last_z) / (z - last_z);
+      for (int i = 0; i < 3; i++) x[i] = x_last[i] + frac * (x[i] - x_last[i]);
+      z = last_z + frac * (z - last_z);
+      L.ds[base + n - 1] = (double)step * frac;
+      step = 0.f;
+    }
+    if (n >= cap) {
+      atomicOr(err, kErrLosOverflow);
+      return -1;
+    }
+    lev_find(a, z, lv);
+    float p, t;
+    lev_pt(lv, z, &p, &t);
+    if (STORE) {
+      const long long s = base + n;
+      L.z[s] = z;
+      L.p[s] = p;
+      L.t[s] = t;
+      L.ds[s] = step;
+      const int i = lv.i;
+      const float dl = (float)(z - lv.z0);
+      for (int ig = 0; ig < c.ng; ig++) {
+        const float q0 = (float)a.q[ig * a.stride + i], q1 = (float)a.q[ig * a.stride + i + 1];
+        L.u[ig * L.cap + s] = q0 + (q1 - q0) / lv.dz * dl;
+      }
+      if (c.ig_h2o >= 0) L.qh2o[s] = L.u[c.ig_h2o * L.cap + s];
+      for (int iw = 0; iw < c.nw; iw++) {
+        const float k0 = (float)a.k[iw * a.stride + i], k1 = (float)a.k[iw * a.stride + i + 1];
+        L.kw[iw * L.cap + s] = k0 + (k1 - k0) / lv.dz * dl;
+      }
+      if (c.ncl > 0 && a.cldz > 0) {
+        const float v = (float)((z - a.clz) / a.cldz);
+        L.aux[s] = expf(-0.5f * v * v);
+      } else {
+        L.aux[s] = 0.0;
+      }
+      // geometry kept for lon/lat of the points that need them
+      if (n == 0)
+        for (int i2 = 0; i2 < 3; i2++) gk->x_first[i2] = x[i2];
+      if (gk->want_p1) {
+        for (int i2 = 0; i2 < 3; i2++) gk->x_p1[i2] = x[i2];
+        gk->want_p1 = false;
+      }
+      if (n == 0 || z < gk->zmin_seen) {
+        gk->zmin_seen = z;
+        gk->imin = n;
+        for (int i2 = 0; i2 < 3; i2++) gk->x_m1[i2] = gk->x_prev[i2];
+        gk->want_p1 = true;
+      }
+      for (int i2 = 0; i2 < 3; i2++) gk->x_prev[i2] = x[i2];
+      for (int i2 = 0; i2 < 3; i2++) gk->x_last[i2] = x[i2];
+    }
+    last_z = z;
+    for (int i2 = 0; i2 < 3; i2++) x_last[i2] = x[i2];
+    n++;
+    if (stop) {
+      if (c.nsf > 0 && a.sft > 0) t = (float)a.sft;
+      *sft_out = (stop == 2 ? (c.nsf > 0 && a.sft > 0 ? a.sft : (double)t) : -999);
+      break;
+    }
+    // refraction (jurassic.c:4388-4415): ex1 = (n ex0 + ds grad N) / |...|
+    // = (ex0 + inc) / |ex0 + inc| with inc = ds grad N / n, the increment in
+    // FP32 and the renormalisation as a series in delta = |ex0 + inc|^2 - 1
+    const bool bend = c.refrac && z <= zrefrac;
+    double ex1[3] = {ex0[0], ex0[1], ex0[2]};
+    if (bend) {
+      const float nref = 1.f + kRefracC * p / t;
+      // midpoint xh = x + ds/2 ex0 and its radial unit vector
+      const float d[3] = {0.5f * step * ef[0], 0.5f * step * ef[1], 0.5f * step * ef[2]};
+      const float dzh = dz_of(xh, rf, d);
+      const double zh = z + dzh;
+      const float rh = rf + dzh, rhinv = 1.f / rh;
+      const float xhh[3] = {(xh[0] * rf + d[0]) * rhinv, (xh[1] * rf + d[1]) * rhinv,
+                            (xh[2] * rf + d[2]) * rhinv};
+      Lev lh = lv;
+      lev_find(a, zh, lh);
+      float ph, th;
+      lev_pt(lh, zh, &ph, &th);
+      float inc[3];
+      for (int k = 0; k < 3; k++) {
+        float dk[3] = {0.f, 0.f, 0.f};
+        dk[k] = h;
+        const float dl = dz_of(xhh, rh, dk);
+        const double zk = zh + dl;
+        float dN;
+        Lev lk = lh;
+        lev_find(a, zk, lk);
+        if (lk.i == lh.i) {
+          dN = dN_in(lh, ph, th, (float)(zk - zh));
+        } else {
+          // split at the level boundary between zh and zk
+          const bool up = lk.i > lh.i;
+          const double zb = up ? a.z[lh.i + 1] : a.z[lh.i];
+          const float d1 = (float)(zb - zh), d2 = (float)(zk - zb);
+          const float dn1 = dN_in(lh, ph, th, d1);
+          float pb, tb;
+          lev_pt(lk, zb, &pb, &tb);
+          dN = dn1 + dN_in(lk, pb, tb, d2);
+        }
+        inc[k] = step * (dN / h) / nref;
+      }
+      const float delta = 2.f * (ef[0] * inc[0] + ef[1] * inc[1] + ef[2] * inc[2]) +
+                          (inc[0] * inc[0] + inc[1] * inc[1] + inc[2] * inc[2]);
+      for (int k = 0; k < 3; k++) ex1[k] = ex0[k] + (double)inc[k];
+      if (fabsf(delta) < 1e-3f) {
+        const float corr = delta * (-0.5f + delta * (0.375f - 0.3125f * delta));
+        for (int k = 0; k < 3; k++) ex1[k] += ex1[k] * (double)corr;
+      } else {
+        const double nn = sqrt(ex1[0] * ex1[0] + ex1[1] * ex1[1] + ex1[2] * ex1[2]);
+        for (int k = 0; k < 3; k++) ex1[k] /= nn;
+      }
+    }
+    float D[3];
+    for (int k = 0; k < 3; k++) D[k] = 0.5f * step * (ef[k] + (float)ex1[k]);
+    const float dzs = dz_of(xh, rf, D);
+    for (int k = 0; k < 3; k++) {
+      x[k] += (double)D[k];
+      ex0[k] = ex1[k];
+    }
+    z += dzs;
+  }
+  return n;
+}
+
+__global__ void k_trace_count_m(CtlDev c, BatchDev b, LosDev L, unsigned* err) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= b.nray) return;
+  if (b.obs_skip && b.obs_skip[b.ray_obs[r]]) {
+    L.count[r] = 0;
+    return;
+  }
+  const AtmM a = atm_m(b, c, b.ray_obs[r]);
+  double sft;
+  const int n = walk_m<false>(c, a, b.geo, b.nray, r, L, 0, c.nlos_max, &sft, nullptr, err);
+  L.count[r] = n < 0 ? 0 : n;
+}
+
+__global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, unsigned* err) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= b.nray) return;
+  if (b.obs_skip && b.obs_skip[b.ray_obs[r]]) return;
+  const AtmM a = atm_m(b, c, b.ray_obs[r]);
+  const long long base = L.off[r];
+  const int cap = L.count[r];
+  double sft;
+  GeoKeep gk;
+  gk.want_p1 = false;
+  gk.imin = 0;
+  gk.zmin_seen = 0;
+  for (int i = 0; i < 3; i++) gk.x_prev[i] = gk.x_m1[i] = gk.x_p1[i] = gk.x_first[i] = gk.x_last[i] = 0;
+  const int n = walk_m<true>(c, a, b.geo, b.nray, r, L, base, cap, &sft, &gk, err);
+  L.sft[r] = sft;
+  if (n > 0) L.count[r] = n;
+  const long long nr = b.nray;
+  double* tp = b.tp;
+  // tangent point defaults to the view point (jurassic.c:4218-4220)
+  tp[0 * nr + r] = b.geo[4 * nr + r];
+  tp[1 * nr + r] = b.geo[5 * nr + r];
+  tp[2 * nr + r] = b.geo[6 * nr + r];
+  if (n <= 0) {
+    L.count[r] = 0;
+    return;
+  }
+  const double* z = L.z + base;
+  double* ds = L.ds + base;
+  double dummy, lon0, lat0, lonl, latl;
+  to_geo(gk.x_first, &dummy, &lon0, &lat0);
+  to_geo(gk.x_last, &dummy, &lonl, &latl);
+  // tangent point (tangent_point, jurassic.c:5223-5263), before trapezoid
+  const int imin = gk.imin;
+  if (imin <= 0 || imin >= n - 1) {
+    tp[0 * nr + r] = z[n - 1];
+    tp[1 * nr + r] = lonl;
+    tp[2 * nr + r] = latl;
+  } else {
+    const double y0 = z[imin - 1], y1 = z[imin], y2 = z[imin + 1];
+    const double x1 = sqrt(ds[imin] * ds[imin] - (y1 - y0) * (y1 - y0));
+    const double x2 = x1 + sqrt(ds[imin + 1] * ds[imin + 1] - (y2 - y1) * (y2 - y1));
+    const double aa = 1 / (x1 - x2) * (-(y0 - y1) / x1 + (y0 - y2) / x2);
+    const double bb = -(y0 - y1) / x1 - aa * x1;
+    const double cc = y0;
+    const double xt = -bb / (2 * aa);
+    tp[0 * nr + r] = aa * xt * xt + bb * xt + cc;
+    double v[3], tlon, tlat;
+    for (int i = 0; i < 3; i++) v[i] = lin(0.0, gk.x_m1[i], x2, gk.x_p1[i], xt);
+    to_geo(v, &dummy, &tlon, &tlat);
+    tp[1 * nr + r] = tlon;
+    tp[2 * nr + r] = tlat;
+  }
+  double* e = L.ends + 6LL * r;
+  e[0] = z[0];
+  e[1] = lon0;
+  e[2] = lat0;
+  e[3] = z[n - 1];
+  e[4] = lonl;
+  e[5] = latl;
+  // trapezoid segment lengths
+  float prev = (float)ds[0];
+  ds[0] = 0.5f * prev;
+  for (int ip = 1; ip < n; ip++) {
+    const float cur = (float)ds[ip];
+    ds[ip] = 0.5f * (prev + cur);
+    prev = cur;
+  }
+  // column densities (q stored in the u plane) and Curtis-Godson means
+  const double* p = L.p + base;
+  const double* t = L.t + base;
+  const float c10kb = (float)(10.0 / kKB);
+  for (int ig = 0; ig < c.ng; ig++) {
+    double* u = L.u + ig * L.cap + base;
+    double* cgu = L.cga ? L.cgu + ig * L.cap + base : nullptr;
+    double* cgp = L.cga ? L.cgp + ig * L.cap + base : nullptr;
+    double* cgt = L.cga ? L.cgt + ig * L.cap + base : nullptr;
+    float su = 0.f, sp = 0.f, st = 0.f, cu = 0.f, cp = 0.f, ct = 0.f;
+    for (int ip = 0; ip < n; ip++) {
+      const float pf = (float)p[ip], tf = (float)t[ip];
+      const float uu = c10kb * (float)u[ip] * pf / tf * (float)ds[ip];
+      u[ip] = uu;
+      if (cgu) {
+        // compensated running sums
+        float y = uu - cu, s2 = su + y;
+        cu = (s2 - su) - y;
+        su = s2;
+        y = uu * pf - cp;
+        s2 = sp + y;
+        cp = (s2 - sp) - y;
+        sp = s2;
+        y = uu * tf - ct;
+        s2 = st + y;
+        ct = (s2 - st) - y;
+        st = s2;
+        cgu[ip] = su;
+        cgp[ip] = sp / su;
+        cgt[ip] = st / su;
+      }
+    }
+  }
+}
+
+}  // namespace
+
+void launch_trace_count_mixed(const CtlDev& c, const BatchDev& b, const LosDev& L, unsigned* err,
+                              cudaStream_t s) {
+  const int bs = 64;
+  k_trace_count_m<<<(b.nray + bs - 1) / bs, bs, 0, s>>>(c, b, L, err);
+}
+
+void launch_trace_fill_mixed(const CtlDev& c, const BatchDev& b, const LosDev& L, unsigned* err,
+                             cudaStream_t s) {
+  const int bs = 64;
+  k_trace_fill_m<<<(b.nray + bs - 1) / bs, bs, 0, s>>>(c, b, L, err);
+}
+
+}  // namespace jgb

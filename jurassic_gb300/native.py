@@ -119,6 +119,7 @@ SIGNATURES = {
     "jgb_kernel_batch": (C.c_int, [C.c_void_p, C.POINTER(_Batch), _dp, C.c_int]),
     "jgb_normal_equations": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _dp, _dp, _dp, _dp, _dp,
                                        C.c_int]),
+    "jgb_formod_contrib": (C.c_int, [C.c_void_p, C.POINTER(_Batch), _dp, _dp, C.c_int]),
     "jgb_retrieve_batch": (C.c_int, [C.c_void_p, C.POINTER(_Ret), C.POINTER(_Batch), _dp, _dp,
                                      _dp, _ip, C.c_int]),
     "jgb_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
@@ -359,6 +360,19 @@ class Context:
             oa += ni * ni
             ob += ni
         return outA, outb
+
+    def contributions(self, batch, precision: int = FP64):
+        """Emitter contributions (TASK c, src/formod.c:200-249): continua off,
+        one forward model per emitter with only that emitter's mixing ratio
+        (no extinction), then one with the extinction only.  ``batch`` holds
+        the atmosphere as after formod.  Returns (rad, tau) of shape
+        [ng+1, nd, nray]; entry ng is "EXTINCT"."""
+        ctl = self.ctl
+        s, arr, keep = self._batch_struct(batch)
+        rad = np.zeros((ctl.ng + 1, ctl.nd, batch.nray))
+        tau = np.zeros_like(rad)
+        self._check(load().jgb_formod_contrib(self.h, C.byref(s), _p(rad), _p(tau), precision))
+        return rad, tau
 
     def _ret_struct(self, ret):
         r = ret.sized(self.ctl)

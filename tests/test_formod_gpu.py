@@ -4,7 +4,8 @@ the reference formod, pinned bit-exact to the reference build).
 FP64 path: relative radiance error <= 1e-9 (rounding-level; CUDA's libm and
            the host libm differ in the last bits).
 Mixed path: |BT_gpu - BT_oracle| <= 10 mK per (ray, channel), BT from the
-           reference's BRIGHT formula in FP64.
+           reference's BRIGHT formula in FP64; tangent point within 2 m and
+           1e-4 degrees (mixed ray tracing).
 """
 import copy
 
@@ -40,7 +41,13 @@ def _check(ctl, ref, out, precision, what=""):
         assert dbt <= BT_TOL_K, "%s mixed |dBT| %.4f K" % (what, dbt)
         assert np.max(np.abs(out.tau - tau_ref)) <= 2e-4, what
     tp = np.stack([out.tpz, out.tplon, out.tplat])
-    assert np.max(np.abs(tp - tp_ref)) <= 1e-8, what
+    if precision == native.FP64:
+        assert np.max(np.abs(tp - tp_ref)) <= 1e-8, what
+    else:
+        # mixed ray tracing: FP32 altitude increments and atmosphere, FP64
+        # position; tangent altitude within 2 m, longitude/latitude 1e-4 deg
+        assert np.max(np.abs(tp[0] - tp_ref[0])) <= 2e-3, what
+        assert np.max(np.abs(tp[1:] - tp_ref[1:])) <= 1e-4, what
 
 
 def _run_single(w, ctl=None, precisions=(native.FP64, native.MIXED), atm_mod=None, obs_mod=None):
@@ -182,3 +189,37 @@ def test_limb_cga_batch_uneven(built_lib, built_oracle):
     out = ctx.formod_batch(w.batch.fresh_outputs(), native.MIXED)
     dbt = np.max(np.abs(_bt(ctl, out.rad) - _bt(ctl, ref.rad)))
     assert dbt <= BT_TOL_K, dbt
+
+
+def test_contributions_task_c(built_lib, built_oracle):
+    """TASK c (formod.c:200-249): per-emitter and extinction-only forward
+    models with the continua off, against the oracle run on the same
+    modified atmospheres."""
+    from oracle import oracle
+    w = synth.config_limb_ega()
+    ctl = w.ctl
+    atm, obs = w.batch.item(ctl, 0)
+    atm.k = np.where(atm.z < 20.0, 1e-3, 0.0)[None, :] * np.ones((ctl.nw, 1))
+    batch = synth.pack(ctl, [(atm, obs)])
+    ctl_off = copy.deepcopy(ctl)
+    ctl_off.ctm_co2 = ctl_off.ctm_h2o = ctl_off.ctm_n2 = ctl_off.ctm_o2 = 0
+    ora = oracle.Oracle(ctl_off, w.tables, w.filters)
+    refs = []
+    for v in range(ctl.ng + 1):
+        a2 = atm.copy()
+        a2.k = np.zeros_like(a2.k) if v < ctl.ng else a2.k
+        a2.q = np.array([a2.q[g] if g == v else np.zeros_like(a2.q[g]) for g in range(ctl.ng)])
+        refs.append(ora.formod(a2, obs))
+    ctx = native.Context(ctl, w.tables, w.filters)
+    for prec in (native.FP64, native.MIXED):
+        rad, tau = ctx.contributions(batch, prec)
+        for v in range(ctl.ng + 1):
+            r_ref, t_ref = refs[v][0], refs[v][1]
+            if prec == native.FP64:
+                assert np.max(np.abs(rad[v] - r_ref) / np.abs(r_ref)) <= FP64_RTOL, v
+                assert np.max(np.abs(tau[v] - t_ref)) <= 1e-10, v
+            else:
+                assert np.max(np.abs(_bt(ctl, rad[v]) - _bt(ctl, r_ref))) <= BT_TOL_K, v
+        # the context's own continua are back on afterwards
+        out = ctx.formod(atm.copy(), obs, native.FP64)
+        assert np.allclose(out.rad, ctx.formod(atm.copy(), obs, native.FP64).rad)
