@@ -109,6 +109,14 @@ int jgb_set_table(jgb_ctx *ctx, int id, int ig, int np, const double *p, const i
                   const double *t, const int *nu, const float *u, const float *eps,
                   int tt_cap, int tu_cap);
 
+/* Field of view (formod_fov, jurassic.c:3121-3192; FOV control parameter,
+   read_shape of the FOV file): n samples of altitude offset dz [km] and
+   weight w.  Every forward model of the context then convolves the pencil
+   beams of the rays within +-5 of each ray (same observation, same time)
+   over view-point altitude before BT conversion and masking.  n = 0 turns it
+   off.  Not available in jgb_formod_batch_dev_noalloc. */
+int jgb_set_fov(jgb_ctx *ctx, int n, const double *dz, const double *w);
+
 /* Source function of channel id from its filter function
    (init_srcfunc, jurassic.c:3631-3681), computed on the device. */
 int jgb_set_filter(jgb_ctx *ctx, int id, int n, const double *fnu, const double *f);

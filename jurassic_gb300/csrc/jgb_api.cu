@@ -259,6 +259,13 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
   CK(cudaGetLastError());
   CK(cudaEventRecord(x->ev[3], s));
 
+  // with a field of view the path kernels write pencil beams to scratch
+  BatchDev bo = b;
+  if (c.fov) {
+    CK(x->fov_raw.reserve(sizeof(double) * 2 * (size_t)c.nd * nray));
+    bo.rad = x->fov_raw.as<double>();
+    bo.tau = bo.rad + (size_t)c.nd * nray;
+  }
   // reflection needs per-point source and emissivity per channel
   const bool need_refl = c.sftype >= 2 && c.nsf > 0;
   TblDev T = tbl_view(x);
@@ -270,7 +277,7 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
       refl = x->refl.as<double>();
     }
     CK(cudaEventRecord(x->ev[4], s));
-    launch_path_fp64(c, T, ch, b, L, refl, s);
+    launch_path_fp64(c, T, ch, bo, L, refl, s);
     launches += 1;
   } else {
     if (x->srf_stale) {
@@ -357,7 +364,7 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
         x->tune_ms.clear();
         for (int v = 0; v < path_mixed_variants(); v++) {
           CK(cudaEventRecord(x->ev[4], s));
-          launch_path_mixed(c, T, ch, b, L, Pm, refl, v, s);
+          launch_path_mixed(c, T, ch, bo, L, Pm, refl, v, s);
           CK(cudaEventRecord(x->ev[5], s));
           CK(cudaEventSynchronize(x->ev[5]));
           const float ms = elapsed(x->ev[4], x->ev[5]);
@@ -370,10 +377,18 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
       }
     }
     CK(cudaEventRecord(x->ev[4], s));
-    launch_path_mixed(c, T, ch, b, L, Pm, refl, x->path_variant, s);
+    launch_path_mixed(c, T, ch, bo, L, Pm, refl, x->path_variant, s);
     launches += 6;
   }
   CK(cudaGetLastError());
+  if (c.fov) {
+    const double* fd = x->d_fov.as<double>();
+    launch_fov(c, b, bo.rad, bo.tau, x->nfov, fd, fd + x->nfov, ch.nu, d_err, s);
+    launches += 1;
+    CK(cudaMemcpyAsync(&h_err, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (h_err & kErrFov) return fail(x, JGB_ERR_ARG, "Cannot apply FOV convolution!");
+  }
   CK(cudaEventRecord(x->ev[5], s));
   x->stats.los_points = total;
   x->stats.path_launches = launches;
@@ -934,6 +949,20 @@ int jgb_set_table(jgb_ctx* x, int id, int ig, int np, const double* p, const int
                     eps + (size_t)ip * tt_cap * tu_cap, sizeof(float) * tu_cap,
                     sizeof(float) * w, ntt, cudaMemcpyHostToDevice));
   }
+  return JGB_OK;
+}
+
+int jgb_set_fov(jgb_ctx* x, int n, const double* dz, const double* w) {
+  if (!x || n < 0 || (n > 0 && (!dz || !w))) return fail(x, JGB_ERR_ARG, "bad field of view");
+  if (n == 1) return fail(x, JGB_ERR_ARG, "Could not read any data!");  // read_shape needs >= 2
+  if (n > 20000) return fail(x, JGB_ERR_ARG, "Too many data points!");  // NSHAPE
+  cudaSetDevice(x->device);
+  x->nfov = n;
+  x->c.fov = n > 0;
+  if (n == 0) return JGB_OK;
+  CK(x->d_fov.reserve(sizeof(double) * 2 * n));
+  CK(cudaMemcpy(x->d_fov.as<double>(), dz, sizeof(double) * n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(x->d_fov.as<double>() + n, w, sizeof(double) * n, cudaMemcpyHostToDevice));
   return JGB_OK;
 }
 

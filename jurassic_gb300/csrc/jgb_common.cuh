@@ -32,6 +32,7 @@ enum : unsigned {
   kErrLosOverflow = 1u,
   kErrObserverBelowSurface = 2u,
   kErrBadInput = 4u,
+  kErrFov = 8u,
 };
 
 // ---------------------------------------------------------------------------
@@ -121,6 +122,7 @@ struct CtlDev {
   double rayds, raydz;
   int ig_co2, ig_h2o;
   int nlos_max;
+  int fov;   // field-of-view convolution on: path kernels write pencil values only
 };
 
 // Emissivity tables, dense with capacities tp x tt x tu per (channel, emitter).

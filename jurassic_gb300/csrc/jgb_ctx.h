@@ -58,6 +58,9 @@ struct jgb_ctx {
   std::vector<int> h_nt;
   std::vector<float> h_pf, h_tf;
   unsigned grid_mask = 0;
+  // field of view: nfov samples (dz, w) on the device, pencil-beam scratch
+  int nfov = 0;
+  jgb::DevBuf d_fov, fov_raw;
   jgb::DevBuf t_np, t_p, t_nt, t_t, t_nu, t_u, t_eps, t_pf, t_tf, t_meta;
   bool meta_stale = true;
   // source function

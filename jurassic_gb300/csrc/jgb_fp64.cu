@@ -567,8 +567,13 @@ __global__ void k_path_fp64(CtlDev c, TblDev T, ChanDev ch, BatchDev b, LosDev L
       }
     }
   }
-  if (c.write_bbt) rad = kC2 * nu / log1p(kC1 * (nu * nu * nu) / rad);
   const long long oi = (long long)id * nray + r;
+  if (c.fov) {  // pencil beam only: FOV convolution, BT and mask follow in k_fov
+    b.rad[oi] = rad;
+    b.tau[oi] = tau;
+    return;
+  }
+  if (c.write_bbt) rad = kC2 * nu / log1p(kC1 * (nu * nu * nu) / rad);
   b.rad[oi] = b.mask[oi] ? __longlong_as_double(0x7ff8000000000000LL) : rad;
   b.tau[oi] = tau;
 }
@@ -662,6 +667,62 @@ void launch_srcfunc(int nd, int id0, int nch, const int* fn_off, const double* f
                     const double* f, const double* st, double* sr, cudaStream_t s) {
   const int nth = kNS * nch, bs = 128;
   k_srcfunc<<<(nth + bs - 1) / bs, bs, 0, s>>>(nd, id0, nch, fn_off, fnu, f, st, sr);
+}
+
+// formod_fov (jurassic.c:3121-3192), then BRIGHT and the mask of formod
+// (3057-3067): one thread per (ray, channel) reads the pencil beams of the
+// rays within +-5 of its own in the same observation with the same time.
+__global__ void k_fov(CtlDev c, BatchDev b, const double* prad, const double* ptau, int nfov,
+                      const double* fdz, const double* fw, const double* nu, unsigned* err) {
+  const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nray = b.nray;
+  if (gid >= nray * c.nd) return;
+  const int id = (int)(gid / nray);
+  const int r = (int)(gid % nray);
+  const int o = b.ray_obs[r];
+  if (b.obs_skip && b.obs_skip[o]) return;
+  const double* time = b.geo;
+  const double* vpz = b.geo + 4 * nray;
+  double zz[11];
+  int ray[11], nz = 0;
+  const int lo = r - 5 > 0 ? r - 5 : 0;
+  const int hi = r + 6 < nray ? r + 6 : (int)nray;
+  for (int r2 = lo; r2 < hi; r2++)
+    if (b.ray_obs[r2] == o && time[r2] == time[r]) {
+      zz[nz] = vpz[r2];
+      ray[nz++] = r2;
+    }
+  if (nz < 2) {
+    atomicOr(err, kErrFov);
+    return;
+  }
+  const double* pr = prad + (long long)id * nray;
+  const double* pt = ptau + (long long)id * nray;
+  double rs = 0, ts = 0, wsum = 0;
+  for (int i = 0; i < nfov; i++) {
+    const double zf = vpz[r] + fdz[i];
+    const int k = bracket_irr(zz, nz, zf);
+    rs += fw[i] * lin(zz[k], pr[ray[k]], zz[k + 1], pr[ray[k + 1]], zf);
+    ts += fw[i] * lin(zz[k], pt[ray[k]], zz[k + 1], pt[ray[k + 1]], zf);
+    wsum += fw[i];
+  }
+  rs /= wsum;
+  ts /= wsum;
+  if (c.write_bbt) {
+    const double v = nu[id];
+    rs = kC2 * v / log1p(kC1 * (v * v * v) / rs);
+  }
+  const long long oi = (long long)id * nray + r;
+  b.rad[oi] = b.mask[oi] ? __longlong_as_double(0x7ff8000000000000LL) : rs;
+  b.tau[oi] = ts;
+}
+
+void launch_fov(const CtlDev& c, const BatchDev& b, const double* prad, const double* ptau,
+                int nfov, const double* fdz, const double* fw, const double* nu, unsigned* err,
+                cudaStream_t s) {
+  const long long nth = (long long)b.nray * c.nd;
+  const int bs = 128;
+  k_fov<<<(unsigned)((nth + bs - 1) / bs), bs, 0, s>>>(c, b, prad, ptau, nfov, fdz, fw, nu, err);
 }
 
 void launch_hydrostatic(const CtlDev& c, const BatchDev& b, double* p_out, cudaStream_t s) {

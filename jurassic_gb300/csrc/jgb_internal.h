@@ -12,6 +12,10 @@ namespace jgb {
 // jgb_fp64.cu
 void launch_trace_count(const CtlDev& c, const ChanDev& ch, const BatchDev& b, const LosDev& L,
                         unsigned* err, cudaStream_t s);
+// jgb_fp64.cu: field-of-view convolution + BT + mask of pencil-beam results
+void launch_fov(const CtlDev& c, const BatchDev& b, const double* prad, const double* ptau,
+                int nfov, const double* fdz, const double* fw, const double* nu, unsigned* err,
+                cudaStream_t s);
 // jgb_trace_mixed.cu: ray tracing of the mixed-precision forward model
 void launch_trace_count_mixed(const CtlDev& c, const BatchDev& b, const LosDev& L, unsigned* err,
                               cudaStream_t s);

@@ -556,8 +556,13 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
       }
     }
   }
-  if (c.write_bbt) radd = kC2 * nud / log1p(kC1 * (nud * nud * nud) / radd);
   const long long oi = (long long)id * b.nray + r;
+  if (c.fov) {  // pencil beam only: FOV convolution, BT and mask follow in k_fov
+    b.rad[oi] = radd;
+    b.tau[oi] = (double)tau;
+    return;
+  }
+  if (c.write_bbt) radd = kC2 * nud / log1p(kC1 * (nud * nud * nud) / radd);
   b.rad[oi] = b.mask[oi] ? __longlong_as_double(0x7ff8000000000000LL) : radd;
   b.tau[oi] = (double)tau;
 }

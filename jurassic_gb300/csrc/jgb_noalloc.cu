@@ -111,6 +111,7 @@ extern "C" int jgb_formod_batch_dev_noalloc(jgb_ctx* x, const jgb_batch* db) {
   if (scratch_address(v.device, &base) != JGB_OK)
     return ctx_fail(x, JGB_ERR_CUDA, "cannot resolve the device address of the scratch array");
   const CtlDev& c = v.c;
+  if (c.fov) return ctx_fail(x, JGB_ERR_UNSUPPORTED, "field of view not available without allocation");
   cudaStream_t s = v.stream;
   const int nobs = db->nobs;
   int nlev = 0, nray = 0;

@@ -109,6 +109,7 @@ SIGNATURES = {
     "jgb_set_table": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _ip, _dp, _ip, _fp,
                                 _fp, C.c_int, C.c_int]),
     "jgb_set_filter": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp]),
+    "jgb_set_fov": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp]),
     "jgb_set_srcfunc": (C.c_int, [C.c_void_p, _dp]),
     "jgb_get_srcfunc": (C.c_int, [C.c_void_p, _dp, _dp]),
     "jgb_formod": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
@@ -171,7 +172,7 @@ class Context:
     """One device context: control set, tables and source function."""
 
     def __init__(self, ctl: Ctl, tables=None, filters=None, device: int = 0,
-                 nlos_max: int = 4096, srcfunc: Optional[np.ndarray] = None):
+                 nlos_max: int = 4096, srcfunc: Optional[np.ndarray] = None, fov=None):
         L = load()
         self.ctl = ctl
         self._keep = dict(
@@ -203,6 +204,15 @@ class Context:
             self.set_srcfunc(srcfunc)
         elif filters is not None:
             self.set_filters(filters)
+        if fov is not None:
+            self.set_fov(*fov)
+
+    def set_fov(self, dz, w):
+        """Field of view (formod_fov): shape samples dz [km], w (read_shape
+        of the file named by the FOV control parameter); empty arrays turn it
+        off."""
+        dz, w = _d(dz), _d(w)
+        self._check(load().jgb_set_fov(self.h, len(dz), _p(dz), _p(w)))
 
     def _check(self, rc):
         if rc != JGB_OK:

@@ -85,6 +85,120 @@ def write_tbl(ctl: Ctl, tbl: Tables) -> None:
                                     tbl.u[id, ig, ip, it, iu], tbl.eps[id, ig, ip, it, iu]))
 
 
+UMIN, UMAX, EPSMIN, EPSMAX = 0.0, 1e30, 0.0, 1.0   # jurassic.h:264-339
+
+
+def _read_ascii_table(fn, tp, tt, tu):
+    """One ASCII table (read_tbl TBLFMT=1, src/jurassic.c:4991-5047): lines
+    ``p T u eps``; points outside [UMIN, UMAX] x [EPSMIN, EPSMAX] are skipped;
+    a new pressure or temperature opens a new block; within a block a point
+    is appended only if both u and eps exceed the last appended point,
+    otherwise it overwrites that point."""
+    p = np.zeros(tp)
+    nt = np.zeros(tp, np.int32)
+    t = np.zeros((tp, tt))
+    nu = np.zeros((tp, tt), np.int32)
+    u = np.zeros((tp, tt, tu), np.float32)
+    e = np.zeros((tp, tt, tu), np.float32)
+    ip = it = iu = -1
+    p_old = t_old = u_old = e_old = -999.0
+    nrange = 0
+    with open(fn) as f:
+        for line in f:
+            parts = line.split()
+            if len(parts) < 4:
+                continue
+            try:
+                press, temp, uu, eps = (float(v) for v in parts[:4])
+            except ValueError:
+                continue
+            if uu < UMIN or uu > UMAX or eps < EPSMIN or eps > EPSMAX:
+                nrange += 1
+                continue
+            if press != p_old:
+                p_old = press
+                ip += 1
+                if ip >= tp:
+                    raise JurassicError("Too many pressure levels!")
+                it = -1
+            if temp != t_old:
+                t_old = temp
+                it += 1
+                if it >= tt:
+                    raise JurassicError("Too many temperatures!")
+                iu = -1
+            if (eps > e_old and uu > u_old) or iu < 0:
+                e_old, u_old = eps, uu
+                iu += 1
+                if iu >= tu:
+                    raise JurassicError("Too many column densities!")
+            p[ip] = press
+            t[ip, it] = temp
+            u[ip, it, iu] = np.float32(uu)
+            e[ip, it, iu] = np.float32(eps)
+            nt[ip] = it + 1
+            nu[ip, it] = iu + 1
+    return ip + 1, p, nt, t, nu, u, e, nrange
+
+
+def _read_binary_table(fn, tp, tt, tu):
+    """One binary table (read_tbl TBLFMT=2, src/jurassic.c:5050-5082)."""
+    buf = open(fn, "rb").read()
+    o = 0
+
+    def take(dt, n):
+        nonlocal o
+        a = np.frombuffer(buf, dtype=dt, count=n, offset=o)
+        o += a.nbytes
+        return a
+
+    n = int(take("<i4", 1)[0])
+    if n > tp:
+        raise JurassicError("Too many pressure levels!")
+    p = np.zeros(tp)
+    nt = np.zeros(tp, np.int32)
+    t = np.zeros((tp, tt))
+    nu = np.zeros((tp, tt), np.int32)
+    u = np.zeros((tp, tt, tu), np.float32)
+    e = np.zeros((tp, tt, tu), np.float32)
+    p[:n] = take("<f8", n)
+    for ip in range(n):
+        ntt = int(take("<i4", 1)[0])
+        if ntt > tt:
+            raise JurassicError("Too many temperatures!")
+        nt[ip] = ntt
+        t[ip, :ntt] = take("<f8", ntt)
+        for it in range(ntt):
+            k = int(take("<i4", 1)[0])
+            if k > tu:
+                raise JurassicError("Too many column densities!")
+            nu[ip, it] = k
+            u[ip, it, :k] = take("<f4", k)
+            e[ip, it, :k] = take("<f4", k)
+    return n, p, nt, t, nu, u, e, 0
+
+
+def read_tbl(ctl: Ctl, tp=41, tt=30, tu=320) -> Tables:
+    """Read every (channel, emitter) table named by ``ctl.tblbase``,
+    ``ctl.nu`` and ``ctl.emitter`` in format ``ctl.tblfmt`` (read_tbl,
+    src/jurassic.c:4949-5110); a missing file leaves np = -1 (the reference
+    warns and goes on).  Capacities tp x tt x tu play TBLNP/TBLNT/TBLNU."""
+    if ctl.tblfmt not in (1, 2):
+        raise JurassicError("Unknown look-up table format!")
+    tbl = Tables.empty(ctl.nd, ctl.ng, tp, tt, tu)
+    reader = _read_ascii_table if ctl.tblfmt == 1 else _read_binary_table
+    for id in range(ctl.nd):
+        for ig in range(ctl.ng):
+            fn = ctl.table_filename(id, ig)
+            if not os.path.exists(fn):
+                continue
+            n, p, nt, t, nu, u, e, _ = reader(fn, tp, tt, tu)
+            tbl.np_[id, ig] = n
+            tbl.p[id, ig], tbl.nt[id, ig], tbl.t[id, ig] = p, nt, t
+            tbl.nu[id, ig], tbl.u[id, ig], tbl.eps[id, ig] = nu, u, e
+    return tbl
+
+
 def read_filter(path: str):
     """Two-column filter/shape file (read_shape, src/jurassic.c:4907-4945)."""
     xs, ys = [], []

@@ -71,6 +71,9 @@ struct jrc_ctx {
   /* continua */
   double ct[CT_TOTAL];
   int have_ct;
+  /* field of view (formod_fov): nfov samples, 0 = off */
+  int nfov;
+  double *fov_dz, *fov_w;
   char err[256];
 };
 
@@ -281,7 +284,76 @@ void jrc_destroy(jrc_ctx *c) {
   free(c->retq_zmin); free(c->retq_zmax); free(c->retk_zmin); free(c->retk_zmax);
   free(c->tnp); free(c->tnt); free(c->tnu); free(c->tp); free(c->tt);
   free(c->tu); free(c->teps); free(c->sr);
+  free(c->fov_dz); free(c->fov_w);
   free(c);
+}
+
+int jrc_set_fov(jrc_ctx *c, int n, const double *dz, const double *w) {
+  free(c->fov_dz);
+  free(c->fov_w);
+  c->fov_dz = c->fov_w = NULL;
+  c->nfov = 0;
+  if (n <= 0)
+    return 0;
+  c->fov_dz = malloc((size_t) n * sizeof(double));
+  c->fov_w = malloc((size_t) n * sizeof(double));
+  memcpy(c->fov_dz, dz, (size_t) n * sizeof(double));
+  memcpy(c->fov_w, w, (size_t) n * sizeof(double));
+  c->nfov = n;
+  return 0;
+}
+
+/* formod_fov (jurassic.c:3121-3192): each ray's radiance and transmittance
+   become the FOV-weighted average of the pencil-beam profiles over view-point
+   altitude, built from the rays within +-5 indices with the same time. */
+#define K_NFOV 5
+static int fov_apply(const jrc_ctx *c, jrc_obs *obs) {
+  const int nd = c->nd, nr = obs->nr;
+  const double *time = obs->geo, *vpz = obs->geo + 4 * (size_t) nr;
+  double *rad0 = malloc((size_t) (nd * nr) * sizeof(double));
+  double *tau0 = malloc((size_t) (nd * nr) * sizeof(double));
+  memcpy(rad0, obs->rad, (size_t) (nd * nr) * sizeof(double));
+  memcpy(tau0, obs->tau, (size_t) (nd * nr) * sizeof(double));
+  int rc = 0;
+  for (int ir = 0; ir < nr && rc == 0; ir++) {
+    double zz[2 * K_NFOV + 1];
+    int ray[2 * K_NFOV + 1], nz = 0;
+    const int lo = ir - K_NFOV > 0 ? ir - K_NFOV : 0;
+    const int hi = ir + 1 + K_NFOV < nr ? ir + 1 + K_NFOV : nr;
+    for (int ir2 = lo; ir2 < hi; ir2++)
+      if (time[ir2] == time[ir]) {
+        zz[nz] = vpz[ir2];
+        ray[nz++] = ir2;
+      }
+    if (nz < 2) {
+      rc = -4;
+      break;
+    }
+    double wsum = 0;
+    for (int id = 0; id < nd; id++) {
+      obs->rad[(size_t) id * nr + ir] = 0;
+      obs->tau[(size_t) id * nr + ir] = 0;
+    }
+    for (int i = 0; i < c->nfov; i++) {
+      const double zfov = vpz[ir] + c->fov_dz[i];
+      const int idx = bracket_irr(zz, nz, zfov);
+      for (int id = 0; id < nd; id++) {
+        const double *r = rad0 + (size_t) id * nr, *t = tau0 + (size_t) id * nr;
+        obs->rad[(size_t) id * nr + ir] +=
+          c->fov_w[i] * lin(zz[idx], r[ray[idx]], zz[idx + 1], r[ray[idx + 1]], zfov);
+        obs->tau[(size_t) id * nr + ir] +=
+          c->fov_w[i] * lin(zz[idx], t[ray[idx]], zz[idx + 1], t[ray[idx + 1]], zfov);
+      }
+      wsum += c->fov_w[i];
+    }
+    for (int id = 0; id < nd; id++) {
+      obs->rad[(size_t) id * nr + ir] /= wsum;
+      obs->tau[(size_t) id * nr + ir] /= wsum;
+    }
+  }
+  free(rad0);
+  free(tau0);
+  return rc;
 }
 
 int jrc_set_table(jrc_ctx *c, int id, int ig, int np, const double *p,
@@ -1046,6 +1118,8 @@ static int formod_one(const jrc_ctx *c, const jrc_atm *atm, jrc_obs *obs,
     obs->tp[1 * nr + ir] = tp3[1];
     obs->tp[2 * nr + ir] = tp3[2];
   }
+  if (rc == 0 && c->nfov > 0)
+    rc = fov_apply(c, obs);
   if (c->write_bbt)
     for (int id = 0; id < nd; id++)
       for (int ir = 0; ir < nr; ir++) {
@@ -1079,6 +1153,8 @@ int jrc_formod(jrc_ctx *c, jrc_atm *atm, jrc_obs *obs) {
     set_err(c, "Observer below surface!");
   if (rc == -3)
     set_err(c, "Too many LOS points!");
+  if (rc == -4)
+    set_err(c, "Cannot apply FOV convolution!");
   return rc;
 }
 

@@ -106,6 +106,10 @@ int jrc_sizes(const jrc_ctx *c, const jrc_atm *atm, const jrc_obs *obs,
 int jrc_atm2x(const jrc_ctx *c, const jrc_atm *atm, double *x, int *iqa,
               int *ipa);
 
+/* Field of view (formod_fov, jurassic.c:3121-3192): n samples of (dz, w)
+   as read by read_shape from the FOV file; n = 0 switches it off. */
+int jrc_set_fov(jrc_ctx *c, int n, const double *dz, const double *w);
+
 /* Finite-difference Jacobian (kernel, jurassic.c:4004-4099): kmat[m][n]. */
 int jrc_kernel(jrc_ctx *c, jrc_atm *atm, jrc_obs *obs, double *kmat,
                int nthreads);

@@ -111,6 +111,7 @@ def lib():
         L.jrc_kernel.argtypes = [C.c_void_p, C.POINTER(_Atm), C.POINTER(_Obs), _dp, C.c_int]
         L.jrc_retrieval.argtypes = [C.c_void_p, C.POINTER(_Ret), C.POINTER(_Atm),
                                     C.POINTER(_Obs), _dp, _dp, _dp, _dp, C.c_int, _ip, C.c_int]
+        L.jrc_set_fov.argtypes = [C.c_void_p, C.c_int, _dp, _dp]
         L.jrc_retrieval_ex.argtypes = [C.c_void_p, C.POINTER(_Ret), C.POINTER(_Atm),
                                        C.POINTER(_Obs), _dp, _dp, _dp, _dp, C.c_int, _ip, C.c_int,
                                        C.POINTER(_Ana)]
@@ -125,7 +126,7 @@ def continua_blob():
 class Oracle:
     """One CPU-oracle context: a control set, its tables and source functions."""
 
-    def __init__(self, ctl, tables, filters, nlos_max=4096):
+    def __init__(self, ctl, tables, filters, nlos_max=4096, fov=None):
         L = lib()
         self.ctl = ctl
         self._keep = []
@@ -150,6 +151,10 @@ class Oracle:
                  ret_sfeps=ctl.ret_sfeps, nlos_max=nlos_max)
         tp, tt, tu = tables.u.shape[2:]
         self.h = L.jrc_create(C.byref(c), tp, tt, tu)
+        if fov is not None:
+            dz, w = _d(fov[0]), _d(fov[1])
+            self._keep.append((dz, w))
+            self._check(L.jrc_set_fov(self.h, len(dz), _ptr(dz), _ptr(w)))
         blob = continua_blob()
         self._check(L.jrc_set_continua(self.h, _ptr(blob), len(blob)))
         for id in range(ctl.nd):

@@ -35,13 +35,17 @@ def build(tag="std", flags=()):
     return r.returncode == 0
 
 
-def write_inputs(workdir, ctl, tables, filters, ret=None, extra_lines=()):
-    """Files the reference reads: ctl, TBLFMT=2 tables, .filt filters."""
-    from jurassic_gb300.tables import write_filters, write_tbl
+def write_inputs(workdir, ctl, tables, filters, ret=None, extra_lines=(), fov=None):
+    """Files the reference reads: ctl, TBLFMT=2 tables, .filt filters and,
+    with fov = (dz, w), the FOV shape file."""
+    from jurassic_gb300.tables import write_filter, write_filters, write_tbl
     import copy
     c = copy.copy(ctl)
     c.tblbase = os.path.join(workdir, "tbl")
-    c.tblfmt = 2
+    c.tblfmt = ctl.tblfmt if ctl.tblfmt in (1, 2) else 2
+    if fov is not None:
+        c.fov = os.path.join(workdir, "fov.dat")
+        write_filter(c.fov, np.asarray(fov[0], float), np.asarray(fov[1], float))
     write_tbl(c, tables)
     write_filters(c, filters)
     lines = c.to_lines()
@@ -141,7 +145,8 @@ def _atm_dict(ctl, atm):
                 scal=atm.scal(ctl))
 
 
-def run(ctl, tables, filters, jobs, tag="std", ret=None, workdir=None, timeout=3600):
+def run(ctl, tables, filters, jobs, tag="std", ret=None, workdir=None, timeout=3600, fov=None,
+        post_write=None):
     """Run jobs [(kind, atm, obs, extra), ...] through the reference.
 
     kind in {"formod", "raytrace", "kernel", "retrieval"}.  Returns one result
@@ -149,7 +154,9 @@ def run(ctl, tables, filters, jobs, tag="std", ret=None, workdir=None, timeout=3
     """
     own = workdir is None
     tmp = tempfile.mkdtemp(prefix="jref_") if own else workdir
-    ctlfile = write_inputs(tmp, ctl, tables, filters, ret=ret)
+    ctlfile = write_inputs(tmp, ctl, tables, filters, ret=ret, fov=fov)
+    if post_write is not None:      # e.g. rewrite table files before the reference reads them
+        post_write(tmp)
     js = []
     for kind, atm, obs, extra in jobs:
         j = dict(kind=kind, atm=_atm_dict(ctl, atm), geo=obs.geo(), rad=obs.rad)

@@ -130,6 +130,74 @@ def formod_cases():
          **obs_arrays("obs_", obs))
 
 
+def fov_shape():
+    dz = np.linspace(-2.0, 2.0, 21)
+    return dz, np.exp(-dz ** 2)
+
+
+def fov_case():
+    """Limb with field-of-view convolution (formod_fov, jurassic.c:3121-3192):
+    8 rays at 10-31 km, a masked channel, radiance and BT output."""
+    w = synth.config_limb_ega(n_rays=8)
+    tbl = small_tables(w.ctl, 15)
+    atm, obs = w.batch.item(w.ctl, 0)
+    obs.rad[2, 5] = np.nan
+    res = {}
+    for label, mod in (("ega", {}), ("bbt", {"write_bbt": 1})):
+        ctl = copy.deepcopy(w.ctl)
+        for k, v in mod.items():
+            setattr(ctl, k, v)
+        r = refimpl.run(ctl, tbl, w.filters, [("formod", atm, obs, None)], fov=fov_shape())[0]
+        res.update({label + "_ctl": ctl_json(ctl), label + "_rad": r["rad"],
+                    label + "_tau": r["tau"], label + "_tp": r["tp"]})
+    dz, wf = fov_shape()
+    save("ref_formod_fov.npz", fov_dz=dz, fov_w=wf, **res, **table_arrays(tbl, w.filters),
+         **atm_arrays("atm_", w.ctl, atm), **obs_arrays("obs_", obs))
+
+
+def tbl_ascii_case():
+    """ASCII tables (read_tbl TBLFMT=1) with lines the reader must skip (out
+    of range, text) or fold (a point that does not increase u and eps
+    overwrites the previous one): the reference's forward model with these
+    files, and the files themselves."""
+    w = synth.config_limb_ega(n_rays=4)
+    ctl = copy.deepcopy(w.ctl)
+    ctl.tblfmt = 1
+    tbl = small_tables(ctl, 16)
+    atm, obs = w.batch.item(w.ctl, 0)
+    texts = {}
+
+    def mangle(workdir):
+        c2 = copy.copy(ctl)
+        c2.tblbase = os.path.join(workdir, "tbl")
+        for id in range(ctl.nd):
+            for ig in range(ctl.ng):
+                fn = c2.table_filename(id, ig)
+                lines = open(fn).read().splitlines()
+                out = []
+                for k, line in enumerate(lines):
+                    out.append(line)
+                    parts = line.split()
+                    if len(parts) != 4:
+                        continue
+                    p, t, u, e = parts
+                    if k % 97 == 5:
+                        out.append("%s %s %s %s" % (p, t, u, "1.5"))         # eps > EPSMAX
+                        out.append("%s %s %s %s" % (p, t, "-1", e))          # u < UMIN
+                        out.append("this line is not data")
+                    if k % 89 == 7:
+                        # u and eps not above the last point: it overwrites that point
+                        out.append("%s %s %.9e %.9e" % (p, t, 0.9995 * float(u), 0.9995 * float(e)))
+                txt = "\n".join(out) + "\n"
+                open(fn, "w").write(txt)
+                texts["tbl_%d_%d" % (id, ig)] = np.frombuffer(txt.encode(), dtype=np.uint8)
+
+    r = refimpl.run(ctl, tbl, w.filters, [("formod", atm, obs, None)], post_write=mangle)[0]
+    save("ref_tbl_ascii.npz", ctl=ctl_json(ctl), rad=r["rad"], tau=r["tau"], **texts,
+         **table_arrays(tbl, w.filters), **atm_arrays("atm_", ctl, atm),
+         **obs_arrays("obs_", obs))
+
+
 def kernel_case():
     ctl = Ctl(emitter=["CO2", "H2O"], nu=[667.78, 792.0], formod=1)
     z = np.arange(0.0, 82.0, 2.0)
@@ -186,6 +254,8 @@ def main():
     formod_cases()
     kernel_case()
     retrieval_case()
+    fov_case()
+    tbl_ascii_case()
 
 
 if __name__ == "__main__":

@@ -102,3 +102,63 @@ def test_read_ret_defaults(tmp_path):
     r = read_ret(argv, ctl)
     assert r.kernel_recomp == 3 and r.conv_itmax == 30 and r.conv_dmin == 0.1
     assert np.array_equal(r.err_noise, [1e-4, 1e-4]) and r.err_temp == 2.0
+
+
+# ---------------------------------------------------------------------------
+# emissivity table files (read_tbl / write_tbl, src/jurassic.c:4949-5110,
+# 5810-5892)
+
+@pytest.mark.parametrize("fmt", [1, 2])
+def test_table_files_round_trip(tmp_path, fmt):
+    import copy
+    from jurassic_gb300 import synth
+    from jurassic_gb300.tables import read_tbl, write_tbl
+    w = synth.config_limb_ega()
+    ctl = copy.deepcopy(w.ctl)
+    ctl.tblbase = str(tmp_path / "tbl")
+    ctl.tblfmt = fmt
+    tbl = synth.make_tables(ctl, 3, tp=12, tt=5, tu=40)
+    tbl.np_[1, 0] = -1                       # missing file
+    write_tbl(ctl, tbl)
+    back = read_tbl(ctl, 12, 5, 40)
+    assert np.array_equal(back.np_, tbl.np_)
+    for id in range(ctl.nd):
+        for ig in range(ctl.ng):
+            n = int(tbl.np_[id, ig])
+            if n < 0:
+                continue
+            assert np.array_equal(back.p[id, ig, :n], tbl.p[id, ig, :n])
+            assert np.array_equal(back.nt[id, ig, :n], tbl.nt[id, ig, :n])
+            for ip in range(n):
+                for it in range(int(tbl.nt[id, ig, ip])):
+                    k = int(tbl.nu[id, ig, ip, it])
+                    assert back.nu[id, ig, ip, it] == k
+                    assert back.t[id, ig, ip, it] == tbl.t[id, ig, ip, it]
+                    assert np.array_equal(back.u[id, ig, ip, it, :k], tbl.u[id, ig, ip, it, :k])
+                    assert np.array_equal(back.eps[id, ig, ip, it, :k], tbl.eps[id, ig, ip, it, :k])
+
+
+def test_ascii_tables_read_like_the_reference(tmp_path, built_oracle):
+    """ASCII table files with skipped and folded lines: read by read_tbl here
+    and by the reference; the oracle's forward model with the tables read
+    here equals the reference's with the tables it read."""
+    import golden_io as G
+    from jurassic_gb300.tables import read_tbl
+    from oracle import oracle
+    f = G.load("ref_tbl_ascii.npz")
+    ctl = G.ctl_from(f["ctl"])
+    ctl.tblbase = str(tmp_path / "tbl")
+    for id in range(ctl.nd):
+        for ig in range(ctl.ng):
+            with open(ctl.table_filename(id, ig), "wb") as fo:
+                fo.write(f["tbl_%d_%d" % (id, ig)].tobytes())
+    tbl = read_tbl(ctl, 32, 6, 64)
+    ora = oracle.Oracle(ctl, tbl, G.filters_from(f, ctl.nd))
+    atm = G.atm_from(f, "atm_", ctl)
+    obs = G.obs_from(f, "obs_", ctl.nd)
+    rad, tau, tp, _ = ora.formod(atm, obs)
+    assert np.max(np.abs(rad - f["rad"]) / np.abs(f["rad"])) <= 1e-12
+    assert np.max(np.abs(tau - f["tau"])) <= 1e-14
+    # the folded lines changed the tables: they differ from the unmangled set
+    orig = G.tables_from(f)
+    assert not np.array_equal(tbl.u, orig.u)

@@ -139,3 +139,23 @@ def test_oracle_direct_vs_reference_build(built_oracle):
         r = refimpl.run(ctl, w.tables, w.filters, [("formod", atm, obs, None)])[0]
         assert np.array_equal(rad, r["rad"]) and np.array_equal(tau, r["tau"])
         assert np.array_equal(tp, r["tp"])
+
+
+@pytest.mark.parametrize("case", ["ega", "bbt"])
+def test_formod_fov_vs_reference(built_oracle, case):
+    """Field-of-view convolution (formod_fov, jurassic.c:3121-3192) after the
+    pencil beams, before BT conversion and masking."""
+    from oracle import oracle
+    f = G.load("ref_formod_fov.npz")
+    ctl = G.ctl_from(f[case + "_ctl"])
+    ora = oracle.Oracle(ctl, G.tables_from(f), G.filters_from(f, ctl.nd),
+                        fov=(f["fov_dz"], f["fov_w"]))
+    atm = G.atm_from(f, "atm_", ctl)
+    obs = G.obs_from(f, "obs_", ctl.nd)
+    rad, tau, tp, _ = ora.formod(atm, obs)
+    assert np.isnan(rad[2, 5]) and np.isnan(f[case + "_rad"][2, 5])
+    fin = np.isfinite(rad)
+    assert np.array_equal(fin, np.isfinite(f[case + "_rad"]))
+    assert _rel(rad[fin], f[case + "_rad"][fin]) <= RTOL
+    assert np.max(np.abs(tau - f[case + "_tau"])) <= 1e-14
+    assert np.max(np.abs(tp - f[case + "_tp"])) <= 1e-9
