@@ -201,6 +201,170 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_jacobian(args, rank, world, local, pg):
+    """Batched FD Jacobian + normal equations (kernel(), jurassic.c:4004-4099,
+    and K^T Se^-1 K, retrieval.c:403-444): nadir profiles, 81 levels on
+    0-80 km, 150 channels on 650-2400 cm^-1, CO2 + H2O + O3 + CH4, state =
+    T and the four gases on all levels (n = 405), Se diagonal from a 0.2 K
+    noise-equivalent brightness temperature at 250 K."""
+    import copy
+    import ctypes as C
+    from jurassic_gb300 import native, synth
+    nobs = args.nobs if args.nobs != 100000 else 2048
+    w = synth.config_nadir(nobs, seed=4, nd=150, nlev=81, ztop=80.0,
+                           emitters=("CO2", "H2O", "O3", "CH4"))
+    ctl = copy.deepcopy(w.ctl)
+    ctl.rett_zmin, ctl.rett_zmax = 0.0, 80.0
+    ctl.retq_zmin = np.zeros(ctl.ng)
+    ctl.retq_zmax = np.full(ctl.ng, 80.0)
+    ctx = native.Context(ctl, w.tables, w.filters, device=local)
+    L = native.load()
+    m, n = ctx.kernel_sizes(w.batch)
+    units = int(np.sum(m.astype(np.int64) * (n + 1)))
+    small = synth.pack(ctl, [w.batch.item(ctl, i) for i in range(min(8, nobs))])
+    for _ in range(args.warmup):
+        ctx.kernel_batch(small, native.MIXED)
+    barrier(pg)
+    ms = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            Ks, _ = ctx.kernel_batch(w.batch, native.MIXED)
+            ms.append(1e3 * (time.perf_counter() - t0))
+    barrier(pg)
+    ms_step = allmax(pg, statistics.mean(ms))
+    value = units * world / (ms_step / 1e3)
+    # normal equations on the device
+    nu = np.asarray(ctl.nu)
+    x = 1.43877506 * nu / 250.0
+    dbdt = 1.19104259e-8 * nu ** 3 * x * np.exp(x) / (250.0 * np.expm1(x) ** 2)
+    sig = 0.2 * dbdt
+    rng = np.random.default_rng(5)
+    Kc = np.ascontiguousarray(np.concatenate([k.ravel() for k in Ks]))
+    wv = np.concatenate([1.0 / sig[:mi] for mi in m])
+    dy = rng.standard_normal(wv.size) / wv
+    nA, nb = int(np.sum(n.astype(np.int64) ** 2)), int(np.sum(n))
+    dev = {}
+    for k, a in (("K", Kc), ("w", wv), ("dy", dy)):
+        dev[k] = L.jgb_dev_alloc(a.nbytes)
+        L.jgb_memcpy_h2d(dev[k], a.ctypes.data, a.nbytes)
+    dev["A"] = L.jgb_dev_alloc(8 * nA)
+    dev["b"] = L.jgb_dev_alloc(8 * nb)
+    mi = np.ascontiguousarray(m, np.int32)
+    ni = np.ascontiguousarray(n, np.int32)
+    flops = float(np.sum(2.0 * m * (n + 1.0) ** 2))
+    ne = {}
+    A = {}
+    for name, prec in (("mixed_3xtf32", native.MIXED), ("fp64", native.FP64)):
+        kms = C.c_float(0)
+        ctx._check(L.jgb_normal_equations_dev(ctx.h, nobs, mi.ctypes.data_as(C.POINTER(C.c_int)),
+                                              ni.ctypes.data_as(C.POINTER(C.c_int)), dev["K"],
+                                              dev["w"], dev["dy"], dev["A"], dev["b"], prec,
+                                              C.byref(kms)))
+        a = np.zeros(nA)
+        L.jgb_memcpy_d2h(a.ctypes.data, dev["A"], a.nbytes)
+        A[name] = a
+        ne[name] = {"kernel_ms": kms.value, "tflops": flops / (kms.value / 1e3) / 1e12}
+    for p in dev.values():
+        L.jgb_dev_free(p)
+    rel = float(np.max(np.abs(A["mixed_3xtf32"] - A["fp64"])) / np.max(np.abs(A["fp64"])))
+    try:
+        bf16 = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"]
+        kind = "measured"
+    except (OSError, KeyError, ValueError):
+        bf16, kind = 1900.0, "fallback"
+    peak = bf16 / 2 / 3     # dense TF32 = half the bf16 rate; 3xTF32 = three products
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32 path loop, f64 perturbation bookkeeping", "data": "synthetic (seeded)",
+                "config": {"workload": "fd_jacobian_nadir_%dobs_81lev_150ch_4gas_n405" % nobs,
+                           "observations": nobs, "state_elements": int(n[0]),
+                           "radiances_per_step": units,
+                           "l2_policy": "inputs larger than L2 (129 MB); no flush"},
+                "e2e": {"value": value, "unit": UNIT,
+                        "h2d_bytes_per_step": int(w.batch.nlev * 8 * (6 + ctl.ng + ctl.nw)),
+                        "d2h_bytes_per_step": int(8 * Kc.size)},
+                "normal_equations": dict(ne, flops=flops, problems=nobs, m=int(m[0]),
+                                         n=int(n[0]), mixed_vs_fp64_max_rel=rel,
+                                         roofline={"bound": "tensor", "peak": peak,
+                                                   "unit": "TFLOP/s", "peak_kind": kind,
+                                                   "peak_note": "bf16 dense / 2 (TF32) / 3 (3xTF32)",
+                                                   "frac": ne["mixed_3xtf32"]["tflops"] / peak}),
+                "clocks": clk.summary()}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def run_normal(args, rank, world, local, pg):
+    """Normal-equation products alone (matrix_product, retrieval.c:403-444):
+    nobs problems with m = 150 measurements and n = 405 state elements
+    (the shapes of the Jacobian workload), seeded K with the magnitudes of
+    radiance Jacobians; 3xTF32 (tensor cores, mma.sync m16n8k8) and FP64."""
+    import ctypes as C
+    from jurassic_gb300 import native, synth
+    from jurassic_gb300.model import Ctl
+    nobs = args.nobs if args.nobs != 100000 else 2048
+    m_, n_ = 150, 405
+    ctl = Ctl(emitter=["CO2"], nu=[700.0])
+    ctx = native.Context(ctl, device=local)
+    L = native.load()
+    rng = np.random.default_rng(6)
+    K = (rng.standard_normal((nobs, m_, n_)) * np.exp(rng.uniform(-6, 0, (nobs, 1, n_))) * 1e-4)
+    w = 1.0 / (2e-6 * (1 + rng.uniform(0, 1, (nobs, m_))))
+    dy = rng.standard_normal((nobs, m_)) / w
+    dev = {}
+    for k, a in (("K", K), ("w", w), ("dy", dy)):
+        a = np.ascontiguousarray(a)
+        dev[k] = L.jgb_dev_alloc(a.nbytes)
+        L.jgb_memcpy_h2d(dev[k], a.ctypes.data, a.nbytes)
+    dev["A"] = L.jgb_dev_alloc(8 * nobs * n_ * n_)
+    dev["b"] = L.jgb_dev_alloc(8 * nobs * n_)
+    mi = np.full(nobs, m_, np.int32)
+    ni = np.full(nobs, n_, np.int32)
+    flops = 2.0 * m_ * (n_ + 1) ** 2 * nobs
+    res, A = {}, {}
+    for name, prec in (("mixed_3xtf32", native.MIXED), ("fp64", native.FP64)):
+        times = []
+        for _ in range(args.warmup + args.steps):
+            kms = C.c_float(0)
+            ctx._check(L.jgb_normal_equations_dev(ctx.h, nobs, mi.ctypes.data_as(C.POINTER(C.c_int)),
+                                                  ni.ctypes.data_as(C.POINTER(C.c_int)), dev["K"],
+                                                  dev["w"], dev["dy"], dev["A"], dev["b"], prec,
+                                                  C.byref(kms)))
+            times.append(kms.value)
+        t = statistics.mean(times[args.warmup:])
+        a = np.zeros(nobs * n_ * n_)
+        L.jgb_memcpy_d2h(a.ctypes.data, dev["A"], a.nbytes)
+        A[name] = a
+        res[name] = {"kernel_ms": t, "tflops": flops / (t / 1e3) / 1e12}
+    for p in dev.values():
+        L.jgb_dev_free(p)
+    try:
+        bf16 = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"]
+        kind = "measured"
+    except (OSError, KeyError, ValueError):
+        bf16, kind = 1900.0, "fallback"
+    peak = bf16 / 2 / 3
+    rel = float(np.max(np.abs(A["mixed_3xtf32"] - A["fp64"])) / np.max(np.abs(A["fp64"])))
+    if rank == 0:
+        v = res["mixed_3xtf32"]["tflops"]
+        print(json.dumps({
+            "metric": "normal-equation TFLOP/s", "value": v, "unit": "TFLOP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": res["mixed_3xtf32"]["kernel_ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "3xTF32 (fp32 accumulate)",
+            "data": "synthetic (seeded)",
+            "config": {"workload": "normal_equations_%dx(150x405)" % nobs,
+                       "l2_policy": "K (%.0f MB) larger than L2; no flush" % (K.nbytes / 1e6)},
+            "fp64": res["fp64"], "mixed_vs_fp64_max_rel": rel, "flops_per_step": flops,
+            "roofline": {"bound": "tensor", "achieved": v, "peak": peak, "unit": "TFLOP/s",
+                         "frac": v / peak, "traffic": None, "peak_kind": kind,
+                         "peak_note": "bf16 dense / 2 (TF32) / 3 (3xTF32)"}}), flush=True)
+    ctx.close()
+
+
 def serving_workload(seed=5):
     """Retrieval serving stream: a 300-channel context (650-2400 cm^-1,
     CO2 + H2O + O3), requests with 50-300 measured channels, 41-101 levels
@@ -273,7 +437,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="nadir", choices=["nadir", "limb_cga"])
+    ap.add_argument("--workload", default="nadir",
+                    choices=["nadir", "limb_cga", "jacobian", "normal"])
     ap.add_argument("--nobs", type=int, default=100000)
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -293,6 +458,11 @@ def main():
     from jurassic_gb300 import native
     from jurassic_gb300.model import brightness
     native.load()
+    if args.workload in ("jacobian", "normal"):
+        (run_jacobian if args.workload == "jacobian" else run_normal)(args, rank, world, local, pg)
+        if pg is not None:
+            pg.destroy_process_group()
+        return
     w = build_workload(args)
     ctl, b = w.ctl, w.batch
     ctx = native.Context(ctl, w.tables, w.filters, device=local)

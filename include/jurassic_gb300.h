@@ -161,6 +161,14 @@ int jgb_normal_equations(jgb_ctx *ctx, int nret, const int *m, const int *n, con
                          const double *w, const double *dy, double *A, double *b,
                          int precision);
 
+/* jgb_normal_equations on device buffers (K, w, dy, A, b device pointers;
+   m, n host arrays; at most 65535 problems).  Returns when done; with
+   kernel_ms != NULL the products are computed twice and *kernel_ms is the
+   CUDA-event time of the second launch (descriptor upload excluded). */
+int jgb_normal_equations_dev(jgb_ctx *ctx, int nret, const int *m, const int *n,
+                             const double *K, const double *w, const double *dy, double *A,
+                             double *b, int precision, float *kernel_ms);
+
 /* Emitter contributions (TASK c, formod.c:200-249) of every observation of a
    host batch: continua off; variant g < ng keeps only emitter g (all other
    mixing ratios and all extinction zero), variant ng ("EXTINCT") has all

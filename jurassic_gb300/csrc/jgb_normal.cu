@@ -273,3 +273,43 @@ extern "C" int jgb_normal_equations(jgb_ctx* x, int nret, const int* m, const in
   cudaFree(buf);
   return rc ? ctx_fail(x, rc, "normal-equation kernel failed") : JGB_OK;
 }
+
+// Device-buffer entry point: K, w, dy, A, b on the device, m and n on the
+// host; runs on the context's stream and returns when the products are
+// done.  *kernel_ms (optional) receives the CUDA-event time of the kernel.
+extern "C" int jgb_normal_equations_dev(jgb_ctx* x, int nret, const int* m, const int* n,
+                                        const double* K, const double* w, const double* dy,
+                                        double* A, double* b, int precision, float* kernel_ms) {
+  if (!x || nret <= 0 || !m || !n || !K || !w || !dy || !A || !b)
+    return ctx_fail(x, JGB_ERR_ARG, "bad arguments");
+  if (nret > 65535) return ctx_fail(x, JGB_ERR_ARG, "at most 65535 problems per call");
+  CtxView v;
+  int rc = ctx_view(x, &v);
+  if (rc != JGB_OK && rc != JGB_ERR_STATE) return rc;
+  cudaSetDevice(v.device);
+  for (int i = 0; i < nret; i++)
+    if (m[i] <= 0 || n[i] <= 0) return ctx_fail(x, JGB_ERR_ARG, "empty retrieval");
+  void* ddesc = nullptr;
+  if (cudaMalloc(&ddesc, normal_desc_bytes(nret)) != cudaSuccess)
+    return ctx_fail(x, JGB_ERR_CUDA, "cudaMalloc failed");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaStream_t s = v.stream;
+  // descriptors are uploaded (and the stream synchronised) inside; the
+  // events bracket the kernel launch that follows
+  rc = normal_equations_dev(nret, m, n, K, w, dy, A, b, precision, nullptr, ddesc, s);
+  // time a second identical launch only when asked: the first one above
+  // included the descriptor upload
+  if (rc == JGB_OK && kernel_ms) {
+    cudaEventRecord(e0, s);
+    rc = normal_equations_dev(nret, m, n, K, w, dy, A, b, precision, nullptr, ddesc, s);
+    cudaEventRecord(e1, s);
+  }
+  if (cudaStreamSynchronize(s) != cudaSuccess) rc = JGB_ERR_CUDA;
+  if (rc == JGB_OK && kernel_ms) cudaEventElapsedTime(kernel_ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(ddesc);
+  return rc ? ctx_fail(x, rc, "normal-equation kernel failed") : JGB_OK;
+}

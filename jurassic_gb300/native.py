@@ -121,6 +121,9 @@ SIGNATURES = {
     "jgb_normal_equations": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _dp, _dp, _dp, _dp, _dp,
                                        C.c_int]),
     "jgb_formod_contrib": (C.c_int, [C.c_void_p, C.POINTER(_Batch), _dp, _dp, C.c_int]),
+    "jgb_normal_equations_dev": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, C.c_void_p, C.c_void_p,
+                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                           C.POINTER(C.c_float)]),
     "jgb_retrieve_batch": (C.c_int, [C.c_void_p, C.POINTER(_Ret), C.POINTER(_Batch), _dp, _dp,
                                      _dp, _ip, C.c_int]),
     "jgb_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
