@@ -541,11 +541,18 @@ def main():
         hbm, peak_kind = peaks()
         bytes_alg = path_bytes_model(ctl, w.tables, stats["los_points"])
         achieved = bytes_alg / (statistics.mean(path_ms) / 1e3) / 1e9
-        try:
-            traffic = json.load(open(os.path.join(ROOT, "profiles", "path_mixed_traffic.json")))
-            traffic_per_launch = traffic["bytes_per_los_point"] * stats["los_points"]
-        except (OSError, KeyError, ValueError):
-            traffic_per_launch = None
+        # DRAM bytes per LOS point of k_path_mixed from the committed ncu
+        # summary (captured on a 4000-observation nadir batch with the same
+        # channels and emitters), scaled by the LOS points of this launch
+        traffic_per_launch = None
+        if args.workload == "nadir":
+            try:
+                for ln in open(os.path.join(ROOT, "profiles", "k_path_mixed_nadir4000.md")):
+                    if "dram_bytes_per_los_point:" in ln:
+                        per = float(ln.split("dram_bytes_per_los_point:")[1].split("`")[0])
+                        traffic_per_launch = per * stats["los_points"]
+            except (OSError, ValueError, IndexError):
+                traffic_per_launch = None
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -558,9 +565,11 @@ def main():
                            "l2_policy": "inputs and tables larger than L2 (129 MB); no flush",
                            "parallelism": "replicas" if world > 1 else "single GPU"},
                 "stage_ms": {k: stats[k] for k in ("hydro_ms", "trace_ms", "pack_ms", "path_ms")},
-                "autotune": {"path_variant": stats["path_variant"], "variant_ms": stats["tune_ms"][:4],
+                "autotune": {"path_variant": stats["path_variant"], "variant_ms": stats["tune_ms"][:7],
                              "variants": ["no register cap", "5 blocks/SM (<=102 regs)",
-                                          "6 blocks/SM (<=85 regs)", "4 blocks/SM (<=128 regs)"]},
+                                          "6 blocks/SM (<=85 regs)", "4 blocks/SM (<=128 regs)",
+                                          "8 blocks/SM (<=64 regs)", "10 blocks/SM (<=51 regs)",
+                                          "12 blocks/SM (<=42 regs)"]},
                 "wall_s_timed": wall,
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h), "ms_per_step": statistics.mean(e2e_ms)},
@@ -570,6 +579,7 @@ def main():
                 "gpu_launches": int(stats["path_launches"]) * args.steps,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                              "frac": achieved / hbm, "traffic": traffic_per_launch,
+                             "traffic_note": "ncu dram bytes per LOS point (4000-observation capture) x LOS points; the byte model counts table probes mostly served by L1/L2",
                              "kernel": "k_path_mixed", "bytes_model": "per (LOS point, channel): ng*8*(ceil(log2 TU)+4)*4 + 16 B",
                              "bytes_per_launch": bytes_alg, "peak_kind": peak_kind},
                 "clocks": clk.summary()}

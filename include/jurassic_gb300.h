@@ -91,7 +91,7 @@ typedef struct {
   long long los_points;          /* LOS points of the batch */
   int path_launches;             /* kernels launched by the last call */
   int path_variant;              /* mixed path kernel variant chosen by the autotuner */
-  float tune_ms[4];              /* autotuner timings of the variants [ms] */
+  float tune_ms[8];              /* autotuner timings of the variants [ms] */
 } jgb_stats;
 
 /* Context: replaces the process-global table state initialised by the first

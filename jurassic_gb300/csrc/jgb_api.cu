@@ -305,7 +305,8 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
           if (same) x->grid_mask |= 1u << g;
         }
       launch_rowmeta((long long)c.nd * c.ng * x->tp * x->tt, x->tu, x->t_nu.as<int>(),
-                     x->t_u.as<float>(), x->t_eps.as<float>(), x->t_meta.as<float4>(), s);
+                     x->t_u.as<float>(), x->t_eps.as<float>(), x->t_tf.as<float>(),
+                     x->t_meta.as<float4>(), s);
       x->meta_stale = false;
     }
     // tile plan: rays sorted by LOS length, 32 per tile
@@ -393,7 +394,7 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
   x->stats.los_points = total;
   x->stats.path_launches = launches;
   x->stats.path_variant = x->path_variant;
-  for (int v = 0; v < 4; v++) x->stats.tune_ms[v] = v < (int)x->tune_ms.size() ? x->tune_ms[v] : 0.f;
+  for (int v = 0; v < 8; v++) x->stats.tune_ms[v] = v < (int)x->tune_ms.size() ? x->tune_ms[v] : 0.f;
   return JGB_OK;
 }
 
@@ -886,7 +887,7 @@ int jgb_tables_init(jgb_ctx* x, int tp, int tt, int tu) {
   CK(x->t_eps.reserve(sizeof(float) * std::max<size_t>(ndg * tp * tt * tu, 1)));
   CK(x->t_pf.reserve(sizeof(float) * std::max<size_t>(ndg * tp, 1)));
   CK(x->t_tf.reserve(sizeof(float) * std::max<size_t>(ndg * tp * tt, 1)));
-  CK(x->t_meta.reserve(sizeof(float4) * std::max<size_t>(ndg * tp * tt, 1)));
+  CK(x->t_meta.reserve(2 * sizeof(float4) * std::max<size_t>(ndg * tp * tt, 1)));
   x->meta_stale = true;
   CK(cudaMemcpy(x->t_np.p, x->h_np.data(), sizeof(int) * ndg, cudaMemcpyHostToDevice));
   CK(cudaMemset(x->t_nt.p, 0, sizeof(int) * ndg * tp));

@@ -64,18 +64,20 @@ struct RowF {
   const float* u;
   const float* e;
   int n;
-  float u0, un, e0, en;  // first/last entries of the row (one 16-byte load)
+  float u0, un, e0, en;  // first/last entries of the row
+  float t;               // temperature of the row
 };
 
-// 32-bit row arithmetic (the table upload checks that rows x TU < 2^32)
-__device__ __forceinline__ RowF rowf_at(const TblDev& T, long long dg, int ip, int it) {
-  const unsigned r = ((unsigned)dg * (unsigned)T.tp + (unsigned)ip) * (unsigned)T.tt + (unsigned)it;
+// Row r = (dg * tp + ip) * tt + it from its 32-byte record; 32-bit row
+// arithmetic (the table upload checks that rows x TU < 2^32).
+__device__ __forceinline__ RowF rowf_at(const TblDev& T, unsigned r) {
   RowF w;
-  const size_t off = (size_t)(r * (unsigned)T.tu);
+  const unsigned off = r * (unsigned)T.tu;
   w.u = T.u + off;
   w.e = T.eps + off;
-  w.n = __ldg(T.nu + r);
-  const float4 m = __ldg(T.rowmeta + r);
+  const float4 m = __ldg(T.rowmeta + 2 * r), m2 = __ldg(T.rowmeta + 2 * r + 1);
+  w.n = __float_as_int(m2.x);
+  w.t = m2.y;
   w.u0 = m.x;
   w.un = m.y;
   w.e0 = m.z;
@@ -102,17 +104,15 @@ struct Bracket {
 };
 
 __device__ __forceinline__ Bracket hunt_f(const float* g, int n, float x, int h) {
-  h = h < 0 ? 0 : (h > n - 2 ? n - 2 : h);
-  const float a = __ldg(g + h), b = __ldg(g + h + 1);
-  const float c = (h + 2 <= n - 1) ? __ldg(g + h + 2) : b;
-  int i;
-  if (a <= x) {
-    if (x < b || h + 1 >= n - 1) return Bracket{h, a, b};          // h == n-2 on the right end
-    if (x < c || h + 2 >= n - 1) return Bracket{h + 1, b, c};      // h + 1 == n-2 on the right end
-    i = bisect_f(g, h + 2, n - 1, x);
-  } else {
-    i = bisect_f(g, 0, h, x);
+  h = min(max(h, 0), n - 2);
+  const int h2 = min(h + 2, n - 1);
+  const float a = __ldg(g + h), b = __ldg(g + h + 1), c = __ldg(g + h2);
+  // bracket h or h + 1 (at the right end of the row, x == g[n-1] keeps n-2)
+  if (a <= x && (x < c || h2 == n - 1)) {
+    const bool up = x >= b && h + 1 <= n - 2;
+    return up ? Bracket{h + 1, b, c} : Bracket{h, a, b};
   }
+  const int i = a <= x ? bisect_f(g, h + 2, n - 1, x) : bisect_f(g, 0, h, x);
   return Bracket{i, __ldg(g + i), __ldg(g + i + 1)};
 }
 
@@ -122,13 +122,17 @@ __device__ __forceinline__ Bracket hunt_f(const float* g, int n, float x, int h)
 // that inverts e_path also brackets u_eq in the column row (the rows are
 // monotone), and u_eq + du usually stays inside it: then the emissivity is
 // interpolated from the four entries already loaded, with no second search.
-// The bracket is the same either way, so the value is too.
-__device__ __forceinline__ float corner_eps(const RowF& r, bool cga, float e_path, float du,
-                                            float ucg, unsigned short& hu, unsigned short& he) {
+// The bracket is the same either way, so the value is too.  h is the
+// search hint carried along the path: of the emissivity-row search in EGA,
+// of the column-row search in CGA (EGA's column search starts from the
+// emissivity bracket, or from the row start below the table).
+template <bool CGA>
+__device__ __forceinline__ float corner_eps(const RowF& r, float e_path, float du, float ucg,
+                                            unsigned short& h) {
   float uq;
   int ib = -1;
   float u_lo = 0.f, u_hi = 0.f, e_lo = 0.f, e_hi = 0.f;
-  if (cga) {
+  if (CGA) {
     uq = ucg;
   } else {
     if (e_path < r.e0) {
@@ -137,8 +141,8 @@ __device__ __forceinline__ float corner_eps(const RowF& r, bool cga, float e_pat
       const float a = log1pf(-r.en) / r.un;
       uq = log1pf(-e_path) / a;
     } else {
-      const Bracket k = hunt_f(r.e, r.n, e_path, he);
-      he = (unsigned short)k.i;
+      const Bracket k = hunt_f(r.e, r.n, e_path, h);
+      h = (unsigned short)k.i;
       ib = k.i;
       e_lo = k.a;
       e_hi = k.b;
@@ -153,12 +157,10 @@ __device__ __forceinline__ float corner_eps(const RowF& r, bool cga, float e_pat
     const float a = log1pf(-r.en) / r.un;
     return -expm1f(a * uq);
   }
-  if (ib >= 0 && uq >= u_lo && uq < u_hi) {
-    hu = (unsigned short)ib;
+  if (!CGA && ib >= 0 && uq >= u_lo && uq < u_hi)
     return e_lo + (e_hi - e_lo) / (u_hi - u_lo) * (uq - u_lo);
-  }
-  const Bracket k = hunt_f(r.u, r.n, uq, ib >= 0 ? ib : (int)hu);
-  hu = (unsigned short)k.i;
+  const Bracket k = hunt_f(r.u, r.n, uq, CGA ? (int)h : (ib >= 0 ? ib : 0));
+  if (CGA) h = (unsigned short)k.i;
   const float ya = __ldg(r.e + k.i), yb = __ldg(r.e + k.i + 1);
   return ya + (yb - ya) / (k.b - k.a) * (uq - k.a);
 }
@@ -253,7 +255,7 @@ __device__ __forceinline__ Bracket pbracket_f(const float* g, int n, float x, in
   return Bracket{i, __ldg(g + i), __ldg(g + i + 1)};
 }
 
-constexpr int kStateWords = 7;  // t, e, ipr, 2 words of u hints, 2 of eps hints
+constexpr int kStateWords = 5;  // t, e, ipr, 2 words of 16-bit corner hints
 
 // Per (channel, emitter) state carried along the path: transmittance t and
 // emissivity e of the extended path (each accurate where it is small), the
@@ -261,7 +263,7 @@ constexpr int kStateWords = 7;  // t, e, ipr, 2 words of u hints, 2 of eps hints
 struct GasState {
   float t, e;
   int ipr;
-  unsigned short hu[4], he[4];
+  unsigned short h[4];
 };
 
 // One (channel, emitter) at one LOS point (intpol_tbl_ega / intpol_tbl_cga,
@@ -269,9 +271,11 @@ struct GasState {
 // the reference's segment transmittance becomes zero.
 // brw: packed bracket precomputed for the LOS point (grids shared by all
 // channels), or kNoBracket | 1 to search here.
-__device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, bool cga, float pq,
+template <bool CGA>
+__device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, float pq,
                                            float tq, float du, float ucg, unsigned brw,
                                            GasState& s, bool& sat) {
+  constexpr bool cga = CGA;
   const bool pre = brw != (kNoBracket | 1u);
   if (pre && brw == kNoBracket) return 0.f;   // np < 30
   const float* pg = T.pf + dg * T.tp;
@@ -307,17 +311,17 @@ __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, bool c
     it0 = bracket_regf(T.tf + (dg * T.tp + ipr) * T.tt, nt0, tq);
     it1 = bracket_regf(T.tf + (dg * T.tp + ipr + 1) * T.tt, nt1, tq);
   }
-  const float* t0g = T.tf + (dg * T.tp + ipr) * T.tt;
-  const float* t1g = t0g + T.tt;
-  const RowF r00 = rowf_at(T, dg, ipr, it0), r01 = rowf_at(T, dg, ipr, it0 + 1);
-  const RowF r10 = rowf_at(T, dg, ipr + 1, it1), r11 = rowf_at(T, dg, ipr + 1, it1 + 1);
+  const unsigned rp = (unsigned)dg * (unsigned)T.tp + (unsigned)ipr;
+  const unsigned ra = rp * (unsigned)T.tt + (unsigned)it0;
+  const unsigned rc = (rp + 1u) * (unsigned)T.tt + (unsigned)it1;
+  const RowF r00 = rowf_at(T, ra), r01 = rowf_at(T, ra + 1u);
+  const RowF r10 = rowf_at(T, rc), r11 = rowf_at(T, rc + 1u);
   if (r00.n < 2 || r01.n < 2 || r10.n < 2 || r11.n < 2) return 0.f;
-  const float e00 = corner_eps(r00, cga, s.e, du, ucg, s.hu[0], s.he[0]);
-  const float e01 = corner_eps(r01, cga, s.e, du, ucg, s.hu[1], s.he[1]);
-  const float e10 = corner_eps(r10, cga, s.e, du, ucg, s.hu[2], s.he[2]);
-  const float e11 = corner_eps(r11, cga, s.e, du, ucg, s.hu[3], s.he[3]);
-  const float ta = __ldg(t0g + it0), tb = __ldg(t0g + it0 + 1);
-  const float tc = __ldg(t1g + it1), td = __ldg(t1g + it1 + 1);
+  const float e00 = corner_eps<CGA>(r00, s.e, du, ucg, s.h[0]);
+  const float e01 = corner_eps<CGA>(r01, s.e, du, ucg, s.h[1]);
+  const float e10 = corner_eps<CGA>(r10, s.e, du, ucg, s.h[2]);
+  const float e11 = corner_eps<CGA>(r11, s.e, du, ucg, s.h[3]);
+  const float ta = r00.t, tb = r01.t, tc = r10.t, td = r11.t;
   const float ea = e00 + (e01 - e00) / (tb - ta) * (tq - ta);
   const float eb = e10 + (e11 - e10) / (td - tc) * (tq - tc);
   float w;
@@ -342,7 +346,7 @@ __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, bool c
 // through L1 into L2.
 // MINB is the minimum number of resident blocks per SM requested from the
 // register allocator (1 = no cap); the variants are chosen by the autotuner.
-template <int MINB>
+template <int MINB, bool CGA>
 __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, ChanDev ch,
                                                           BatchDev b, LosDev L, MixedPlan P,
                                                           float* refl) {
@@ -358,7 +362,7 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
   const int n = r >= 0 ? L.count[r] : 0;
   const Fields F = fields_of(c, P.brmask);
   const float* base = P.data + P.toff[tile] * (long long)F.n * 32 + lane;
-  const bool cga = c.formod == 0;
+  constexpr bool cga = CGA;
   const double nud = ch.nu[id];
   const float nu = (float)nud;
 
@@ -404,11 +408,9 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
     st.ipr = (int)q[2 * nth];
 #pragma unroll
     for (int k = 0; k < 2; k++) {
-      const unsigned hu = q[(3 + k) * nth], he = q[(5 + k) * nth];
-      st.hu[2 * k] = (unsigned short)(hu & 0xffffu);
-      st.hu[2 * k + 1] = (unsigned short)(hu >> 16);
-      st.he[2 * k] = (unsigned short)(he & 0xffffu);
-      st.he[2 * k + 1] = (unsigned short)(he >> 16);
+      const unsigned hw = q[(3 + k) * nth];
+      st.h[2 * k] = (unsigned short)(hw & 0xffffu);
+      st.h[2 * k + 1] = (unsigned short)(hw >> 16);
     }
     return st;
   };
@@ -418,10 +420,8 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
     q[nth] = __float_as_uint(st.e);
     q[2 * nth] = (unsigned)st.ipr;
 #pragma unroll
-    for (int k = 0; k < 2; k++) {
-      q[(3 + k) * nth] = (unsigned)st.hu[2 * k] | ((unsigned)st.hu[2 * k + 1] << 16);
-      q[(5 + k) * nth] = (unsigned)st.he[2 * k] | ((unsigned)st.he[2 * k + 1] << 16);
-    }
+    for (int k = 0; k < 2; k++)
+      q[(3 + k) * nth] = (unsigned)st.h[2 * k] | ((unsigned)st.h[2 * k + 1] << 16);
   };
   for (int g = 0; g < ng; g++) {
     GasState st;
@@ -429,10 +429,7 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
     st.e = 0.f;
     st.ipr = -1;
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      st.hu[k] = 0;
-      st.he[k] = 0;
-    }
+    for (int k = 0; k < 4; k++) st.h[k] = 0;
     sstore(g, st);
   }
   float rad = 0.f, comp = 0.f, tau = 1.f;
@@ -454,7 +451,7 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
       const unsigned brw = ((P.brmask >> g) & 1u) ? __float_as_uint(f[(F.br0 + g) * 32])
                                                    : (kNoBracket | 1u);
       GasState st = sload(g);
-      const float eg = gas_eps_f(T, dg0 + g, cga, pq, tq, du, ucg, brw, st, sat);
+      const float eg = gas_eps_f<CGA>(T, dg0 + g, pq, tq, du, ucg, brw, st, sat);
       sstore(g, st);
       E = E + (1.f - E) * eg;
     }
@@ -569,8 +566,10 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
 
 // First and last entries of every table row in one float4 (rows with fewer
 // than two entries are never interpolated and get zeros).
+// Row records of the mixed path, two float4 per row (ip, it):
+// {u[0], u[n-1], eps[0], eps[n-1]} and {n (int bits), t[ip][it], 0, 0}.
 __global__ void k_rowmeta(long long nrow, int tu, const int* nu, const float* u, const float* e,
-                          float4* meta) {
+                          const float* tf, float4* meta) {
   const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrow) return;
   const int n = nu[r];
@@ -580,13 +579,15 @@ __global__ void k_rowmeta(long long nrow, int tu, const int* nu, const float* u,
     const float* er = e + r * tu;
     m = make_float4(ur[0], ur[n - 1], er[0], er[n - 1]);
   }
-  meta[r] = m;
+  meta[2 * r] = m;
+  meta[2 * r + 1] = make_float4(__int_as_float(n), tf[r], 0.f, 0.f);
 }
 
 void launch_rowmeta(long long nrow, int tu, const int* nu, const float* u, const float* e,
-                    float4* meta, cudaStream_t s) {
+                    const float* tf, float4* meta, cudaStream_t s) {
   const int bs = 256;
-  if (nrow > 0) k_rowmeta<<<(unsigned)((nrow + bs - 1) / bs), bs, 0, s>>>(nrow, tu, nu, u, e, meta);
+  if (nrow > 0)
+    k_rowmeta<<<(unsigned)((nrow + bs - 1) / bs), bs, 0, s>>>(nrow, tu, nu, u, e, tf, meta);
 }
 
 __global__ void k_src_to_float(int nd, const double* sr, float* srf) {
@@ -608,7 +609,32 @@ void launch_pack_tiles_n(const CtlDev& c, const TblDev& T, const LosDev& L, cons
   k_pack_tiles<<<(unsigned)((nth + bs - 1) / bs), bs, 0, s>>>(c, T, L, P, total_tile_points);
 }
 
-int path_mixed_variants() { return 4; }
+// register caps of the autotuner's variants (minimum resident blocks per SM)
+int path_mixed_variants() { return 7; }
+
+template <bool CGA>
+void launch_variant(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
+                    const LosDev& L, const MixedPlan& P, float* refl, int variant, unsigned nblk,
+                    size_t smem, cudaStream_t s) {
+  if (smem > 48 * 1024) {  // many emitters: opt in to the larger shared memory
+    cudaFuncSetAttribute(k_path_mixed<1, CGA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_path_mixed<5, CGA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_path_mixed<6, CGA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_path_mixed<4, CGA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_path_mixed<8, CGA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_path_mixed<10, CGA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_path_mixed<12, CGA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  }
+  switch (variant) {
+    case 1: k_path_mixed<5, CGA><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl); break;
+    case 2: k_path_mixed<6, CGA><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl); break;
+    case 3: k_path_mixed<4, CGA><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl); break;
+    case 4: k_path_mixed<8, CGA><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl); break;
+    case 5: k_path_mixed<10, CGA><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl); break;
+    case 6: k_path_mixed<12, CGA><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl); break;
+    default: k_path_mixed<1, CGA><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl); break;
+  }
+}
 
 void launch_path_mixed(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
                        const LosDev& L, const MixedPlan& P, float* refl_scratch, int variant,
@@ -616,18 +642,10 @@ void launch_path_mixed(const CtlDev& c, const TblDev& T, const ChanDev& ch, cons
   const int nchb = (c.nd + 3) / 4;
   const unsigned nblk = (unsigned)((long long)P.ntile * nchb);
   const size_t smem = sizeof(unsigned) * kStateWords * 128 * (size_t)(c.ng > 0 ? c.ng : 1);
-  if (smem > 48 * 1024) {  // more than 13 emitters: opt in to the larger shared memory
-    cudaFuncSetAttribute(k_path_mixed<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_path_mixed<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_path_mixed<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_path_mixed<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  }
-  switch (variant) {
-    case 1: k_path_mixed<5><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl_scratch); break;
-    case 2: k_path_mixed<6><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl_scratch); break;
-    case 3: k_path_mixed<4><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl_scratch); break;
-    default: k_path_mixed<1><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl_scratch); break;
-  }
+  if (c.formod == 0)
+    launch_variant<true>(c, T, ch, b, L, P, refl_scratch, variant, nblk, smem, s);
+  else
+    launch_variant<false>(c, T, ch, b, L, P, refl_scratch, variant, nblk, smem, s);
 }
 
 void launch_src_to_float(int nd, const double* sr, float* srf, cudaStream_t s) {

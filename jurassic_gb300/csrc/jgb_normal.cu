@@ -13,6 +13,10 @@
 // FP64: the same products on the FP64 pipes (the plain reference arithmetic).
 #include <cuda_runtime.h>
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "../../include/jurassic_gb300.h"
 #include "jgb_common.cuh"
 #include "jgb_internal.h"
@@ -27,6 +31,7 @@ constexpr int kChunk = 32;  // rows of K per smem stage
 struct NeDesc {
   int m, n;                 // rows of K, columns of K (state size)
   long long koff, moff, aoff, boff;
+  long long xoff;           // offset of the problem's X planes (m x (n+1))
 };
 
 __device__ __forceinline__ unsigned tf32_of(float x) {
@@ -43,20 +48,46 @@ __device__ __forceinline__ void mma_tf32(float* c, const unsigned* a, const unsi
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-// Element (row, col) of the augmented, weighted matrix X = sqrt(W)[K | dy].
-__device__ __forceinline__ float xval(const double* K, const double* w, const double* dy, int m,
-                                      int n, int row, int col) {
-  if (row >= m || col > n) return 0.f;
-  const double v = col < n ? K[(long long)row * n + col] : dy[row];
-  return (float)(v * w[row]);
+// Exact float -> double widening with integer operations (the FP64 pipe of
+// GB300 is narrow); zero, subnormal, infinite and NaN inputs take the
+// conversion instruction.
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)f;
+  const unsigned long long s = (unsigned long long)(u >> 31) << 63;
+  const unsigned long long ex = (unsigned long long)(e + 896u) << 52;   // rebias 127 -> 1023
+  const unsigned long long mt = (unsigned long long)(u & 0x7fffffu) << 29;
+  return __longlong_as_double((long long)(s | ex | mt));
+}
+
+// X = sqrt(W)[K | dy] of every problem, formed once in FP64 and split into
+// a TF32 high part and an FP32 remainder (row-major m x (n+1) per problem):
+// one block per row, threads over the columns.
+__global__ void k_split_x(const NeDesc* desc, const double* Kall, const double* wall,
+                          const double* dyall, float* xhi, float* xlo) {
+  const NeDesc d = desc[blockIdx.y];
+  const int na = d.n + 1;
+  for (int row = blockIdx.x; row < d.m; row += gridDim.x) {
+    const double wr = wall[d.moff + row];
+    const double* Kr = Kall + d.koff + (long long)row * d.n;
+    const long long o = d.xoff + (long long)row * na;
+    for (int col = threadIdx.x; col < na; col += blockDim.x) {
+      const double v = col < d.n ? Kr[col] : dyall[d.moff + row];
+      const float x = (float)(v * wr);
+      const float hi = __uint_as_float(tf32_of(x));
+      xhi[o + col] = hi;
+      xlo[o + col] = x - hi;
+    }
+  }
 }
 
 // One block: output tile (ti, tj) with ti >= tj of retrieval blockIdx.z.
 // 4 warps in a 2x2 arrangement, each a 32x32 sub-tile = 2 (M16) x 4 (N8)
 // mma tiles.
-__global__ void __launch_bounds__(128) k_normal_3xtf32(const NeDesc* desc, const double* Kall,
-                                                       const double* wall, const double* dyall,
-                                                       double* Aall, double* ball) {
+__global__ void __launch_bounds__(128) k_normal_3xtf32(const NeDesc* desc, const float* xhi,
+                                                       const float* xlo, double* Aall,
+                                                       double* ball) {
   const NeDesc d = desc[blockIdx.z];
   const int na = d.n + 1;  // augmented columns
   const int nt = (na + kTile - 1) / kTile;
@@ -68,9 +99,8 @@ __global__ void __launch_bounds__(128) k_normal_3xtf32(const NeDesc* desc, const
   }
   const int tj = t;
   if (ti >= nt) return;
-  const double* K = Kall + d.koff;
-  const double* w = wall + d.moff;
-  const double* dy = dyall + d.moff;
+  const float* XH = xhi + d.xoff;
+  const float* XL = xlo + d.xoff;
   __shared__ float hi_i[kChunk][kTile + 8], lo_i[kChunk][kTile + 8];  // +8: conflict-free fragment reads
   __shared__ float hi_j[kChunk][kTile + 8], lo_j[kChunk][kTile + 8];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -88,13 +118,13 @@ __global__ void __launch_bounds__(128) k_normal_3xtf32(const NeDesc* desc, const
     __syncthreads();
     for (int idx = threadIdx.x; idx < kChunk * kTile; idx += blockDim.x) {
       const int r = idx / kTile, cidx = idx % kTile;
-      const float xi = xval(K, w, dy, d.m, d.n, k0 + r, ti * kTile + cidx);
-      const float xj = xval(K, w, dy, d.m, d.n, k0 + r, tj * kTile + cidx);
-      const float hi1 = __uint_as_float(tf32_of(xi)), hi2 = __uint_as_float(tf32_of(xj));
-      hi_i[r][cidx] = hi1;
-      lo_i[r][cidx] = xi - hi1;
-      hi_j[r][cidx] = hi2;
-      lo_j[r][cidx] = xj - hi2;
+      const int row = k0 + r, ci = ti * kTile + cidx, cj = tj * kTile + cidx;
+      const bool rin = row < d.m;
+      const long long o = (long long)row * na;
+      hi_i[r][cidx] = (rin && ci < na) ? __ldg(XH + o + ci) : 0.f;
+      lo_i[r][cidx] = (rin && ci < na) ? __ldg(XL + o + ci) : 0.f;
+      hi_j[r][cidx] = (rin && cj < na) ? __ldg(XH + o + cj) : 0.f;
+      lo_j[r][cidx] = (rin && cj < na) ? __ldg(XL + o + cj) : 0.f;
     }
     __syncthreads();
 #pragma unroll
@@ -141,7 +171,7 @@ __global__ void __launch_bounds__(128) k_normal_3xtf32(const NeDesc* desc, const
       for (int c = 0; c < 4; c++) {
         const int row = ti * kTile + wr + a * 16 + g + (c >= 2 ? 8 : 0);
         const int col = tj * kTile + wc + bq * 8 + 2 * tg + (c & 1);
-        const double v = (double)acc[a][bq][c];
+        const double v = f2d_bits(acc[a][bq][c]);
         if (row < d.n && col < d.n) {
           if (row >= col) {
             A[(long long)row * d.n + col] = v;
@@ -184,17 +214,43 @@ __global__ void k_normal_fp64(const NeDesc* desc, const double* Kall, const doub
 
 }  // namespace
 
+// Grow-only scratch for the split X planes, one per device; calls that use
+// it are ordered on their stream (the engine and the entry points run on
+// their context's stream; concurrent streams on one device would share it).
+static float* split_buffer(size_t bytes, cudaStream_t s) {
+  static std::mutex mu;
+  static std::map<int, std::pair<void*, size_t>> bufs;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  auto& b = bufs[dev];
+  if (b.second < bytes) {
+    if (b.first) {
+      cudaStreamSynchronize(s);
+      cudaFree(b.first);
+    }
+    b.first = nullptr;
+    b.second = 0;
+    const size_t want = bytes + bytes / 4;
+    if (cudaMalloc(&b.first, want) != cudaSuccess) return nullptr;
+    b.second = want;
+  }
+  return static_cast<float*>(b.first);
+}
+
 int normal_equations_dev(int nret, const int* m, const int* n, const double* K, const double* w,
                          const double* dy, double* A, double* b, int precision, const int* sel,
                          void* desc_dev, cudaStream_t s) {
   // descriptors of the selected problems (host -> device scratch provided by
   // the caller); offsets follow the concatenation of all nret problems
   NeDesc* hd = new NeDesc[nret];
-  long long ko = 0, mo = 0, ao = 0, bo = 0;
-  int maxtiles = 0, maxn = 0, nsel = 0;
+  long long ko = 0, mo = 0, ao = 0, bo = 0, xo = 0;
+  int maxtiles = 0, maxn = 0, maxm = 0, nsel = 0;
   for (int i = 0; i < nret; i++) {
     if (!sel || sel[i]) {
-      hd[nsel++] = NeDesc{m[i], n[i], ko, mo, ao, bo};
+      hd[nsel++] = NeDesc{m[i], n[i], ko, mo, ao, bo, xo};
+      xo += (long long)m[i] * (n[i] + 1);
+      maxm = m[i] > maxm ? m[i] : maxm;
       const int nt = (n[i] + 1 + kTile - 1) / kTile;
       maxtiles = nt * (nt + 1) / 2 > maxtiles ? nt * (nt + 1) / 2 : maxtiles;
       maxn = n[i] > maxn ? n[i] : maxn;
@@ -217,8 +273,14 @@ int normal_equations_dev(int nret, const int* m, const int* n, const double* K, 
   delete[] hd;
   if (e != cudaSuccess) return JGB_ERR_CUDA;
   if (precision == JGB_MIXED) {
+    // X planes in a grow-only buffer of the current device (held to exit)
+    float* xbuf = split_buffer(sizeof(float) * 2 * (size_t)xo, s);
+    if (!xbuf) return JGB_ERR_CUDA;
+    const NeDesc* dd = static_cast<const NeDesc*>(desc_dev);
+    k_split_x<<<dim3((unsigned)(maxm < 1024 ? maxm : 1024), nsel), 128, 0, s>>>(dd, K, w, dy, xbuf,
+                                                                                  xbuf + xo);
     dim3 grid(maxtiles, 1, nsel);
-    k_normal_3xtf32<<<grid, 128, 0, s>>>(static_cast<const NeDesc*>(desc_dev), K, w, dy, A, b);
+    k_normal_3xtf32<<<grid, 128, 0, s>>>(dd, xbuf, xbuf + xo, A, b);
   } else {
     const long long nel = (long long)maxn * (maxn + 1) / 2 + maxn;
     dim3 grid((unsigned)((nel + 127) / 128 < 4096 ? (nel + 127) / 128 : 4096), nsel);

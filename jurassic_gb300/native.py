@@ -72,7 +72,7 @@ class Stats(C.Structure):
                 ("pack_ms", C.c_double), ("path_ms", C.c_double), ("d2h_ms", C.c_double),
                 ("total_ms", C.c_double), ("los_points", C.c_longlong),
                 ("path_launches", C.c_int), ("path_variant", C.c_int),
-                ("tune_ms", C.c_float * 4)]
+                ("tune_ms", C.c_float * 8)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
