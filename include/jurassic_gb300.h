@@ -236,6 +236,9 @@ typedef struct {
      initialisation forward models + S_a, Jacobians, normal equations +
      gradient, damped trials (Cholesky + forward model + cost), results */
   double rebuild_ms, init_ms, jacobian_ms, normal_ms, trial_ms, finish_ms;
+  /* of trial_ms: forward-model calls (host wall time), and their ray-tracing
+     and path-kernel device times (CUDA events) */
+  double trial_fwd_ms, trial_trace_ms, trial_path_ms;
   int active, queued, done;    /* requests in flight, waiting, finished and not yet collected */
   unsigned long long used_bytes;  /* working-set bytes of the active requests */
 } jgb_engine_stats;

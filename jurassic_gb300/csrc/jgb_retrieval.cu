@@ -1081,8 +1081,18 @@ int lm_iteration(jgb_engine* E, WorkSet& w) {
     k_set_iterate<<<nret, 256, 0, s>>>(nret, w.desc_d, w.levoff, w.elems, w.active, apr_arrays(E, w),
                                         cur_arrays(E, w), w.xi, c.nw, c.ncl, c.nsf);
     ECK(cudaGetLastError());
+    const double tfw = now_ms();
     rc = forward(E, w, trying);
     if (rc) return rc;
+    ECK(cudaStreamSynchronize(s));
+    E->st.trial_fwd_ms += now_ms() - tfw;
+    {
+      float a = 0.f, b = 0.f;
+      cudaEventElapsedTime(&a, x->ev[2], x->ev[3]);
+      cudaEventElapsedTime(&b, x->ev[4], x->ev[5]);
+      E->st.trial_trace_ms += a;
+      E->st.trial_path_ms += b;
+    }
     k_residuals<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, w.xi, w.xa, w.ym, w.yi, w.dx, w.dy);
     k_cost<<<(nret + 63) / 64, 64, 0, s>>>(nret, w.desc_d, w.active, w.dx, w.dy, w.sainv, w.w, w.chisq);
     ECK(cudaMemcpyAsync(cnew.data(), w.chisq, sizeof(double) * nret, cudaMemcpyDeviceToHost, s));

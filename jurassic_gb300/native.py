@@ -87,6 +87,8 @@ class EngineStats(C.Structure):
                 ("jacobians", C.c_ulonglong), ("step_ms", C.c_double),
                 ("rebuild_ms", C.c_double), ("init_ms", C.c_double), ("jacobian_ms", C.c_double),
                 ("normal_ms", C.c_double), ("trial_ms", C.c_double), ("finish_ms", C.c_double),
+                ("trial_fwd_ms", C.c_double), ("trial_trace_ms", C.c_double),
+                ("trial_path_ms", C.c_double),
                 ("active", C.c_int),
                 ("queued", C.c_int), ("done", C.c_int), ("used_bytes", C.c_ulonglong)]
 

@@ -72,5 +72,6 @@ def serve(engine, ctl, requests: Sequence, rate_hz: float, seed: int = 0,
                 engine={k: est[k] for k in ("steps", "rebuilds", "forward_calls", "lm_trials",
                                             "jacobians", "step_ms", "rebuild_ms", "init_ms",
                                             "jacobian_ms", "normal_ms", "trial_ms",
-                                            "finish_ms")},
+                                            "finish_ms", "trial_fwd_ms", "trial_trace_ms",
+                                            "trial_path_ms")},
                 results=results)
