@@ -158,6 +158,21 @@ __global__ void k_widen(int n, const int* a, long long* b) {
   if (i < n) b[i] = a[i];
 }
 
+// Batches of mixed precision with at most this many rays x NLOS points are
+// traced in one pass into fixed per-ray slabs (small batches, e.g. the
+// retrieval's damped trials, are latency-bound and the counting pass would
+// double the ray-tracing time); larger ones count first.
+constexpr long long kSinglePassPoints = 1LL << 23;
+
+// Fixed slabs of LOS points per ray (single-pass tracing): ray r owns
+// points [r*slab, (r+1)*slab) and may fill up to slab of them.
+__global__ void k_slab_offsets(int nray, long long slab, long long* off, int* count) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r > nray) return;
+  off[r] = (long long)r * slab;
+  if (r < nray) count[r] = (int)slab;
+}
+
 __global__ void k_iota(int n, int* v) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) v[i] = i;
@@ -200,9 +215,12 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
   if (c.hydz >= 0) launch_hydrostatic(c, b, const_cast<double*>(b.p), s);
   CK(cudaEventRecord(x->ev[2], s));
 
-  // ray tracing: count, scan, fill
+  // ray tracing: count, scan, fill; or, for a small mixed batch, one fill
+  // pass into fixed slabs of NLOS points per ray (the fill pass counts)
+  const long long slab = c.nlos_max;
+  const bool single = precision == JGB_MIXED && (long long)nray * slab <= kSinglePassPoints;
   CK(x->los_cnt.reserve(sizeof(int) * (size_t)std::max(nray, 1)));
-  CK(x->los_cnt64.reserve(sizeof(long long) * (size_t)std::max(nray, 1)));
+  CK(x->los_cnt64.reserve(sizeof(long long) * (size_t)(nray + 1)));
   CK(x->los_off.reserve(sizeof(long long) * (size_t)(nray + 1)));
   CK(x->los_sft.reserve(sizeof(double) * (size_t)std::max(nray, 1)));
   CK(x->los_ends.reserve(6 * sizeof(double) * (size_t)std::max(nray, 1)));
@@ -215,25 +233,30 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
   L.nw = c.nw;
   L.cga = c.formod == 0;
   ChanDev ch = chan_view(x);
-  if (precision == JGB_MIXED)
-    launch_trace_count_mixed(c, b, L, d_err, s);
-  else
-    launch_trace_count(c, ch, b, L, d_err, s);
-  CK(cudaGetLastError());
   long long* cnt64 = x->los_cnt64.as<long long>();
-  k_widen<<<(nray + 255) / 256, 256, 0, s>>>(nray, L.count, cnt64);
-  CK(cudaMemsetAsync(L.off, 0, sizeof(long long), s));
   size_t tmp_bytes = 0;
-  cub::DeviceScan::InclusiveSum(nullptr, tmp_bytes, cnt64, L.off + 1, nray, s);
-  CK(x->scan_tmp.reserve(tmp_bytes + 16));
-  cub::DeviceScan::InclusiveSum(x->scan_tmp.p, tmp_bytes, cnt64, L.off + 1, nray, s);
   long long total = 0;
   unsigned h_err = 0;
-  CK(cudaMemcpyAsync(&total, L.off + nray, sizeof(long long), cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(&h_err, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
-  if (h_err & kErrObserverBelowSurface) return fail(x, JGB_ERR_SURFACE, "Observer below surface!");
-  if (h_err & kErrLosOverflow) return fail(x, JGB_ERR_LOS, "Too many LOS points!");
+  if (!single) {
+    if (precision == JGB_MIXED)
+      launch_trace_count_mixed(c, b, L, d_err, s);
+    else
+      launch_trace_count(c, ch, b, L, d_err, s);
+    CK(cudaGetLastError());
+    k_widen<<<(nray + 255) / 256, 256, 0, s>>>(nray, L.count, cnt64);
+    CK(cudaMemsetAsync(L.off, 0, sizeof(long long), s));
+    cub::DeviceScan::InclusiveSum(nullptr, tmp_bytes, cnt64, L.off + 1, nray, s);
+    CK(x->scan_tmp.reserve(tmp_bytes + 16));
+    cub::DeviceScan::InclusiveSum(x->scan_tmp.p, tmp_bytes, cnt64, L.off + 1, nray, s);
+    CK(cudaMemcpyAsync(&total, L.off + nray, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&h_err, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (h_err & kErrObserverBelowSurface) return fail(x, JGB_ERR_SURFACE, "Observer below surface!");
+    if (h_err & kErrLosOverflow) return fail(x, JGB_ERR_LOS, "Too many LOS points!");
+  } else {
+    k_slab_offsets<<<(nray + 1 + 255) / 256, 256, 0, s>>>(nray, slab, L.off, L.count);
+    total = (long long)nray * slab;
+  }
   const long long cap = std::max(total, 1LL);
   const int nplanes = 8 + c.ng + c.nw + (c.formod == 0 ? 3 * c.ng : 0);
   CK(x->los_planes.reserve(sizeof(double) * (size_t)cap * nplanes));
@@ -257,6 +280,18 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
   else
     launch_trace_fill(c, ch, b, L, d_err, s);
   CK(cudaGetLastError());
+  if (single) {
+    // the fill pass set the counts: errors and the number of LOS points
+    k_widen<<<(nray + 255) / 256, 256, 0, s>>>(nray, L.count, cnt64);
+    cub::DeviceReduce::Sum(nullptr, tmp_bytes, cnt64, cnt64 + nray, nray, s);
+    CK(x->scan_tmp.reserve(tmp_bytes + 16));
+    cub::DeviceReduce::Sum(x->scan_tmp.p, tmp_bytes, cnt64, cnt64 + nray, nray, s);
+    CK(cudaMemcpyAsync(&total, cnt64 + nray, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&h_err, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (h_err & kErrObserverBelowSurface) return fail(x, JGB_ERR_SURFACE, "Observer below surface!");
+    if (h_err & kErrLosOverflow) return fail(x, JGB_ERR_LOS, "Too many LOS points!");
+  }
   CK(cudaEventRecord(x->ev[3], s));
 
   // with a field of view the path kernels write pencil beams to scratch

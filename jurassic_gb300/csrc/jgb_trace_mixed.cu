@@ -56,7 +56,9 @@ __device__ inline AtmM atm_m(const BatchDev& b, const CtlDev& c, int o) {
   return a;
 }
 
-// One level interval [z_i, z_i+1] of the profile in FP32 form.
+// One level interval [z_i, z_i+1] of the profile in FP32 form.  Points are
+// placed in it by their FP32 offset dl = z - z_i, so checking whether a
+// point (or a refraction sub-point) is still in the interval needs no load.
 struct Lev {
   int i;
   double z0;        // z_i
@@ -65,10 +67,13 @@ struct Lev {
   float sp;         // log(p1/p0)/dz (log-linear p) or (p1-p0)/dz (linear fallback)
   float st;         // (t1-t0)/dz
   bool plog;
+  bool first, last; // lowest / highest interval (extrapolation below / above)
 };
 
 __device__ inline void lev_load(const AtmM& a, int i, Lev& L) {
   L.i = i;
+  L.first = i == 0;
+  L.last = i == a.np - 2;
   L.z0 = a.z[i];
   L.dz = (float)(a.z[i + 1] - a.z[i]);
   L.p0 = (float)a.p[i];
@@ -80,21 +85,24 @@ __device__ inline void lev_load(const AtmM& a, int i, Lev& L) {
   L.st = (L.t1 - L.t0) / L.dz;
 }
 
-// Interval of z (locate_irr semantics: 0 below, np-2 above the grid) with
-// the cached interval as hint.
-__device__ inline void lev_find(const AtmM& a, double z, Lev& L) {
-  const int i = L.i;
-  if (i >= 0) {
-    const bool in = a.z[i] <= z && z < a.z[i + 1];
-    const bool below = i == 0 && z < a.z[0];
-    const bool above = i == a.np - 2 && z >= a.z[a.np - 1];
-    if (in || below || above) return;
-  }
-  lev_load(a, bracket_irr(a.z, a.np, z), L);
+// Is offset dl inside the interval (locate_irr semantics: the lowest
+// interval also takes points below the grid, the highest those above)?
+// Only for an ascending grid; otherwise the caller brackets.
+__device__ inline bool lev_holds(const Lev& L, float dl) {
+  return L.i >= 0 && L.dz > 0.f && (dl >= 0.f || L.first) && (dl < L.dz || L.last);
 }
 
-__device__ inline void lev_pt(const Lev& L, double z, float* p, float* t) {
-  const float dl = (float)(z - L.z0);
+// Interval of z with the cached interval as hint; returns dl = z - z_i.
+__device__ inline float lev_find(const AtmM& a, double z, Lev& L) {
+  if (L.i >= 0) {
+    const float dl = (float)(z - L.z0);
+    if (lev_holds(L, dl)) return dl;
+  }
+  lev_load(a, bracket_irr(a.z, a.np, z), L);
+  return (float)(z - L.z0);
+}
+
+__device__ inline void lev_pt(const Lev& L, float dl, float* p, float* t) {
   *p = L.plog ? L.p0 * expf(L.sp * dl) : L.p0 + L.sp * dl;
   *t = L.t0 + L.st * dl;
 }
@@ -115,9 +123,10 @@ __device__ inline float dz_of(const float* xh, float r, const float* d) {
   return num / (r + sqrtf(r * r + num));
 }
 
-// Lon/lat bookkeeping of the fill pass.
+// Lon/lat bookkeeping of the fill pass (positions of the first and last
+// point and of the neighbours of the lowest one).
 struct GeoKeep {
-  double x_first[3], x_prev[3], x_m1[3], x_p1[3], x_last[3];
+  double x_first[3], x_m1[3], x_p1[3], x_last[3];
   double zmin_seen;
   int imin;
   bool want_p1;
@@ -214,9 +223,9 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
       atomicOr(err, kErrLosOverflow);
       return -1;
     }
-    lev_find(a, z, lv);
+    const float dl = lev_find(a, z, lv);
     float p, t;
-    lev_pt(lv, z, &p, &t);
+    lev_pt(lv, dl, &p, &t);
     if (STORE) {
       const long long s = base + n;
       L.z[s] = z;
@@ -224,7 +233,6 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
       L.t[s] = t;
       L.ds[s] = step;
       const int i = lv.i;
-      const float dl = (float)(z - lv.z0);
       for (int ig = 0; ig < c.ng; ig++) {
         const float q0 = (float)a.q[ig * a.stride + i], q1 = (float)a.q[ig * a.stride + i + 1];
         L.u[ig * L.cap + s] = q0 + (q1 - q0) / lv.dz * dl;
@@ -250,11 +258,9 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
       if (n == 0 || z < gk->zmin_seen) {
         gk->zmin_seen = z;
         gk->imin = n;
-        for (int i2 = 0; i2 < 3; i2++) gk->x_m1[i2] = gk->x_prev[i2];
+        for (int i2 = 0; i2 < 3; i2++) gk->x_m1[i2] = x_last[i2];   // the previous point
         gk->want_p1 = true;
       }
-      for (int i2 = 0; i2 < 3; i2++) gk->x_prev[i2] = x[i2];
-      for (int i2 = 0; i2 < 3; i2++) gk->x_last[i2] = x[i2];
     }
     last_z = z;
     for (int i2 = 0; i2 < 3; i2++) x_last[i2] = x[i2];
@@ -262,6 +268,8 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
     if (stop) {
       if (c.nsf > 0 && a.sft > 0) t = (float)a.sft;
       *sft_out = (stop == 2 ? (c.nsf > 0 && a.sft > 0 ? a.sft : (double)t) : -999);
+      if (STORE)
+        for (int i2 = 0; i2 < 3; i2++) gk->x_last[i2] = x[i2];
       break;
     }
     // refraction (jurassic.c:4388-4415): ex1 = (n ex0 + ds grad N) / |...|
@@ -274,34 +282,40 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
       // midpoint xh = x + ds/2 ex0 and its radial unit vector
       const float d[3] = {0.5f * step * ef[0], 0.5f * step * ef[1], 0.5f * step * ef[2]};
       const float dzh = dz_of(xh, rf, d);
-      const double zh = z + dzh;
       const float rh = rf + dzh, rhinv = 1.f / rh;
       const float xhh[3] = {(xh[0] * rf + d[0]) * rhinv, (xh[1] * rf + d[1]) * rhinv,
                             (xh[2] * rf + d[2]) * rhinv};
+      // midpoint offset in the point's interval (FP64 only when it leaves it)
       Lev lh = lv;
-      lev_find(a, zh, lh);
+      float dlh = dl + dzh;
+      if (!lev_holds(lh, dlh)) dlh = lev_find(a, z + dzh, lh);
       float ph, th;
-      lev_pt(lh, zh, &ph, &th);
+      lev_pt(lh, dlh, &ph, &th);
       float inc[3];
       for (int k = 0; k < 3; k++) {
         float dk[3] = {0.f, 0.f, 0.f};
         dk[k] = h;
-        const float dl = dz_of(xhh, rh, dk);
-        const double zk = zh + dl;
+        const float dlk = dz_of(xhh, rh, dk);
         float dN;
-        Lev lk = lh;
-        lev_find(a, zk, lk);
-        if (lk.i == lh.i) {
-          dN = dN_in(lh, ph, th, (float)(zk - zh));
+        if (lev_holds(lh, dlh + dlk)) {
+          dN = dN_in(lh, ph, th, dlk);
         } else {
-          // split at the level boundary between zh and zk
-          const bool up = lk.i > lh.i;
-          const double zb = up ? a.z[lh.i + 1] : a.z[lh.i];
-          const float d1 = (float)(zb - zh), d2 = (float)(zk - zb);
-          const float dn1 = dN_in(lh, ph, th, d1);
-          float pb, tb;
-          lev_pt(lk, zb, &pb, &tb);
-          dN = dn1 + dN_in(lk, pb, tb, d2);
+          // split at the level boundary between the midpoint and zk
+          const double zh = lh.z0 + (double)dlh, zk = zh + dlk;
+          Lev lk = lh;
+          const float dlk0 = lev_find(a, zk, lk);
+          if (lk.i == lh.i) {
+            dN = dN_in(lh, ph, th, dlk);
+          } else {
+            const bool up = lk.i > lh.i;
+            const double zb = up ? a.z[lh.i + 1] : a.z[lh.i];
+            const float d1 = (float)(zb - zh);
+            const float dn1 = dN_in(lh, ph, th, d1);
+            float pb, tb;
+            const float dlb = (float)(zb - lk.z0);
+            lev_pt(lk, dlb, &pb, &tb);
+            dN = dn1 + dN_in(lk, pb, tb, dlk0 - dlb);
+          }
         }
         inc[k] = step * (dN / h) / nref;
       }
@@ -344,7 +358,10 @@ __global__ void k_trace_count_m(CtlDev c, BatchDev b, LosDev L, unsigned* err) {
 __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, unsigned* err) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= b.nray) return;
-  if (b.obs_skip && b.obs_skip[b.ray_obs[r]]) return;
+  if (b.obs_skip && b.obs_skip[b.ray_obs[r]]) {
+    L.count[r] = 0;
+    return;
+  }
   const AtmM a = atm_m(b, c, b.ray_obs[r]);
   const long long base = L.off[r];
   const int cap = L.count[r];
@@ -353,7 +370,7 @@ __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, unsigned* err) {
   gk.want_p1 = false;
   gk.imin = 0;
   gk.zmin_seen = 0;
-  for (int i = 0; i < 3; i++) gk.x_prev[i] = gk.x_m1[i] = gk.x_p1[i] = gk.x_first[i] = gk.x_last[i] = 0;
+  for (int i = 0; i < 3; i++) gk.x_m1[i] = gk.x_p1[i] = gk.x_first[i] = gk.x_last[i] = 0;
   const int n = walk_m<true>(c, a, b.geo, b.nray, r, L, base, cap, &sft, &gk, err);
   L.sft[r] = sft;
   if (n > 0) L.count[r] = n;
