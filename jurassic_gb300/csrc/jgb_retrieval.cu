@@ -311,14 +311,6 @@ __global__ void k_build_sa(int nret, const RetDesc* d, const int* active, const 
   }
 }
 
-__global__ void k_axpy_state(int nret, const RetDesc* d, const int* active, double sign,
-                             const double* step, double* xv) {
-  const int i = blockIdx.x;
-  if (i >= nret || !active[i]) return;
-  for (int j = threadIdx.x; j < d[i].n; j += blockDim.x)
-    xv[d[i].xo + j] = sign > 0 ? xv[d[i].xo + j] + step[d[i].xo + j] : xv[d[i].xo + j] - step[d[i].xo + j];
-}
-
 __global__ void k_dot_state(int nret, const RetDesc* d, const int* active, const double* a,
                             const double* b, double* out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -366,6 +358,28 @@ __global__ void k_copy_segments(int nseg, const unsigned long long* seg) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nw;
          i += (long long)gridDim.x * blockDim.x)
       dst[i] = src[i];
+  }
+}
+
+// Damped-trial candidates of one request, k = 0..count-1 at cand first+k:
+// the iterate of candidate k is what the sequential loop (retrieval.c:
+// 580-633) would form at trial k after k rejections: x_k = b_k + s_k with
+// b_0 = x and b_{k+1} = x_k - s_k (the rejected step taken back), in the
+// same floating-point operations.  xrest receives b_{k+1}.
+__global__ void k_spec_chain(int nreq, const int* first, const int* count, const RetDesc* d,
+                             double* xi, const double* step, double* xrest) {
+  const int r = blockIdx.x;
+  if (r >= nreq) return;
+  const int c0 = first[r], K = count[r], n = d[c0].n;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    double base = xi[d[c0].xo + j];
+    for (int k = 0; k < K; k++) {
+      const long long o = d[c0 + k].xo + j;
+      const double v = base + step[o];
+      xi[o] = v;
+      base = v - step[o];
+      xrest[o] = base;
+    }
   }
 }
 
@@ -562,6 +576,8 @@ struct jgb_engine {
   std::vector<jgb::Request*> active;
   std::map<unsigned long long, jgb::Request*> done;
   jgb::WorkSet ws[2];
+  jgb::WorkSet cw;              // damped-trial candidates of one round
+  jgb::DevBuf chainbuf;
   int cur = 0;
   bool have_ws = false, dirty = true;
   unsigned long long used = 0;
@@ -706,13 +722,15 @@ int run_segments(jgb_engine* E, const std::vector<unsigned long long>& seg) {
   return JGB_OK;
 }
 
-// Build working set `w` for E->active; requests with slot >= 0 bring their
-// iterate state from `old`.
-int build_workset(jgb_engine* E, WorkSet& w, WorkSet* old) {
+// Build working set `w` for the requests `reqs` (inputs uploaded from their
+// host records); with `old`, requests with slot >= 0 bring their iterate
+// state from it; with `carry`, their slots become their index in `w`.
+int build_workset(jgb_engine* E, WorkSet& w, WorkSet* old, const std::vector<Request*>& reqs,
+                  bool carry) {
   jgb_ctx* x = E->x;
   const CtlDev& c = x->c;
   cudaStream_t s = x->stream;
-  const int nret = (int)E->active.size();
+  const int nret = (int)reqs.size();
   const int nscal = 5 + c.ncl + c.nsf, nplanes = 6 + c.ng + c.nw;
   w.nret = nret;
   FdLayout& H = w.H;
@@ -730,7 +748,7 @@ int build_workset(jgb_engine* E, WorkSet& w, WorkSet* old) {
   w.nvec.assign(nret, 0);
   long long nx = 0, nss = 0;
   for (int i = 0; i < nret; i++) {
-    const Request* q = E->active[i];
+    const Request* q = reqs[i];
     H.lev_off[i + 1] = H.lev_off[i] + q->np;
     H.ray_off[i + 1] = H.ray_off[i] + q->nr;
     H.lay[i] = q->lay;
@@ -758,7 +776,7 @@ int build_workset(jgb_engine* E, WorkSet& w, WorkSet* old) {
   std::vector<int4> elems(nx);
   std::vector<SaElem> sael(nx);
   for (int i = 0; i < nret; i++) {
-    const Request* q = E->active[i];
+    const Request* q = reqs[i];
     const int l0 = H.lev_off[i], r0 = H.ray_off[i];
     for (int k = 0; k < nplanes; k++)
       std::memcpy(&lev[(size_t)k * w.nlev + l0], &q->lev[(size_t)k * q->np], sizeof(double) * q->np);
@@ -852,7 +870,7 @@ int build_workset(jgb_engine* E, WorkSet& w, WorkSet* old) {
   std::vector<int> cnt_keep;
   if (old)
     for (int i = 0; i < nret; i++) {
-      const Request* q = E->active[i];
+      const Request* q = reqs[i];
       const int j = q->slot;
       if (j < 0 || q->state == 0) continue;
       const long long ol = old->H.lev_off[j], orr = old->H.ray_off[j];
@@ -888,13 +906,14 @@ int build_workset(jgb_engine* E, WorkSet& w, WorkSet* old) {
     std::vector<int> oc(old->nray), nc(w.nray, 0);
     ECK(cudaMemcpy(oc.data(), old->cnt, sizeof(int) * old->nray, cudaMemcpyDeviceToHost));
     for (int i : cnt_keep) {
-      const int j = E->active[i]->slot;
-      std::memcpy(&nc[H.ray_off[i]], &oc[old->H.ray_off[j]], sizeof(int) * E->active[i]->nr);
+      const int j = reqs[i]->slot;
+      std::memcpy(&nc[H.ray_off[i]], &oc[old->H.ray_off[j]], sizeof(int) * reqs[i]->nr);
     }
     ECK(cudaMemcpyAsync(w.cnt, nc.data(), sizeof(int) * w.nray, cudaMemcpyHostToDevice, s));
     ECK(cudaStreamSynchronize(s));
   }
-  for (int i = 0; i < nret; i++) E->active[i]->slot = i;
+  if (carry)
+    for (int i = 0; i < nret; i++) reqs[i]->slot = i;
   return JGB_OK;
 }
 
@@ -1026,6 +1045,182 @@ int init_requests(jgb_engine* E, WorkSet& w, const std::vector<int>& F) {
   return jacobian(E, w, J);
 }
 
+// Candidates per request in the first and later rounds of damped trials,
+// and the rays of a first round up to which it takes several.
+constexpr int kTrialFirst = 3, kTrialLater = 4;
+constexpr long long kTrialRays = 2048;
+
+// One round of damped trials (retrieval.c:580-633) for the requests flagged
+// in `trying`.  Request i evaluates up to `kk` damping values at once,
+// lambda_i, 10 lambda_i, 100 lambda_i, ... (at most 20 trials per iteration
+// in all): every candidate is a copy of the request in a candidate working
+// set, with the iterate the sequential loop would form after the preceding
+// rejections (k_spec_chain), and all candidates share one forward-model call.
+// The decisions are then taken in lambda order exactly as the sequential
+// loop takes them (first candidate with chi^2 <= the previous iteration's is
+// accepted), and the state of the accepted candidate, or of the last one if
+// all were rejected, moves back into `w`.  The results are the sequential
+// loop's; only fewer latency-bound forward-model calls are made.
+int trial_round(jgb_engine* E, WorkSet& w, std::vector<int>& trying, std::vector<int>& A,
+                std::vector<int>& trials, int kk) {
+  jgb_ctx* x = E->x;
+  const CtlDev& c = x->c;
+  cudaStream_t s = x->stream;
+  const int nret = w.nret;
+  const int nscal = 5 + c.ncl + c.nsf, nplanes = 6 + c.ng + c.nw;
+  std::vector<Request*> creq;
+  std::vector<int> csrc, first, count, who;
+  std::vector<double> lam;
+  for (int i = 0; i < nret; i++) {
+    if (!trying[i]) continue;
+    Request* q = E->active[i];
+    const int K = std::max(1, std::min(kk, 20 - trials[i]));
+    first.push_back((int)creq.size());
+    count.push_back(K);
+    who.push_back(i);
+    double l = q->lmpar;
+    for (int k = 0; k < K; k++) {
+      creq.push_back(q);
+      csrc.push_back(i);
+      lam.push_back(l);
+      l *= 10;
+    }
+  }
+  const int nc = (int)creq.size(), nq = (int)who.size();
+  if (nc == 0) return JGB_OK;
+  WorkSet& cw = E->cw;
+  int rc = build_workset(E, cw, nullptr, creq, false);
+  if (rc) return rc;
+  std::vector<unsigned long long> seg;
+  auto add = [&](const double* src, double* dst, long long nwords) {
+    if (nwords <= 0) return;
+    seg.push_back((unsigned long long)src);
+    seg.push_back((unsigned long long)dst);
+    seg.push_back((unsigned long long)nwords);
+  };
+  for (int k = 0; k < nc; k++) {
+    const RetDesc& d = w.desc[csrc[k]];
+    const RetDesc& e = cw.desc[k];
+    add(w.xa + d.xo, cw.xa + e.xo, d.n);
+    add(w.xi + d.xo, cw.xi + e.xo, d.n);
+    add(w.bvec + d.xo, cw.bvec + e.xo, d.n);
+    add(w.sainv + d.so, cw.sainv + e.so, (long long)d.n * d.n);
+    add(w.cov + d.so, cw.cov + e.so, (long long)d.n * d.n);
+  }
+  rc = run_segments(E, seg);
+  if (rc) return rc;
+  std::vector<int> all(nc, 1);
+  rc = put_flags(E, cw, all);
+  if (rc) return rc;
+  ECK(cudaMemcpyAsync(cw.lmpar, lam.data(), sizeof(double) * nc, cudaMemcpyHostToDevice, s));
+  k_lm_matrix<<<dim3(64, nc), 256, 0, s>>>(nc, cw.desc_d, cw.active, cw.lmpar, cw.sainv, cw.cov, cw.Amat);
+  k_chol_factor<<<nc, 256, 0, s>>>(nc, cw.desc_d, cw.active, cw.Amat, cw.status);
+  k_chol_solve<<<(nc + 63) / 64, 64, 0, s>>>(nc, cw.desc_d, cw.active, cw.Amat, cw.bvec, cw.step);
+  std::vector<int> fc(2 * (size_t)nq);
+  for (int r = 0; r < nq; r++) {
+    fc[r] = first[r];
+    fc[nq + r] = count[r];
+  }
+  ECK(E->chainbuf.reserve(sizeof(int) * fc.size()));
+  ECK(cudaMemcpyAsync(E->chainbuf.p, fc.data(), sizeof(int) * fc.size(), cudaMemcpyHostToDevice, s));
+  k_spec_chain<<<nq, 128, 0, s>>>(nq, E->chainbuf.as<int>(), E->chainbuf.as<int>() + nq, cw.desc_d,
+                                  cw.xi, cw.step, cw.xfin);
+  k_set_iterate<<<nc, 256, 0, s>>>(nc, cw.desc_d, cw.levoff, cw.elems, cw.active, apr_arrays(E, cw),
+                                    cur_arrays(E, cw), cw.xi, c.nw, c.ncl, c.nsf);
+  ECK(cudaGetLastError());
+  const double tfw = now_ms();
+  rc = forward(E, cw, all);
+  if (rc) return rc;
+  ECK(cudaStreamSynchronize(s));
+  E->st.trial_fwd_ms += now_ms() - tfw;
+  {
+    float a = 0.f, b = 0.f;
+    cudaEventElapsedTime(&a, x->ev[2], x->ev[3]);
+    cudaEventElapsedTime(&b, x->ev[4], x->ev[5]);
+    E->st.trial_trace_ms += a;
+    E->st.trial_path_ms += b;
+  }
+  k_residuals<<<nc, 128, 0, s>>>(nc, cw.desc_d, cw.active, cw.xi, cw.xa, cw.ym, cw.yi, cw.dx, cw.dy);
+  k_cost<<<(nc + 63) / 64, 64, 0, s>>>(nc, cw.desc_d, cw.active, cw.dx, cw.dy, cw.sainv, cw.w, cw.chisq);
+  std::vector<double> cnew(nc);
+  std::vector<int> st(nc);
+  ECK(cudaMemcpyAsync(cnew.data(), cw.chisq, sizeof(double) * nc, cudaMemcpyDeviceToHost, s));
+  ECK(cudaMemcpyAsync(st.data(), cw.status, sizeof(int) * nc, cudaMemcpyDeviceToHost, s));
+  ECK(cudaStreamSynchronize(s));
+  E->st.lm_trials++;
+  // the sequential loop's decisions, candidate by candidate in lambda order
+  // stepped: the iterate keeps the step (accepted, or the trial failed);
+  // otherwise the last rejected step was taken back
+  std::vector<int> chosen(nret, -1), accepted(nret, 0), stepped(nret, 0);
+  for (int r = 0; r < nq; r++) {
+    const int i = who[r];
+    Request* q = E->active[i];
+    for (int k = 0; k < count[r]; k++) {
+      const int cidx = first[r] + k;
+      trials[i]++;
+      if (st[cidx]) {  // normal matrix not positive definite: the request fails
+        q->status = JGB_ERR_NUMERIC;
+        q->state = 2;
+        A[i] = 0;
+        chosen[i] = cidx;
+        stepped[i] = 1;
+        break;
+      }
+      q->chisq = cnew[cidx];
+      chosen[i] = cidx;
+      if (q->chisq > q->chisq_old) {
+        q->lmpar *= 10;
+      } else {
+        q->lmpar /= 10;
+        accepted[i] = stepped[i] = 1;
+        break;
+      }
+    }
+    trying[i] = A[i] && !accepted[i] && trials[i] < 20;
+  }
+  // state of the chosen candidates back into the working set
+  seg.clear();
+  std::vector<int> cnt_c(cw.nray), cnt_w(w.nray);
+  bool any_chosen = false;
+  for (int i = 0; i < nret; i++) {
+    const int k = chosen[i];
+    if (k < 0) continue;
+    any_chosen = true;
+    const Request* q = E->active[i];
+    const RetDesc& d = w.desc[i];
+    const RetDesc& e = cw.desc[k];
+    const long long lw = w.H.lev_off[i], lc = cw.H.lev_off[k];
+    const long long rw = w.H.ray_off[i], rcw = cw.H.ray_off[k];
+    for (int pl = 0; pl < nplanes; pl++)
+      add(cw.cur_lev + pl * cw.nlev + lc, w.cur_lev + pl * w.nlev + lw, q->np);
+    add(cw.cur_scal + (long long)k * nscal, w.cur_scal + (long long)i * nscal, nscal);
+    for (int id = 0; id < c.nd; id++) {
+      add(cw.rad + id * cw.nray + rcw, w.rad + id * w.nray + rw, q->nr);
+      add(cw.tau + id * cw.nray + rcw, w.tau + id * w.nray + rw, q->nr);
+    }
+    for (int pl = 0; pl < 3; pl++) add(cw.tp + pl * cw.nray + rcw, w.tp + pl * w.nray + rw, q->nr);
+    add(cw.yi + e.yo, w.yi + d.yo, d.m);
+    add(cw.dy + e.yo, w.dy + d.yo, d.m);
+    add(cw.dx + e.xo, w.dx + d.xo, d.n);
+    add(cw.step + e.xo, w.step + d.xo, d.n);
+    add((stepped[i] ? cw.xi : cw.xfin) + e.xo, w.xi + d.xo, d.n);
+  }
+  if (!any_chosen) return JGB_OK;
+  rc = run_segments(E, seg);
+  if (rc) return rc;
+  // LOS point counts (they size the chunks of later Jacobians)
+  ECK(cudaMemcpyAsync(cnt_c.data(), cw.cnt, sizeof(int) * cw.nray, cudaMemcpyDeviceToHost, s));
+  ECK(cudaMemcpyAsync(cnt_w.data(), w.cnt, sizeof(int) * w.nray, cudaMemcpyDeviceToHost, s));
+  ECK(cudaStreamSynchronize(s));
+  for (int i = 0; i < nret; i++)
+    if (chosen[i] >= 0)
+      std::memcpy(&cnt_w[w.H.ray_off[i]], &cnt_c[cw.H.ray_off[chosen[i]]],
+                  sizeof(int) * E->active[i]->nr);
+  ECK(cudaMemcpyAsync(w.cnt, cnt_w.data(), sizeof(int) * w.nray, cudaMemcpyHostToDevice, s));
+  ECK(cudaStreamSynchronize(s));
+  return JGB_OK;
+}
+
 // One LM iteration (retrieval.c:559-652) of every iterating request.
 int lm_iteration(jgb_engine* E, WorkSet& w) {
   jgb_ctx* x = E->x;
@@ -1062,66 +1257,23 @@ int lm_iteration(jgb_engine* E, WorkSet& w) {
   ECK(cudaStreamSynchronize(s));
   E->st.normal_ms += now_ms() - t0;
   t0 = now_ms();
-  std::vector<int> trying = A;
-  std::vector<double> lmpar(nret, 0), cnew(nret);
-  std::vector<int> st(nret), reject(nret);
-  for (int it2 = 0; it2 < 20; it2++) {
-    bool anyt = false;
-    for (int i = 0; i < nret; i++) anyt |= trying[i] != 0;
-    if (!anyt) break;
-    for (int i = 0; i < nret; i++) lmpar[i] = E->active[i]->lmpar;
-    rc = put_flags(E, w, trying);
-    if (rc) return rc;
-    ECK(cudaMemcpyAsync(w.lmpar, lmpar.data(), sizeof(double) * nret, cudaMemcpyHostToDevice, s));
-    k_lm_matrix<<<dim3(64, nret), 256, 0, s>>>(nret, w.desc_d, w.active, w.lmpar, w.sainv, w.cov, w.Amat);
-    k_chol_factor<<<nret, 256, 0, s>>>(nret, w.desc_d, w.active, w.Amat, w.status);
-    k_chol_solve<<<(nret + 63) / 64, 64, 0, s>>>(nret, w.desc_d, w.active, w.Amat, w.bvec, w.step);
-    k_axpy_state<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, +1.0, w.step, w.xi);
-    const CtlDev& c = x->c;
-    k_set_iterate<<<nret, 256, 0, s>>>(nret, w.desc_d, w.levoff, w.elems, w.active, apr_arrays(E, w),
-                                        cur_arrays(E, w), w.xi, c.nw, c.ncl, c.nsf);
-    ECK(cudaGetLastError());
-    const double tfw = now_ms();
-    rc = forward(E, w, trying);
-    if (rc) return rc;
-    ECK(cudaStreamSynchronize(s));
-    E->st.trial_fwd_ms += now_ms() - tfw;
-    {
-      float a = 0.f, b = 0.f;
-      cudaEventElapsedTime(&a, x->ev[2], x->ev[3]);
-      cudaEventElapsedTime(&b, x->ev[4], x->ev[5]);
-      E->st.trial_trace_ms += a;
-      E->st.trial_path_ms += b;
-    }
-    k_residuals<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, w.xi, w.xa, w.ym, w.yi, w.dx, w.dy);
-    k_cost<<<(nret + 63) / 64, 64, 0, s>>>(nret, w.desc_d, w.active, w.dx, w.dy, w.sainv, w.w, w.chisq);
-    ECK(cudaMemcpyAsync(cnew.data(), w.chisq, sizeof(double) * nret, cudaMemcpyDeviceToHost, s));
-    ECK(cudaMemcpyAsync(st.data(), w.status, sizeof(int) * nret, cudaMemcpyDeviceToHost, s));
-    ECK(cudaStreamSynchronize(s));
-    E->st.lm_trials++;
-    for (int i = 0; i < nret; i++) {
-      reject[i] = 0;
-      if (!trying[i]) continue;
-      Request* q = E->active[i];
-      if (st[i]) {  // normal matrix not positive definite: the request fails
-        q->status = JGB_ERR_NUMERIC;
-        q->state = 2;
-        trying[i] = 0;
-        A[i] = 0;
-        continue;
+  // damped trials in rounds of candidates: several damping values per
+  // request while the candidates of a round stay few enough rays for the
+  // forward model to remain latency-bound, else one
+  std::vector<int> trying = A, trials(nret, 0);
+  for (int round = 0;; round++) {
+    long long rays = 0;
+    int ntry = 0;
+    for (int i = 0; i < nret; i++)
+      if (trying[i]) {
+        rays += E->active[i]->nr;
+        ntry++;
       }
-      q->chisq = cnew[i];
-      if (q->chisq > q->chisq_old) {
-        q->lmpar *= 10;
-        reject[i] = 1;
-      } else {
-        q->lmpar /= 10;
-      }
-    }
-    rc = put_flags(E, w, reject);
+    if (ntry == 0) break;
+    int kk = round ? kTrialLater : kTrialFirst;
+    while (kk > 1 && rays * kk > kTrialRays) kk--;
+    rc = trial_round(E, w, trying, A, trials, kk);
     if (rc) return rc;
-    k_axpy_state<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, -1.0, w.step, w.xi);
-    for (int i = 0; i < nret; i++) trying[i] = reject[i];
   }
   E->st.trial_ms += now_ms() - t0;
   rc = put_flags(E, w, A);
@@ -1292,7 +1444,7 @@ int engine_step(jgb_engine* E) {
   if (E->dirty) {
     const double tb = now_ms();
     WorkSet& nw = E->ws[1 - E->cur];
-    int rc = build_workset(E, nw, E->have_ws ? &E->ws[E->cur] : nullptr);
+    int rc = build_workset(E, nw, E->have_ws ? &E->ws[E->cur] : nullptr, E->active, true);
     if (rc) return rc;
     ECK(cudaStreamSynchronize(x->stream));
     E->st.rebuild_ms += now_ms() - tb;
