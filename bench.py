@@ -519,11 +519,12 @@ def main():
     d2h = fields["rad"].nbytes + fields["tau"].nbytes + fields["tp"].nbytes
     for _ in range(max(1, args.warmup - 1)):
         ctx.formod_batch_ptrs(hb, b.nobs, native.MIXED, device=False)
-    e2e_ms = []
+    e2e_ms, e2e_st = [], []
     for _ in range(args.steps):
         t0 = time.perf_counter()
         ctx.formod_batch_ptrs(hb, b.nobs, native.MIXED, device=False)
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
+        e2e_st.append(ctx.stats())
     e2e_value = units * world / (allmax(pg, statistics.mean(e2e_ms)) / 1e3)
 
     # ---- plain FP64 GPU form ----
@@ -565,6 +566,7 @@ def main():
                            "l2_policy": "inputs and tables larger than L2 (129 MB); no flush",
                            "parallelism": "replicas" if world > 1 else "single GPU"},
                 "stage_ms": {k: stats[k] for k in ("hydro_ms", "trace_ms", "pack_ms", "path_ms")},
+                "trace_passes": stats["trace_passes"],
                 "autotune": {"path_variant": stats["path_variant"], "variant_ms": stats["tune_ms"][:7],
                              "variants": ["no register cap", "5 blocks/SM (<=102 regs)",
                                           "6 blocks/SM (<=85 regs)", "4 blocks/SM (<=128 regs)",
@@ -572,7 +574,9 @@ def main():
                                           "12 blocks/SM (<=42 regs)"]},
                 "wall_s_timed": wall,
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                        "d2h_bytes_per_step": int(d2h), "ms_per_step": statistics.mean(e2e_ms)},
+                        "d2h_bytes_per_step": int(d2h), "ms_per_step": statistics.mean(e2e_ms),
+                        "stage_ms": {k: statistics.mean(st[k] for st in e2e_st)
+                                     for k in ("h2d_ms", "d2h_ms", "path_ms", "total_ms")}},
                 "fp64": None if fp64_value is None else {
                     "value": fp64_value, "unit": UNIT, "ms_per_step": statistics.mean(fp64_ms),
                     "speedup_mixed_over_fp64": value / fp64_value},

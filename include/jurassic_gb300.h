@@ -92,6 +92,10 @@ typedef struct {
   int path_launches;             /* kernels launched by the last call */
   int path_variant;              /* mixed path kernel variant chosen by the autotuner */
   float tune_ms[8];              /* autotuner timings of the variants [ms] */
+  int trace_passes;              /* ray-tracing passes over the batch: 1 = one
+                                    pass, 2 = count + fill, 3 = a capacity
+                                    bound was exceeded and the rays were
+                                    counted */
 } jgb_stats;
 
 /* Context: replaces the process-global table state initialised by the first
@@ -116,6 +120,14 @@ int jgb_set_table(jgb_ctx *ctx, int id, int ig, int np, const double *p, const i
    over view-point altitude before BT conversion and masking.  n = 0 turns it
    off.  Not available in jgb_formod_batch_dev_noalloc. */
 int jgb_set_fov(jgb_ctx *ctx, int n, const double *dz, const double *w);
+
+/* Mixed-precision ray tracing of a batch larger than 2^23 / NLOS rays runs
+   in one pass into per-ray capacities from a geometric bound of the LOS
+   points (a ray that outgrows its capacity makes the batch count its rays
+   first, as FP64 always does).  scale multiplies the bound (memory against
+   the chance of a second pass); 0 always counts first.  Default 1.  The
+   results do not depend on it. */
+int jgb_set_los_bound_scale(jgb_ctx *ctx, double scale);
 
 /* Source function of channel id from its filter function
    (init_srcfunc, jurassic.c:3631-3681), computed on the device. */

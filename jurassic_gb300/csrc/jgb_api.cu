@@ -215,10 +215,15 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
   if (c.hydz >= 0) launch_hydrostatic(c, b, const_cast<double*>(b.p), s);
   CK(cudaEventRecord(x->ev[2], s));
 
-  // ray tracing: count, scan, fill; or, for a small mixed batch, one fill
-  // pass into fixed slabs of NLOS points per ray (the fill pass counts)
+  // ray tracing.  Mixed precision traces in one pass: a small batch into
+  // fixed slabs of NLOS points per ray, a large one into capacities from a
+  // geometric bound of every ray's LOS points; if a ray outgrows its bound,
+  // or in FP64, the rays are counted first (count, scan, fill).
   const long long slab = c.nlos_max;
-  const bool single = precision == JGB_MIXED && (long long)nray * slab <= kSinglePassPoints;
+  enum { kSlab, kBound, kCount } mode =
+      precision != JGB_MIXED ? kCount
+      : (long long)nray * slab <= kSinglePassPoints ? kSlab
+      : x->los_bound_scale > 0 ? kBound : kCount;
   CK(x->los_cnt.reserve(sizeof(int) * (size_t)std::max(nray, 1)));
   CK(x->los_cnt64.reserve(sizeof(long long) * (size_t)(nray + 1)));
   CK(x->los_off.reserve(sizeof(long long) * (size_t)(nray + 1)));
@@ -235,53 +240,61 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
   ChanDev ch = chan_view(x);
   long long* cnt64 = x->los_cnt64.as<long long>();
   size_t tmp_bytes = 0;
-  long long total = 0;
+  long long total = 0, cap = 1;
   unsigned h_err = 0;
-  if (!single) {
+  int passes = 0;
+  for (;;) {
+    if (mode == kSlab) {
+      k_slab_offsets<<<(nray + 1 + 255) / 256, 256, 0, s>>>(nray, slab, L.off, L.count);
+      total = (long long)nray * slab;
+    } else {
+      // per-ray capacities (bound) or exact counts, then their offsets
+      if (mode == kBound)
+        launch_los_bound_mixed(c, b, x->los_bound_scale, L.count, s);
+      else if (precision == JGB_MIXED)
+        launch_trace_count_mixed(c, b, L, d_err, s);
+      else
+        launch_trace_count(c, ch, b, L, d_err, s);
+      CK(cudaGetLastError());
+      passes += mode == kCount;
+      k_widen<<<(nray + 255) / 256, 256, 0, s>>>(nray, L.count, cnt64);
+      CK(cudaMemsetAsync(L.off, 0, sizeof(long long), s));
+      cub::DeviceScan::InclusiveSum(nullptr, tmp_bytes, cnt64, L.off + 1, nray, s);
+      CK(x->scan_tmp.reserve(tmp_bytes + 16));
+      cub::DeviceScan::InclusiveSum(x->scan_tmp.p, tmp_bytes, cnt64, L.off + 1, nray, s);
+      CK(cudaMemcpyAsync(&total, L.off + nray, sizeof(long long), cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(&h_err, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      if (h_err & kErrObserverBelowSurface) return fail(x, JGB_ERR_SURFACE, "Observer below surface!");
+      if (h_err & kErrLosOverflow) return fail(x, JGB_ERR_LOS, "Too many LOS points!");
+    }
+    cap = std::max(total, 1LL);
+    const int nplanes = 8 + c.ng + c.nw + (c.formod == 0 ? 3 * c.ng : 0);
+    CK(x->los_planes.reserve(sizeof(double) * (size_t)cap * nplanes));
+    double* P = x->los_planes.as<double>();
+    L.cap = cap;
+    L.z = P + 0 * cap;
+    L.lon = P + 1 * cap;
+    L.lat = P + 2 * cap;
+    L.p = P + 3 * cap;
+    L.t = P + 4 * cap;
+    L.ds = P + 5 * cap;
+    L.aux = P + 6 * cap;
+    L.qh2o = P + 7 * cap;
+    L.u = P + 8 * cap;
+    L.kw = L.u + (long long)c.ng * cap;
+    L.cgp = L.kw + (long long)c.nw * cap;
+    L.cgt = L.cgp + (long long)c.ng * cap;
+    L.cgu = L.cgt + (long long)c.ng * cap;
     if (precision == JGB_MIXED)
-      launch_trace_count_mixed(c, b, L, d_err, s);
+      launch_trace_fill_mixed(c, b, L, d_err, s);
     else
-      launch_trace_count(c, ch, b, L, d_err, s);
+      launch_trace_fill(c, ch, b, L, d_err, s);
     CK(cudaGetLastError());
-    k_widen<<<(nray + 255) / 256, 256, 0, s>>>(nray, L.count, cnt64);
-    CK(cudaMemsetAsync(L.off, 0, sizeof(long long), s));
-    cub::DeviceScan::InclusiveSum(nullptr, tmp_bytes, cnt64, L.off + 1, nray, s);
-    CK(x->scan_tmp.reserve(tmp_bytes + 16));
-    cub::DeviceScan::InclusiveSum(x->scan_tmp.p, tmp_bytes, cnt64, L.off + 1, nray, s);
-    CK(cudaMemcpyAsync(&total, L.off + nray, sizeof(long long), cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(&h_err, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    if (h_err & kErrObserverBelowSurface) return fail(x, JGB_ERR_SURFACE, "Observer below surface!");
-    if (h_err & kErrLosOverflow) return fail(x, JGB_ERR_LOS, "Too many LOS points!");
-  } else {
-    k_slab_offsets<<<(nray + 1 + 255) / 256, 256, 0, s>>>(nray, slab, L.off, L.count);
-    total = (long long)nray * slab;
-  }
-  const long long cap = std::max(total, 1LL);
-  const int nplanes = 8 + c.ng + c.nw + (c.formod == 0 ? 3 * c.ng : 0);
-  CK(x->los_planes.reserve(sizeof(double) * (size_t)cap * nplanes));
-  double* P = x->los_planes.as<double>();
-  L.cap = cap;
-  L.z = P + 0 * cap;
-  L.lon = P + 1 * cap;
-  L.lat = P + 2 * cap;
-  L.p = P + 3 * cap;
-  L.t = P + 4 * cap;
-  L.ds = P + 5 * cap;
-  L.aux = P + 6 * cap;
-  L.qh2o = P + 7 * cap;
-  L.u = P + 8 * cap;
-  L.kw = L.u + (long long)c.ng * cap;
-  L.cgp = L.kw + (long long)c.nw * cap;
-  L.cgt = L.cgp + (long long)c.ng * cap;
-  L.cgu = L.cgt + (long long)c.ng * cap;
-  if (precision == JGB_MIXED)
-    launch_trace_fill_mixed(c, b, L, d_err, s);
-  else
-    launch_trace_fill(c, ch, b, L, d_err, s);
-  CK(cudaGetLastError());
-  if (single) {
-    // the fill pass set the counts: errors and the number of LOS points
+    passes++;
+    if (mode == kCount) break;
+    // single pass: the fill pass set the counts; errors and the number of
+    // LOS points
     k_widen<<<(nray + 255) / 256, 256, 0, s>>>(nray, L.count, cnt64);
     cub::DeviceReduce::Sum(nullptr, tmp_bytes, cnt64, cnt64 + nray, nray, s);
     CK(x->scan_tmp.reserve(tmp_bytes + 16));
@@ -291,6 +304,12 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
     CK(cudaStreamSynchronize(s));
     if (h_err & kErrObserverBelowSurface) return fail(x, JGB_ERR_SURFACE, "Observer below surface!");
     if (h_err & kErrLosOverflow) return fail(x, JGB_ERR_LOS, "Too many LOS points!");
+    if (h_err & kErrSlabOverflow) {  // a bound was too small: count exactly
+      CK(cudaMemsetAsync(d_err, 0, sizeof(unsigned), s));
+      mode = kCount;
+      continue;
+    }
+    break;
   }
   CK(cudaEventRecord(x->ev[3], s));
 
@@ -427,6 +446,7 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
   }
   CK(cudaEventRecord(x->ev[5], s));
   x->stats.los_points = total;
+  x->stats.trace_passes = passes;
   x->stats.path_launches = launches;
   x->stats.path_variant = x->path_variant;
   for (int v = 0; v < 8; v++) x->stats.tune_ms[v] = v < (int)x->tune_ms.size() ? x->tune_ms[v] : 0.f;
@@ -985,6 +1005,12 @@ int jgb_set_table(jgb_ctx* x, int id, int ig, int np, const double* p, const int
                     eps + (size_t)ip * tt_cap * tu_cap, sizeof(float) * tu_cap,
                     sizeof(float) * w, ntt, cudaMemcpyHostToDevice));
   }
+  return JGB_OK;
+}
+
+int jgb_set_los_bound_scale(jgb_ctx* x, double scale) {
+  if (!x || !(scale >= 0) || scale > 1e6) return fail(x, JGB_ERR_ARG, "bad LOS bound scale");
+  x->los_bound_scale = scale;
   return JGB_OK;
 }
 

@@ -33,6 +33,7 @@ enum : unsigned {
   kErrObserverBelowSurface = 2u,
   kErrBadInput = 4u,
   kErrFov = 8u,
+  kErrSlabOverflow = 16u,  // a ray outgrew its estimated capacity (traced again)
 };
 
 // ---------------------------------------------------------------------------

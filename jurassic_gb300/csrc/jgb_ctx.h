@@ -77,6 +77,7 @@ struct jgb_ctx {
       kx_mask, kx_pert, kx_h, kx_ymap, kx_K, kx_base_rayoff, kx_base_levoff;
   cudaEvent_t ev[8] = {};
   int path_variant = -1;  // mixed path kernel variant chosen by the autotuner
+  double los_bound_scale = 1.0;  // factor on the per-ray LOS bound (0: count first)
   std::vector<float> tune_ms;
   jgb_stats stats{};
   std::string err;

@@ -21,6 +21,8 @@ void launch_trace_count_mixed(const CtlDev& c, const BatchDev& b, const LosDev& 
                               cudaStream_t s);
 void launch_trace_fill_mixed(const CtlDev& c, const BatchDev& b, const LosDev& L, unsigned* err,
                              cudaStream_t s);
+void launch_los_bound_mixed(const CtlDev& c, const BatchDev& b, double scale, int* cap,
+                            cudaStream_t s);
 void launch_trace_fill(const CtlDev& c, const ChanDev& ch, const BatchDev& b, const LosDev& L,
                        unsigned* err, cudaStream_t s);
 void launch_path_fp64(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,

@@ -207,7 +207,7 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
     if ((z < zmin || z > zmax) && n > 0) {
       if (!STORE) {
         if (n >= cap) {
-          atomicOr(err, kErrLosOverflow);
+          atomicOr(err, cap < c.nlos_max ? kErrSlabOverflow : kErrLosOverflow);
           return -1;
         }
         return n + 1;
@@ -220,7 +220,7 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
       step = 0.f;
     }
     if (n >= cap) {
-      atomicOr(err, kErrLosOverflow);
+      atomicOr(err, cap < c.nlos_max ? kErrSlabOverflow : kErrLosOverflow);
       return -1;
     }
     const float dl = lev_find(a, z, lv);
@@ -355,6 +355,71 @@ __global__ void k_trace_count_m(CtlDev c, BatchDev b, LosDev L, unsigned* err) {
   L.count[r] = n < 0 ? 0 : n;
 }
 
+// Upper bound of the LOS points of every ray, for tracing a large batch in
+// one pass.  The step rule ds = min(RAYDS, RAYDZ/|cos a|) (jurassic.c:
+// 4278-4287) makes every step either RAYDS long or move the point by RAYDZ
+// along the local vertical, less the curvature term ds^2/(2 r) <=
+// RAYDS^2/(2 RE).  A path of length S through a total altitude change V so
+// takes at most S/RAYDS + V/(RAYDZ - RAYDS^2/(2 RE)) steps, plus the first
+// and the clipped last point.  S and V come from the straight line of sight
+// (entry at the top of the atmosphere, exit at the top or at the lowest
+// level), with 10 % and, with refraction, 4 km of altitude as margins for
+// the bending; the bound is scaled by jgb_set_los_bound_scale.  A ray that
+// still outgrows its bound raises
+// kErrSlabOverflow in the fill pass and the batch is traced again with
+// exact counts, so the bound only decides the memory and the speed.
+__global__ void k_los_bound_m(CtlDev c, BatchDev b, double scale, int* cap) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= b.nray) return;
+  if (b.obs_skip && b.obs_skip[b.ray_obs[r]]) {
+    cap[r] = 0;
+    return;
+  }
+  const AtmM a = atm_m(b, c, b.ray_obs[r]);
+  double zmin = a.z[0], zmax = a.z[0];
+  for (int i = 1; i < a.np; i++) {
+    zmin = fmin(zmin, a.z[i]);
+    zmax = fmax(zmax, a.z[i]);
+  }
+  const long long nr = b.nray;
+  const double* g = b.geo;
+  const double obsz = g[1 * nr + r], vpz = g[4 * nr + r];
+  if (vpz > zmax || obsz < zmin) {  // no LOS, or an error raised by the fill pass
+    cap[r] = 2;
+    return;
+  }
+  double xo[3], xv[3], d[3];
+  to_cart(obsz, g[2 * nr + r], g[3 * nr + r], xo);
+  to_cart(vpz, g[5 * nr + r], g[6 * nr + r], xv);
+  const double dn = sqrt((xv[0] - xo[0]) * (xv[0] - xo[0]) + (xv[1] - xo[1]) * (xv[1] - xo[1]) +
+                         (xv[2] - xo[2]) * (xv[2] - xo[2]));
+  for (int i = 0; i < 3; i++) d[i] = dn > 0 ? (xv[i] - xo[i]) / dn : 0.0;
+  // |xo + s d|^2 = r02 + 2 bb s + s^2
+  const double bb = xo[0] * d[0] + xo[1] * d[1] + xo[2] * d[2];
+  const double r02 = xo[0] * xo[0] + xo[1] * xo[1] + xo[2] * xo[2];
+  const double rt = kRE + zmax, rb = kRE + zmin;
+  const double disc_t = fmax(bb * bb - (r02 - rt * rt), 0.0);
+  const double s_in = r02 > rt * rt ? fmax(-bb - sqrt(disc_t), 0.0) : 0.0;
+  const double r_in = sqrt(fmax(r02 + 2 * bb * s_in + s_in * s_in, 0.0));
+  const double s_t = -bb, rmin = sqrt(fmax(r02 - bb * bb, 0.0));
+  double s_out, V;
+  if (rmin < rb && s_t > s_in) {  // down to the lowest level
+    s_out = -bb - sqrt(fmax(bb * bb - (r02 - rb * rb), 0.0));
+    V = r_in - rb;
+  } else {
+    s_out = -bb + sqrt(disc_t);
+    V = (s_t > s_in && s_t < s_out) ? (r_in - rmin) + (rt - rmin) : fabs(rt - r_in);
+  }
+  const double S = fmax(s_out - s_in, 0.0);
+  double est = c.rayds > 0 ? S / c.rayds : 0.0;
+  if (c.raydz > 0) {
+    const double per = fmax(c.raydz - c.rayds * c.rayds / (2 * kRE), 0.5 * c.raydz);
+    est += (V + (c.refrac ? 4.0 : 0.0)) / per;
+  }
+  const double bound = ceil(scale * 1.1 * est) + 16;
+  cap[r] = bound >= (double)c.nlos_max ? c.nlos_max : (int)bound;
+}
+
 __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, unsigned* err) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= b.nray) return;
@@ -466,6 +531,12 @@ void launch_trace_count_mixed(const CtlDev& c, const BatchDev& b, const LosDev& 
                               cudaStream_t s) {
   const int bs = 64;
   k_trace_count_m<<<(b.nray + bs - 1) / bs, bs, 0, s>>>(c, b, L, err);
+}
+
+void launch_los_bound_mixed(const CtlDev& c, const BatchDev& b, double scale, int* cap,
+                            cudaStream_t s) {
+  const int bs = 128;
+  k_los_bound_m<<<(b.nray + bs - 1) / bs, bs, 0, s>>>(c, b, scale, cap);
 }
 
 void launch_trace_fill_mixed(const CtlDev& c, const BatchDev& b, const LosDev& L, unsigned* err,

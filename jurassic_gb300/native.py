@@ -72,7 +72,7 @@ class Stats(C.Structure):
                 ("pack_ms", C.c_double), ("path_ms", C.c_double), ("d2h_ms", C.c_double),
                 ("total_ms", C.c_double), ("los_points", C.c_longlong),
                 ("path_launches", C.c_int), ("path_variant", C.c_int),
-                ("tune_ms", C.c_float * 8)]
+                ("tune_ms", C.c_float * 8), ("trace_passes", C.c_int)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
@@ -112,6 +112,7 @@ SIGNATURES = {
                                 _fp, C.c_int, C.c_int]),
     "jgb_set_filter": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp]),
     "jgb_set_fov": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp]),
+    "jgb_set_los_bound_scale": (C.c_int, [C.c_void_p, C.c_double]),
     "jgb_set_srcfunc": (C.c_int, [C.c_void_p, _dp]),
     "jgb_get_srcfunc": (C.c_int, [C.c_void_p, _dp, _dp]),
     "jgb_formod": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
@@ -218,6 +219,11 @@ class Context:
         off."""
         dz, w = _d(dz), _d(w)
         self._check(load().jgb_set_fov(self.h, len(dz), _p(dz), _p(w)))
+
+    def set_los_bound_scale(self, scale: float):
+        """Factor on the per-ray LOS-point bound of one-pass mixed ray tracing
+        of large batches (0: always count the rays first)."""
+        self._check(load().jgb_set_los_bound_scale(self.h, float(scale)))
 
     def _check(self, rc):
         if rc != JGB_OK:
