@@ -815,6 +815,11 @@ int jgb_create(const jgb_ctl* ctl, int device, jgb_ctx** out) {
     return JGB_ERR_CUDA;
   }
   for (auto& e : x->ev) cudaEventCreate(&e);
+  for (auto& e : x->pev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  if (cudaStreamCreateWithFlags(&x->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    jgb_destroy(x);
+    return JGB_ERR_CUDA;
+  }
   CtlDev& c = x->c;
   c.ng = ctl->ng;
   c.nd = ctl->nd;
@@ -911,8 +916,12 @@ void jgb_destroy(jgb_ctx* x) {
                     &x->kx_pert, &x->kx_h, &x->kx_ymap, &x->kx_K, &x->kx_base_rayoff,
                     &x->kx_base_levoff};
   for (DevBuf* b : bufs) b->release();
+  if (x->copy_stream) cudaStreamSynchronize(x->copy_stream);
   for (auto& e : x->ev)
     if (e) cudaEventDestroy(e);
+  for (auto& e : x->pev)
+    if (e) cudaEventDestroy(e);
+  if (x->copy_stream) cudaStreamDestroy(x->copy_stream);
   if (x->stream) cudaStreamDestroy(x->stream);
   delete x;
 }
@@ -1068,6 +1077,12 @@ int jgb_get_srcfunc(jgb_ctx* x, double* st, double* sr) {
   return JGB_OK;
 }
 
+// Forward model of a batch in host memory.  A large batch runs as two
+// chunks of whole observations, each a compact sub-batch on the device: the
+// first eighth is copied in and computed while the rest is copied in on the
+// copy stream, and its results go back while the rest is computed, so only
+// the first chunk's inputs and the last chunk's results move while the
+// device waits.  Rays are independent, so the results are those of one batch.
 int jgb_formod_batch(jgb_ctx* x, const jgb_batch* hb, int precision) {
   if (!x || !hb || hb->nobs <= 0) return fail(x, JGB_ERR_ARG, "empty batch");
   if (precision != JGB_FP64 && precision != JGB_MIXED) return fail(x, JGB_ERR_ARG, "precision");
@@ -1075,7 +1090,7 @@ int jgb_formod_batch(jgb_ctx* x, const jgb_batch* hb, int precision) {
   if (rc) return rc;
   cudaSetDevice(x->device);
   const CtlDev& c = x->c;
-  cudaStream_t s = x->stream;
+  cudaStream_t s = x->stream, cs = x->copy_stream;
   const int nobs = hb->nobs;
   const int nlev = hb->lev_off[nobs], nray = hb->ray_off[nobs];
   if (nlev <= 0 || nray <= 0) return fail(x, JGB_ERR_ARG, "no levels or rays");
@@ -1084,8 +1099,19 @@ int jgb_formod_batch(jgb_ctx* x, const jgb_batch* hb, int precision) {
       return fail(x, JGB_ERR_ARG, "an atmosphere needs at least two levels");
   const int nscal = 5 + c.ncl + c.nsf;
   const int nlevf = 6 + c.ng + c.nw;  // time z lon lat p t q[] k[]
-  CK(x->b_levoff.reserve(sizeof(int) * (nobs + 1)));
-  CK(x->b_rayoff.reserve(sizeof(int) * (nobs + 1)));
+  // chunks of observations [ob[k], ob[k+1])
+  int nchunk = 1, ob[3] = {0, nobs, nobs};
+  const double in_bytes = 8.0 * ((double)nlev * nlevf + (double)nobs * nscal + 7.0 * nray +
+                                 (double)c.nd * nray);
+  if (nobs >= 16 && in_bytes >= 64.0 * (1 << 20)) {
+    const int o1 = nobs / 8;
+    if (hb->ray_off[o1] > 0 && hb->ray_off[o1] < nray) {
+      nchunk = 2;
+      ob[1] = o1;
+    }
+  }
+  CK(x->b_levoff.reserve(sizeof(int) * (nobs + 2)));
+  CK(x->b_rayoff.reserve(sizeof(int) * (nobs + 2)));
   CK(x->b_rayobs.reserve(sizeof(int) * nray));
   CK(x->b_lev.reserve(sizeof(double) * (size_t)nlev * nlevf));
   CK(x->b_scal.reserve(sizeof(double) * (size_t)nobs * nscal));
@@ -1094,62 +1120,156 @@ int jgb_formod_batch(jgb_ctx* x, const jgb_batch* hb, int precision) {
   CK(x->b_tau.reserve(sizeof(double) * (size_t)c.nd * nray));
   CK(x->b_tp.reserve(sizeof(double) * 3 * (size_t)nray));
   CK(x->b_mask.reserve((size_t)c.nd * nray));
-  double* lev = x->b_lev.as<double>();
-  BatchDev b{};
-  b.nobs = nobs;
-  b.nlev = nlev;
-  b.nray = nray;
-  b.nscal = nscal;
-  b.lev_off = x->b_levoff.as<int>();
-  b.ray_obs = x->b_rayobs.as<int>();
-  b.time = lev;
-  b.z = lev + (size_t)nlev;
-  b.lon = lev + 2 * (size_t)nlev;
-  b.lat = lev + 3 * (size_t)nlev;
-  b.p = lev + 4 * (size_t)nlev;
-  b.t = lev + 5 * (size_t)nlev;
-  b.q = lev + 6 * (size_t)nlev;
-  b.k = lev + (6 + (size_t)c.ng) * nlev;
-  b.scal = x->b_scal.as<double>();
-  b.geo = x->b_geo.as<double>();
-  b.rad = x->b_rad.as<double>();
-  b.tau = x->b_tau.as<double>();
-  b.tp = x->b_tp.as<double>();
-  b.mask = x->b_mask.as<unsigned char>();
+  struct Chunk {
+    int o0, o1, l0, l1, r0, r1;
+    BatchDev b;
+    int* rayoff;
+    std::vector<int> hlev, hray;  // offsets relative to the chunk
+  };
+  Chunk ck[2];
+  for (int k = 0; k < nchunk; k++) {
+    Chunk& h = ck[k];
+    h.o0 = ob[k];
+    h.o1 = ob[k + 1];
+    h.l0 = hb->lev_off[h.o0];
+    h.l1 = hb->lev_off[h.o1];
+    h.r0 = hb->ray_off[h.o0];
+    h.r1 = hb->ray_off[h.o1];
+    const int no = h.o1 - h.o0, nl = h.l1 - h.l0, nr = h.r1 - h.r0;
+    h.hlev.resize(no + 1);
+    h.hray.resize(no + 1);
+    for (int o = 0; o <= no; o++) {
+      h.hlev[o] = hb->lev_off[h.o0 + o] - h.l0;
+      h.hray[o] = hb->ray_off[h.o0 + o] - h.r0;
+    }
+    double* lev = x->b_lev.as<double>() + (size_t)nlevf * h.l0;  // compact planes of stride nl
+    BatchDev& b = h.b;
+    b = BatchDev{};
+    b.nobs = no;
+    b.nlev = nl;
+    b.nray = nr;
+    b.nscal = nscal;
+    b.lev_off = x->b_levoff.as<int>() + h.o0 + k;
+    h.rayoff = x->b_rayoff.as<int>() + h.o0 + k;
+    b.ray_obs = x->b_rayobs.as<int>() + h.r0;
+    b.time = lev;
+    b.z = lev + (size_t)nl;
+    b.lon = lev + 2 * (size_t)nl;
+    b.lat = lev + 3 * (size_t)nl;
+    b.p = lev + 4 * (size_t)nl;
+    b.t = lev + 5 * (size_t)nl;
+    b.q = lev + 6 * (size_t)nl;
+    b.k = lev + (6 + (size_t)c.ng) * nl;
+    b.scal = x->b_scal.as<double>() + (size_t)nscal * h.o0;
+    b.geo = x->b_geo.as<double>() + 7 * (size_t)h.r0;
+    b.rad = x->b_rad.as<double>() + (size_t)c.nd * h.r0;
+    b.tau = x->b_tau.as<double>() + (size_t)c.nd * h.r0;
+    b.tp = x->b_tp.as<double>() + 3 * (size_t)h.r0;
+    b.mask = x->b_mask.as<unsigned char>() + (size_t)c.nd * h.r0;
+  }
+  const size_t D = sizeof(double);
+  auto upload = [&](const Chunk& h, cudaStream_t st) -> cudaError_t {
+    const BatchDev& b = h.b;
+    const size_t nl = (size_t)b.nlev, nr = (size_t)b.nray, no = (size_t)b.nobs;
+    cudaError_t e = cudaMemcpyAsync((void*)b.lev_off, h.hlev.data(), sizeof(int) * (no + 1),
+                                    cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(h.rayoff, h.hray.data(), sizeof(int) * (no + 1), cudaMemcpyHostToDevice, st);
+    const double* src[6] = {hb->time, hb->z, hb->lon, hb->lat, hb->p, hb->t};
+    const double* dst[6] = {b.time, b.z, b.lon, b.lat, b.p, b.t};
+    for (int i = 0; i < 6 && e == cudaSuccess; i++)
+      e = cudaMemcpyAsync((void*)dst[i], src[i] + h.l0, D * nl, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && c.ng)
+      e = cudaMemcpy2DAsync((void*)b.q, D * nl, hb->q + h.l0, D * nlev, D * nl, c.ng,
+                            cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && c.nw)
+      e = cudaMemcpy2DAsync((void*)b.k, D * nl, hb->k + h.l0, D * nlev, D * nl, c.nw,
+                            cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync((void*)b.scal, hb->scal + (size_t)nscal * h.o0, D * no * nscal,
+                          cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync((void*)b.geo, D * nr, hb->geo + h.r0, D * nray, D * nr, 7,
+                            cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(b.rad, D * nr, hb->rad + h.r0, D * nray, D * nr, c.nd,
+                            cudaMemcpyHostToDevice, st);
+    return e;
+  };
+  auto download = [&](const Chunk& h, cudaStream_t st) -> cudaError_t {
+    const BatchDev& b = h.b;
+    const size_t nr = (size_t)b.nray;
+    cudaError_t e = cudaMemcpy2DAsync(hb->rad + h.r0, D * nray, b.rad, D * nr, D * nr, c.nd,
+                                      cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(hb->tau + h.r0, D * nray, b.tau, D * nr, D * nr, c.nd,
+                            cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(hb->tp + h.r0, D * nray, b.tp, D * nr, D * nr, 3,
+                            cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && c.hydz >= 0)
+      e = cudaMemcpyAsync(hb->p + h.l0, b.p, D * (size_t)b.nlev, cudaMemcpyDeviceToHost, st);
+    return e;
+  };
+  // on an error, let the copy stream finish with the caller's buffers
+  auto bail = [&](int code) {
+    cudaStreamSynchronize(cs);
+    return code;
+  };
   CK(cudaEventRecord(x->ev[0], s));
-  const size_t L = (size_t)nlev * sizeof(double);
-  CK(cudaMemcpyAsync(x->b_levoff.p, hb->lev_off, sizeof(int) * (nobs + 1), cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(x->b_rayoff.p, hb->ray_off, sizeof(int) * (nobs + 1), cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync((void*)b.time, hb->time, L, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync((void*)b.z, hb->z, L, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync((void*)b.lon, hb->lon, L, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync((void*)b.lat, hb->lat, L, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync((void*)b.p, hb->p, L, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync((void*)b.t, hb->t, L, cudaMemcpyHostToDevice, s));
-  if (c.ng) CK(cudaMemcpyAsync((void*)b.q, hb->q, L * c.ng, cudaMemcpyHostToDevice, s));
-  if (c.nw) CK(cudaMemcpyAsync((void*)b.k, hb->k, L * c.nw, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync((void*)b.scal, hb->scal, sizeof(double) * (size_t)nobs * nscal, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync((void*)b.geo, hb->geo, sizeof(double) * 7 * (size_t)nray, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(b.rad, hb->rad, sizeof(double) * (size_t)c.nd * nray, cudaMemcpyHostToDevice, s));
-  k_ray_obs<<<(nobs + 127) / 128, 128, 0, s>>>(nobs, x->b_rayoff.as<int>(), x->b_rayobs.as<int>());
-  const long long nm = (long long)c.nd * nray;
-  k_mask<<<(unsigned)((nm + 255) / 256), 256, 0, s>>>(nm, b.rad, x->b_mask.as<unsigned char>());
-  CK(cudaEventRecord(x->ev[1], s));
-  rc = run_core(x, b, precision, true);
-  if (rc) return rc;
-  CK(cudaMemcpyAsync(hb->rad, b.rad, sizeof(double) * (size_t)c.nd * nray, cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(hb->tau, b.tau, sizeof(double) * (size_t)c.nd * nray, cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(hb->tp, b.tp, sizeof(double) * 3 * (size_t)nray, cudaMemcpyDeviceToHost, s));
-  if (c.hydz >= 0) CK(cudaMemcpyAsync(hb->p, b.p, L, cudaMemcpyDeviceToHost, s));
+  CK(upload(ck[0], s));
+  if (nchunk > 1) {
+    CK(cudaStreamWaitEvent(cs, x->ev[0], 0));
+    CK(upload(ck[1], cs));
+    CK(cudaEventRecord(x->pev[0], cs));
+  }
+  double acc[4] = {0, 0, 0, 0}, h2d_ms = 0;
+  long long los = 0;
+  int launches = 0, passes = 0;
+  for (int k = 0; k < nchunk; k++) {
+    Chunk& h = ck[k];
+    if (k > 0) CK(cudaStreamWaitEvent(s, x->pev[0], 0));
+    const int no = h.b.nobs;
+    k_ray_obs<<<(no + 127) / 128, 128, 0, s>>>(no, h.rayoff, const_cast<int*>(h.b.ray_obs));
+    const long long nm = (long long)c.nd * h.b.nray;
+    k_mask<<<(unsigned)((nm + 255) / 256), 256, 0, s>>>(nm, h.b.rad,
+                                                        const_cast<unsigned char*>(h.b.mask));
+    CK(cudaEventRecord(x->ev[1], s));
+    rc = run_core(x, h.b, precision, true);
+    if (rc) return bail(rc);
+    if (k + 1 < nchunk) {
+      CK(cudaEventRecord(x->pev[1], s));
+      CK(cudaStreamWaitEvent(cs, x->pev[1], 0));
+      CK(download(h, cs));
+      CK(cudaEventRecord(x->pev[2], cs));
+      // the next chunk's first host synchronisation waits for this one anyway
+      CK(cudaEventSynchronize(x->ev[5]));
+      if (k == 0) h2d_ms = elapsed(x->ev[0], x->ev[1]);
+      acc[0] += elapsed(x->ev[1], x->ev[2]);
+      acc[1] += elapsed(x->ev[2], x->ev[3]);
+      acc[2] += elapsed(x->ev[3], x->ev[4]);
+      acc[3] += elapsed(x->ev[4], x->ev[5]);
+      los += x->stats.los_points;
+      launches += x->stats.path_launches;
+      passes = std::max(passes, x->stats.trace_passes);
+    } else {
+      CK(download(h, s));
+    }
+  }
+  if (nchunk > 1) CK(cudaStreamWaitEvent(s, x->pev[2], 0));
   CK(cudaEventRecord(x->ev[6], s));
   CK(cudaStreamSynchronize(s));
-  x->stats.h2d_ms = elapsed(x->ev[0], x->ev[1]);
-  x->stats.hydro_ms = elapsed(x->ev[1], x->ev[2]);
-  x->stats.trace_ms = elapsed(x->ev[2], x->ev[3]);
-  x->stats.pack_ms = elapsed(x->ev[3], x->ev[4]);
-  x->stats.path_ms = elapsed(x->ev[4], x->ev[5]);
+  if (nchunk == 1) h2d_ms = elapsed(x->ev[0], x->ev[1]);
+  x->stats.h2d_ms = h2d_ms;
+  x->stats.hydro_ms = acc[0] + elapsed(x->ev[1], x->ev[2]);
+  x->stats.trace_ms = acc[1] + elapsed(x->ev[2], x->ev[3]);
+  x->stats.pack_ms = acc[2] + elapsed(x->ev[3], x->ev[4]);
+  x->stats.path_ms = acc[3] + elapsed(x->ev[4], x->ev[5]);
   x->stats.d2h_ms = elapsed(x->ev[5], x->ev[6]);
   x->stats.total_ms = elapsed(x->ev[0], x->ev[6]);
+  x->stats.los_points += los;
+  x->stats.path_launches += launches;
+  x->stats.trace_passes = std::max(passes, x->stats.trace_passes);
   return JGB_OK;
 }
 

@@ -76,6 +76,9 @@ struct jgb_ctx {
   jgb::DevBuf kx_levoff, kx_rayoff, kx_rayobs, kx_src, kx_lev, kx_scal, kx_geo, kx_rad, kx_tau, kx_tp,
       kx_mask, kx_pert, kx_h, kx_ymap, kx_K, kx_base_rayoff, kx_base_levoff;
   cudaEvent_t ev[8] = {};
+  // copies of the second chunk of a host batch overlap the first's compute
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t pev[3] = {};
   int path_variant = -1;  // mixed path kernel variant chosen by the autotuner
   double los_bound_scale = 1.0;  // factor on the per-ray LOS bound (0: count first)
   std::vector<float> tune_ms;
