@@ -61,8 +61,7 @@ constexpr unsigned kNoBracket = 0x80000000u;
 // the result does not depend on the hint.
 
 struct RowF {
-  const float* u;
-  const float* e;
+  unsigned off;          // row start in the u and eps arrays
   int n;
   float u0, un, e0, en;  // first/last entries of the row
   float t;               // temperature of the row
@@ -72,9 +71,7 @@ struct RowF {
 // arithmetic (the table upload checks that rows x TU < 2^32).
 __device__ __forceinline__ RowF rowf_at(const TblDev& T, unsigned r) {
   RowF w;
-  const unsigned off = r * (unsigned)T.tu;
-  w.u = T.u + off;
-  w.e = T.eps + off;
+  w.off = r * (unsigned)T.tu;
   const float4 m = __ldg(T.rowmeta + 2 * r), m2 = __ldg(T.rowmeta + 2 * r + 1);
   w.n = __float_as_int(m2.x);
   w.t = m2.y;
@@ -127,8 +124,10 @@ __device__ __forceinline__ Bracket hunt_f(const float* g, int n, float x, int h)
 // of the column-row search in CGA (EGA's column search starts from the
 // emissivity bracket, or from the row start below the table).
 template <bool CGA>
-__device__ __forceinline__ float corner_eps(const RowF& r, float e_path, float du, float ucg,
-                                            unsigned short& h) {
+__device__ __forceinline__ float corner_eps(const TblDev& T, const RowF& r, float e_path, float du,
+                                            float ucg, unsigned short& h) {
+  const float* ru = T.u + r.off;
+  const float* re = T.eps + r.off;
   float uq;
   int ib = -1;
   float u_lo = 0.f, u_hi = 0.f, e_lo = 0.f, e_hi = 0.f;
@@ -141,13 +140,13 @@ __device__ __forceinline__ float corner_eps(const RowF& r, float e_path, float d
       const float a = log1pf(-r.en) / r.un;
       uq = log1pf(-e_path) / a;
     } else {
-      const Bracket k = hunt_f(r.e, r.n, e_path, h);
+      const Bracket k = hunt_f(re, r.n, e_path, h);
       h = (unsigned short)k.i;
       ib = k.i;
       e_lo = k.a;
       e_hi = k.b;
-      u_lo = __ldg(r.u + k.i);
-      u_hi = __ldg(r.u + k.i + 1);
+      u_lo = __ldg(ru + k.i);
+      u_hi = __ldg(ru + k.i + 1);
       uq = u_lo + (u_hi - u_lo) / (e_hi - e_lo) * (e_path - e_lo);
     }
     uq = uq + du;
@@ -159,9 +158,9 @@ __device__ __forceinline__ float corner_eps(const RowF& r, float e_path, float d
   }
   if (!CGA && ib >= 0 && uq >= u_lo && uq < u_hi)
     return e_lo + (e_hi - e_lo) / (u_hi - u_lo) * (uq - u_lo);
-  const Bracket k = hunt_f(r.u, r.n, uq, CGA ? (int)h : (ib >= 0 ? ib : 0));
+  const Bracket k = hunt_f(ru, r.n, uq, CGA ? (int)h : (ib >= 0 ? ib : 0));
   if (CGA) h = (unsigned short)k.i;
-  const float ya = __ldg(r.e + k.i), yb = __ldg(r.e + k.i + 1);
+  const float ya = __ldg(re + k.i), yb = __ldg(re + k.i + 1);
   return ya + (yb - ya) / (k.b - k.a) * (uq - k.a);
 }
 
@@ -256,6 +255,8 @@ __device__ __forceinline__ Bracket pbracket_f(const float* g, int n, float x, in
 }
 
 constexpr int kStateWords = 5;  // t, e, ipr, 2 words of 16-bit corner hints
+constexpr int kChanConsts = 16;  // constants of a warp's channel
+constexpr int kThreadFloats = 2;  // per-thread values kept in shared memory
 
 // Per (channel, emitter) state carried along the path: transmittance t and
 // emissivity e of the extended path (each accurate where it is small), the
@@ -317,10 +318,10 @@ __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, float 
   const RowF r00 = rowf_at(T, ra), r01 = rowf_at(T, ra + 1u);
   const RowF r10 = rowf_at(T, rc), r11 = rowf_at(T, rc + 1u);
   if (r00.n < 2 || r01.n < 2 || r10.n < 2 || r11.n < 2) return 0.f;
-  const float e00 = corner_eps<CGA>(r00, s.e, du, ucg, s.h[0]);
-  const float e01 = corner_eps<CGA>(r01, s.e, du, ucg, s.h[1]);
-  const float e10 = corner_eps<CGA>(r10, s.e, du, ucg, s.h[2]);
-  const float e11 = corner_eps<CGA>(r11, s.e, du, ucg, s.h[3]);
+  const float e00 = corner_eps<CGA>(T, r00, s.e, du, ucg, s.h[0]);
+  const float e01 = corner_eps<CGA>(T, r01, s.e, du, ucg, s.h[1]);
+  const float e10 = corner_eps<CGA>(T, r10, s.e, du, ucg, s.h[2]);
+  const float e11 = corner_eps<CGA>(T, r11, s.e, du, ucg, s.h[3]);
   const float ta = r00.t, tb = r01.t, tc = r10.t, td = r11.t;
   const float ea = e00 + (e01 - e00) / (tb - ta) * (tq - ta);
   const float eb = e10 + (e11 - e10) / (td - tc) * (tq - tc);
@@ -388,18 +389,38 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
   const bool h2o_on = c.ctm_h2o && c.ig_h2o >= 0 && cc[4] != 0;
   const bool n2_on = c.ctm_n2 && cc[8] != 0;
   const bool o2_on = c.ctm_o2 && cc[11] != 0;
-  const float co2_296 = (float)cc[1], co2_260 = (float)cc[2], co2_230 = (float)cc[3];
-  const float h2o_s296 = (float)cc[5], h2o_lr = (float)log(cc[6] > 0 ? cc[6] : 1.0);
-  const float h2o_frn = (float)cc[7];
-  const float n2_b = (float)cc[9], n2_beta = (float)cc[10];
-  const float o2_b = (float)cc[12], o2_beta = (float)cc[13];
-  const float* srf = T.srf + (long long)id * kNS;
   const float st0 = (float)kTMIN, sdt = (float)((kTMAX - kTMIN) / (kNS - 1.0));
 
   // per-emitter path state in shared memory, word-major per thread:
   // sh[(g * kStateWords + w) * blockDim.x + threadIdx.x]
   extern __shared__ unsigned sh_state[];
   const int nth = blockDim.x, tid = threadIdx.x;
+  // behind the state: the channel's constants (kChanConsts words per warp:
+  // continuum coefficients, [11] channel index, [12] window index) and
+  // kThreadFloats per thread (cloud extinction, surface emissivity), read
+  // where used so that they hold no registers across the emitter loop
+  float* const sh_tail = reinterpret_cast<float*>(sh_state + kStateWords * nth * (ng > 0 ? ng : 1));
+  volatile float* kc = sh_tail + warp * kChanConsts;
+  volatile int* kci = reinterpret_cast<volatile int*>(sh_tail + warp * kChanConsts);
+  volatile float* kthr = sh_tail + (nth / 32) * kChanConsts + tid;  // [0], [nth]
+  if (lane == 0) {
+    kc[0] = nu;
+    kc[1] = (float)cc[1];
+    kc[2] = (float)cc[2];
+    kc[3] = (float)cc[3];
+    kc[4] = (float)cc[5];
+    kc[5] = (float)log(cc[6] > 0 ? cc[6] : 1.0);
+    kc[6] = (float)cc[7];
+    kc[7] = (float)cc[9];
+    kc[8] = (float)cc[10];
+    kc[9] = (float)cc[12];
+    kc[10] = (float)cc[13];
+    kci[11] = id;
+    kci[12] = w;
+  }
+  kthr[0] = cloud;
+  kthr[nth] = sfeps;
+  __syncwarp();
   auto sload = [&](int g) {
     const unsigned* q = sh_state + (g * kStateWords) * nth + tid;
     GasState st;
@@ -432,10 +453,9 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
     for (int k = 0; k < 4; k++) st.h[k] = 0;
     sstore(g, st);
   }
+  const long long dg0 = (long long)id * ng;
   float rad = 0.f, comp = 0.f, tau = 1.f;
   const bool do_refl = refl != nullptr && r >= 0 && c.sftype >= 2 && sfeps < 1.f && L.sft[r] > 0;
-  float* sc = do_refl ? refl + 2 * (L.off[r] * c.nd) : nullptr;
-  const long long dg0 = (long long)id * ng;
 
   for (int ip = 0; ip < n; ip++) {
     const float* f = base + (long long)ip * F.n * 32;
@@ -451,15 +471,17 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
       const unsigned brw = ((P.brmask >> g) & 1u) ? __float_as_uint(f[(F.br0 + g) * 32])
                                                    : (kNoBracket | 1u);
       GasState st = sload(g);
-      const float eg = gas_eps_f<CGA>(T, dg0 + g, pq, tq, du, ucg, brw, st, sat);
+      const long long dg = dg0 + g;  // (channel, emitter)
+      const float eg = gas_eps_f<CGA>(T, dg, pq, tq, du, ucg, brw, st, sat);
       sstore(g, st);
       E = E + (1.f - E) * eg;
     }
     // extinction and continua
     float beta = c.nw > 0 ? f[(F.kw0 + w) * 32] : 0.f;
-    if (has_cloud) beta += f[F.aux * 32] * cloud;
+    if (has_cloud) beta += f[F.aux * 32] * kthr[0];
     const float pr = p / (float)kP0;
     if (co2_on) {
+      const float co2_296 = kc[1], co2_260 = kc[2], co2_230 = kc[3];
       const float d230 = t - 230.f, d260 = t - 260.f, d296 = t - 296.f;
       const float ctw = d260 * 5.050505e-4f * d296 * co2_230 - d230 * 9.259259e-4f * d296 * co2_260 +
                         d230 * 4.208754e-4f * d260 * co2_296;
@@ -469,11 +491,13 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
     if (h2o_on) {
       const float q = f[F.qh2o * 32];
       const float uh = f[(F.u0 + c.ig_h2o) * 32];
+      const float nu = kc[0], h2o_s296 = kc[4], h2o_lr = kc[5], h2o_frn = kc[6];
       const float self = h2o_s296 * __expf(h2o_lr * (296.f - t) * (1.f / 36.f));
       const float a1 = nu * ((uh / ds) * 1e-20f) * tanhf(.7193876f / t * nu);
       beta += a1 * (296.f / t) * pr * (q * self + (1.f - q) * h2o_frn);
     }
     if (n2_on || o2_on) {
+      const float n2_b = kc[7], n2_beta = kc[8], o2_b = kc[9], o2_beta = kc[10];
       const float x = pr * 273.f / t;
       const float x2 = 0.1f * x * x;
       if (n2_on)
@@ -481,7 +505,9 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
                 (0.79f + 0.21f * (1.294f - 0.4545f * t / 296.f));
       if (o2_on) beta += x2 * __expf(o2_beta * (1.f / 296.f - 1.f / t)) * 0.21f * o2_b;
     }
-    // source function (formod_srcfunc)
+    // source function (formod_srcfunc); the channel index is re-read from
+    // shared memory so that the table pointer holds no registers in the loop
+    const float* srf = T.srf + (long long)kci[11] * kNS;
     const float xs = (t - st0) / sdt;
     int is = (int)xs;
     is = is < 0 ? 0 : (is > kNS - 2 ? kNS - 2 : is);
@@ -497,13 +523,17 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
       rad = tsum;
       tau *= (1.f - eps);
     }
-    if (sc) {
+    if (do_refl) {
+      float* sc = refl + 2 * (L.off[r] * c.nd);
       sc[2 * ((long long)ip * c.nd + id)] = src;
       sc[2 * ((long long)ip * c.nd + id) + 1] = eps;
     }
   }
   if (r < 0) return;
 
+  const double nud2 = ch.nu[id];
+  const float sfeps2 = kthr[nth];
+  const float* srf = T.srf + (long long)id * kNS;
   double radd = (double)rad;
   const double sft = L.sft[r];
   if (c.sftype >= 1 && sft > 0) {
@@ -512,8 +542,9 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
     is = is < 0 ? 0 : (is > kNS - 2 ? kNS - 2 : is);
     const float s0 = srf[is], s1 = srf[is + 1];
     const float ssf = s0 + (s1 - s0) * (xs - (float)is);
-    radd += (double)(sfeps * ssf * tau);
+    radd += (double)(sfeps2 * ssf * tau);
     if (do_refl) {
+      const float* sc = refl + 2 * (L.off[r] * c.nd);
       float tr = 1.f;
       double acc = 0;
       for (int ip = n - 1; ip >= 0; ip--) {
@@ -522,7 +553,7 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
         acc += (double)(src * e * tr);
         tr *= (1.f - e);
       }
-      radd += acc * (double)tau * (double)(1.f - sfeps);
+      radd += acc * (double)tau * (double)(1.f - sfeps2);
       if (c.sftype >= 3) {
         const double* e6 = L.ends + 6LL * r;
         // solar zenith angle (sza, jurassic.c:5183-5219) and incidence
@@ -548,7 +579,7 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
                               sqrt(x0[0] * x0[0] + x0[1] * x0[1] + x0[2] * x0[2]) /
                               sqrt(x1[0] * x1[0] + x1[1] * x1[1] + x1[2] * x1[2]);
           const double rcos = cosa / cos(sza2 * (kPI / 180.0));
-          radd += 6.764e-5 / (2. * kPI) * planck(kTSUN, nud) * tr * (1 - sfeps) * tau * rcos;
+          radd += 6.764e-5 / (2. * kPI) * planck(kTSUN, nud2) * tr * (1 - sfeps2) * tau * rcos;
         }
       }
     }
@@ -559,7 +590,7 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
     b.tau[oi] = (double)tau;
     return;
   }
-  if (c.write_bbt) radd = kC2 * nud / log1p(kC1 * (nud * nud * nud) / radd);
+  if (c.write_bbt) radd = kC2 * nud2 / log1p(kC1 * (nud2 * nud2 * nud2) / radd);
   b.rad[oi] = b.mask[oi] ? __longlong_as_double(0x7ff8000000000000LL) : radd;
   b.tau[oi] = (double)tau;
 }
@@ -641,7 +672,10 @@ void launch_path_mixed(const CtlDev& c, const TblDev& T, const ChanDev& ch, cons
                        cudaStream_t s) {
   const int nchb = (c.nd + 3) / 4;
   const unsigned nblk = (unsigned)((long long)P.ntile * nchb);
-  const size_t smem = sizeof(unsigned) * kStateWords * 128 * (size_t)(c.ng > 0 ? c.ng : 1);
+  // state, then kChanConsts per warp and kThreadFloats per thread (128
+  // threads, 4 warps per block)
+  const size_t smem = sizeof(unsigned) * kStateWords * 128 * (size_t)(c.ng > 0 ? c.ng : 1) +
+                      sizeof(float) * (4 * kChanConsts + kThreadFloats * 128);
   if (c.formod == 0)
     launch_variant<true>(c, T, ch, b, L, P, refl_scratch, variant, nblk, smem, s);
   else
