@@ -129,6 +129,14 @@ int jgb_set_fov(jgb_ctx *ctx, int n, const double *dz, const double *w);
    results do not depend on it. */
 int jgb_set_los_bound_scale(jgb_ctx *ctx, double scale);
 
+/* Mixed-precision path loop of a batch too small to fill the device (at most
+   32 x SMs warps of tile x channel x emitter): split over the emitters, one
+   warp per (tile, channel, emitter) for the emitters' path states, then one
+   per (tile, channel) for their combination and the radiance.  mode -1 (the
+   default) decides by that size, 0 never splits, 1 always does.  The results
+   do not depend on it. */
+int jgb_set_path_split(jgb_ctx *ctx, int mode);
+
 /* Source function of channel id from its filter function
    (init_srcfunc, jurassic.c:3631-3681), computed on the device. */
 int jgb_set_filter(jgb_ctx *ctx, int id, int n, const double *fnu, const double *f);

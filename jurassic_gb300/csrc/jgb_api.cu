@@ -409,7 +409,22 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
       CK(x->refl.reserve(sizeof(float) * 2 * (size_t)cap * c.nd));
       refl = x->refl.as<float>();
     }
-    if (x->path_variant < 0) {
+    // a batch with too few tiles to fill the device is latency-bound: split
+    // the path over the emitters (ng warps per tile and channel)
+    const long long split_warps = (long long)ntile * c.nd * c.ng;
+    const bool split = c.ng > 1 && (x->path_split == 1 ||
+                                    (x->path_split < 0 && split_warps <= 32LL * x->sms));
+    Pm.seg_eps = nullptr;
+    Pm.seg_sat = nullptr;
+    if (split) {
+      const size_t nseg = (size_t)std::max(tile_points, 1LL) * c.nd * c.ng * 32;
+      CK(x->seg.reserve(nseg * (sizeof(float) + 1)));
+      Pm.seg_eps = x->seg.as<float>();
+      Pm.seg_sat = reinterpret_cast<unsigned char*>(Pm.seg_eps + nseg);
+      CK(cudaEventRecord(x->ev[4], s));
+      launch_path_split(c, T, ch, bo, L, Pm, refl, s);
+      launches += 7;
+    } else if (x->path_variant < 0) {
       // autotune: time every variant on this batch (results are identical)
       const char* force = getenv("JGB_PATH_VARIANT");
       if (force) {
@@ -431,9 +446,11 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
         }
       }
     }
-    CK(cudaEventRecord(x->ev[4], s));
-    launch_path_mixed(c, T, ch, bo, L, Pm, refl, x->path_variant, s);
-    launches += 6;
+    if (!split) {
+      CK(cudaEventRecord(x->ev[4], s));
+      launch_path_mixed(c, T, ch, bo, L, Pm, refl, x->path_variant, s);
+      launches += 6;
+    }
   }
   CK(cudaGetLastError());
   if (c.fov) {
@@ -816,6 +833,7 @@ int jgb_create(const jgb_ctl* ctl, int device, jgb_ctx** out) {
   }
   for (auto& e : x->ev) cudaEventCreate(&e);
   for (auto& e : x->pev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  cudaDeviceGetAttribute(&x->sms, cudaDevAttrMultiProcessorCount, device);
   if (cudaStreamCreateWithFlags(&x->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
     jgb_destroy(x);
     return JGB_ERR_CUDA;
@@ -910,7 +928,7 @@ void jgb_destroy(jgb_ctx* x) {
                     &x->b_tp, &x->b_mask, &x->b_p, &x->los_off, &x->los_cnt, &x->los_cnt64,
                     &x->los_sft, &x->los_ends, &x->los_planes, &x->scan_tmp, &x->err_word,
                     &x->tiles_perm, &x->tiles_keys, &x->tiles_keys2, &x->tiles_vals,
-                    &x->tiles_off, &x->tiles_len, &x->tiles_data, &x->refl,
+                    &x->tiles_off, &x->tiles_len, &x->tiles_data, &x->refl, &x->seg,
                     &x->kx_levoff, &x->kx_rayoff, &x->kx_rayobs, &x->kx_src, &x->kx_lev,
                     &x->kx_scal, &x->kx_geo, &x->kx_rad, &x->kx_tau, &x->kx_tp, &x->kx_mask,
                     &x->kx_pert, &x->kx_h, &x->kx_ymap, &x->kx_K, &x->kx_base_rayoff,
@@ -1014,6 +1032,12 @@ int jgb_set_table(jgb_ctx* x, int id, int ig, int np, const double* p, const int
                     eps + (size_t)ip * tt_cap * tu_cap, sizeof(float) * tu_cap,
                     sizeof(float) * w, ntt, cudaMemcpyHostToDevice));
   }
+  return JGB_OK;
+}
+
+int jgb_set_path_split(jgb_ctx* x, int mode) {
+  if (!x || mode < -1 || mode > 1) return fail(x, JGB_ERR_ARG, "bad path split mode");
+  x->path_split = mode;
   return JGB_OK;
 }
 

@@ -81,6 +81,9 @@ struct jgb_ctx {
   cudaEvent_t pev[3] = {};
   int path_variant = -1;  // mixed path kernel variant chosen by the autotuner
   double los_bound_scale = 1.0;  // factor on the per-ray LOS bound (0: count first)
+  int path_split = -1;    // path split over emitters: -1 when latency-bound, 0 never, 1 always
+  int sms = 152;          // multiprocessors of the device
+  jgb::DevBuf seg;        // segment emissivities and flags of the split path
   std::vector<float> tune_ms;
   jgb_stats stats{};
   std::string err;

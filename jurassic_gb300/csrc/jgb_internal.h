@@ -40,11 +40,19 @@ struct MixedPlan {
   float* data;          // tile planes
   int nfield;
   unsigned brmask;      // emitters with p-T brackets precomputed per LOS point
+  // split path (latency-bound batches): segment emissivity and saturation
+  // flag of every (tile point, channel, emitter, lane), else nullptr
+  float* seg_eps;
+  unsigned char* seg_sat;
 };
 int mixed_nfield(const CtlDev& c, unsigned brmask);
 void launch_pack_tiles_n(const CtlDev& c, const TblDev& T, const LosDev& L, const MixedPlan& P,
                          long long total_tile_points, cudaStream_t s);
 int path_mixed_variants();
+// the path split over emitters: one warp per (tile, channel, emitter) for the
+// emitter path states, then the combination and radiance per (tile, channel)
+void launch_path_split(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
+                       const LosDev& L, const MixedPlan& P, float* refl_scratch, cudaStream_t s);
 void launch_path_mixed(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
                        const LosDev& L, const MixedPlan& P, float* refl_scratch, int variant,
                        cudaStream_t s);

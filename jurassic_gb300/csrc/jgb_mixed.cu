@@ -347,7 +347,10 @@ __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, float 
 // through L1 into L2.
 // MINB is the minimum number of resident blocks per SM requested from the
 // register allocator (1 = no cap); the variants are chosen by the autotuner.
-template <int MINB, bool CGA>
+// SPLIT: the emitters' segment emissivities come from k_path_gas (P.seg_eps,
+// P.seg_sat) instead of being computed here; everything else is this same
+// code, so both forms give the same results.
+template <int MINB, bool CGA, bool SPLIT = false>
 __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, ChanDev ch,
                                                           BatchDev b, LosDev L, MixedPlan P,
                                                           float* refl) {
@@ -444,7 +447,7 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
     for (int k = 0; k < 2; k++)
       q[(3 + k) * nth] = (unsigned)st.h[2 * k] | ((unsigned)st.h[2 * k + 1] << 16);
   };
-  for (int g = 0; g < ng; g++) {
+  for (int g = 0; g < ng && !SPLIT; g++) {
     GasState st;
     st.t = 1.f;
     st.e = 0.f;
@@ -453,6 +456,10 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
     for (int k = 0; k < 4; k++) st.h[k] = 0;
     sstore(g, st);
   }
+  // split form: segment emissivities of (point, this channel, emitter g) at
+  // seg0 + ip * segstride + g * 32
+  const long long segstride = (long long)c.nd * ng * 32;
+  const long long seg0 = SPLIT ? ((P.toff[tile] * c.nd + id) * ng) * 32 + lane : 0;
   const long long dg0 = (long long)id * ng;
   float rad = 0.f, comp = 0.f, tau = 1.f;
   const bool do_refl = refl != nullptr && r >= 0 && c.sftype >= 2 && sfeps < 1.f && L.sft[r] > 0;
@@ -464,16 +471,23 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
     bool sat = false;
 #pragma unroll 1
     for (int g = 0; g < ng; g++) {
-      const float du = cga ? 0.f : f[(F.u0 + g) * 32];
-      const float pq = cga ? f[(F.cgp0 + g) * 32] : p;
-      const float tq = cga ? f[(F.cgt0 + g) * 32] : t;
-      const float ucg = cga ? f[(F.cgu0 + g) * 32] : 0.f;
-      const unsigned brw = ((P.brmask >> g) & 1u) ? __float_as_uint(f[(F.br0 + g) * 32])
-                                                   : (kNoBracket | 1u);
-      GasState st = sload(g);
-      const long long dg = dg0 + g;  // (channel, emitter)
-      const float eg = gas_eps_f<CGA>(T, dg, pq, tq, du, ucg, brw, st, sat);
-      sstore(g, st);
+      float eg;
+      if (SPLIT) {
+        const long long o = seg0 + ip * segstride + g * 32;
+        eg = P.seg_eps[o];
+        if (P.seg_sat[o]) sat = true;
+      } else {
+        const float du = cga ? 0.f : f[(F.u0 + g) * 32];
+        const float pq = cga ? f[(F.cgp0 + g) * 32] : p;
+        const float tq = cga ? f[(F.cgt0 + g) * 32] : t;
+        const float ucg = cga ? f[(F.cgu0 + g) * 32] : 0.f;
+        const unsigned brw = ((P.brmask >> g) & 1u) ? __float_as_uint(f[(F.br0 + g) * 32])
+                                                     : (kNoBracket | 1u);
+        GasState st = sload(g);
+        const long long dg = dg0 + g;  // (channel, emitter)
+        eg = gas_eps_f<CGA>(T, dg, pq, tq, du, ucg, brw, st, sat);
+        sstore(g, st);
+      }
       E = E + (1.f - E) * eg;
     }
     // extinction and continua
@@ -595,6 +609,55 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
   b.tau[oi] = (double)tau;
 }
 
+// Emitter path states of the split form: one warp per (tile, channel,
+// emitter) walks the tile's points with the state of that emitter only and
+// writes every segment emissivity and saturation flag.  The emitters' states
+// are independent along the path (intpol_tbl_ega / intpol_tbl_cga keep one
+// tau_path per emitter); only their combination per point couples them, and
+// that is left to k_path_mixed<..., SPLIT>.  A latency-bound batch (few
+// tiles) so runs ng warps where the fused form runs one.
+template <bool CGA>
+__global__ void __launch_bounds__(128) k_path_gas(CtlDev c, TblDev T, BatchDev b, LosDev L,
+                                                  MixedPlan P) {
+  const int lane = threadIdx.x & 31;
+  const int ng = c.ng;
+  const long long per_tile = (long long)c.nd * ng;
+  const long long wg = (long long)blockIdx.x * 4 + (threadIdx.x >> 5);
+  const int tile = (int)(wg / per_tile);
+  if (tile >= P.ntile) return;
+  const int rem = (int)(wg - (long long)tile * per_tile);
+  const int id = rem / ng, g = rem - id * ng;
+  int r = P.perm[tile * 32 + lane];
+  if (r >= 0 && b.obs_skip && b.obs_skip[b.ray_obs[r]]) r = -1;
+  const int n = r >= 0 ? L.count[r] : 0;
+  const Fields F = fields_of(c, P.brmask);
+  const float* base = P.data + P.toff[tile] * (long long)F.n * 32 + lane;
+  constexpr bool cga = CGA;
+  const long long dg = (long long)id * ng + g;
+  const long long segstride = (long long)c.nd * ng * 32;
+  const long long seg0 = ((P.toff[tile] * c.nd + id) * ng + g) * 32 + lane;
+  GasState st;
+  st.t = 1.f;
+  st.e = 0.f;
+  st.ipr = -1;
+#pragma unroll
+  for (int k = 0; k < 4; k++) st.h[k] = 0;
+  const unsigned brbit = (P.brmask >> g) & 1u;
+  for (int ip = 0; ip < n; ip++) {
+    const float* f = base + (long long)ip * F.n * 32;
+    const float du = cga ? 0.f : f[(F.u0 + g) * 32];
+    const float pq = cga ? f[(F.cgp0 + g) * 32] : f[F.p * 32];
+    const float tq = cga ? f[(F.cgt0 + g) * 32] : f[F.t * 32];
+    const float ucg = cga ? f[(F.cgu0 + g) * 32] : 0.f;
+    const unsigned brw = brbit ? __float_as_uint(f[(F.br0 + g) * 32]) : (kNoBracket | 1u);
+    bool sat = false;
+    const float eg = gas_eps_f<CGA>(T, dg, pq, tq, du, ucg, brw, st, sat);
+    const long long o = seg0 + ip * segstride;
+    P.seg_eps[o] = eg;
+    P.seg_sat[o] = sat ? 1 : 0;
+  }
+}
+
 // First and last entries of every table row in one float4 (rows with fewer
 // than two entries are never interpolated and get zeros).
 // Row records of the mixed path, two float4 per row (ip, it):
@@ -680,6 +743,28 @@ void launch_path_mixed(const CtlDev& c, const TblDev& T, const ChanDev& ch, cons
     launch_variant<true>(c, T, ch, b, L, P, refl_scratch, variant, nblk, smem, s);
   else
     launch_variant<false>(c, T, ch, b, L, P, refl_scratch, variant, nblk, smem, s);
+}
+
+template <bool CGA>
+void launch_split(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
+                  const LosDev& L, const MixedPlan& P, float* refl, size_t smem, cudaStream_t s) {
+  const long long warps = (long long)P.ntile * c.nd * c.ng;
+  k_path_gas<CGA><<<(unsigned)((warps + 3) / 4), 128, 0, s>>>(c, T, b, L, P);
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(k_path_mixed<1, CGA, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+  const unsigned nblk = (unsigned)((long long)P.ntile * ((c.nd + 3) / 4));
+  k_path_mixed<1, CGA, true><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl);
+}
+
+void launch_path_split(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
+                       const LosDev& L, const MixedPlan& P, float* refl_scratch, cudaStream_t s) {
+  const size_t smem = sizeof(unsigned) * kStateWords * 128 * (size_t)(c.ng > 0 ? c.ng : 1) +
+                      sizeof(float) * (4 * kChanConsts + kThreadFloats * 128);
+  if (c.formod == 0)
+    launch_split<true>(c, T, ch, b, L, P, refl_scratch, smem, s);
+  else
+    launch_split<false>(c, T, ch, b, L, P, refl_scratch, smem, s);
 }
 
 void launch_src_to_float(int nd, const double* sr, float* srf, cudaStream_t s) {

@@ -113,6 +113,7 @@ SIGNATURES = {
     "jgb_set_filter": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp]),
     "jgb_set_fov": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp]),
     "jgb_set_los_bound_scale": (C.c_int, [C.c_void_p, C.c_double]),
+    "jgb_set_path_split": (C.c_int, [C.c_void_p, C.c_int]),
     "jgb_set_srcfunc": (C.c_int, [C.c_void_p, _dp]),
     "jgb_get_srcfunc": (C.c_int, [C.c_void_p, _dp, _dp]),
     "jgb_formod": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
@@ -224,6 +225,11 @@ class Context:
         """Factor on the per-ray LOS-point bound of one-pass mixed ray tracing
         of large batches (0: always count the rays first)."""
         self._check(load().jgb_set_los_bound_scale(self.h, float(scale)))
+
+    def set_path_split(self, mode: int):
+        """Mixed path loop split over the emitters: -1 for batches too small
+        to fill the device (default), 0 never, 1 always."""
+        self._check(load().jgb_set_path_split(self.h, int(mode)))
 
     def _check(self, rc):
         if rc != JGB_OK:
