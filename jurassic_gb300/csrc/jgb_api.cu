@@ -178,19 +178,32 @@ __global__ void k_iota(int n, int* v) {
   if (i < n) v[i] = i;
 }
 
-// tile plan from rays sorted by LOS length (descending)
-__global__ void k_tiles(int nray, int ntile, const int* sorted_cnt, const int* sorted_ray,
-                        int* perm, int* tlen, long long* tpts) {
+// tile plan from the rays in sort order (descending key)
+__global__ void k_tiles(int nray, int ntile, const int* count, const int* sorted_ray, int* perm,
+                        int* tlen, long long* tpts) {
   const int tile = blockIdx.x * blockDim.x + threadIdx.x;
   if (tile >= ntile) return;
   int mx = 0;
   for (int l = 0; l < 32; l++) {
     const int k = tile * 32 + l;
     perm[tile * 32 + l] = k < nray ? sorted_ray[k] : -1;
-    if (k < nray) mx = sorted_cnt[k] > mx ? sorted_cnt[k] : mx;
+    if (k < nray) mx = max(mx, count[sorted_ray[k]]);
   }
   tlen[tile] = mx;
   tpts[tile] = mx;
+}
+
+// Sort key of a batch whose masked pairs are skipped: rays with the same
+// number of measured channels first, then by LOS length, so that a tile's
+// rays tend to share their masks and whole warps of unmeasured channels
+// have nothing to do.
+__global__ void k_mask_keys(int nray, int nd, const unsigned char* mask, const int* count,
+                            int* key) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nray) return;
+  int m = 0;
+  for (int id = 0; id < nd; id++) m += mask[(long long)id * nray + r] ? 0 : 1;
+  key[r] = (m << 13) | min(count[r], 8191);
 }
 
 float elapsed(cudaEvent_t a, cudaEvent_t b) {
@@ -374,11 +387,17 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
     int* vals_in = x->tiles_vals.as<int>();
     int* vals_out = vals_in + nray;
     k_iota<<<(nray + 255) / 256, 256, 0, s>>>(nray, vals_in);
+    const int* keys = L.count;
+    if (b.skip_masked) {
+      k_mask_keys<<<(nray + 255) / 256, 256, 0, s>>>(nray, c.nd, b.mask, L.count,
+                                                      x->tiles_keys.as<int>());
+      keys = x->tiles_keys.as<int>();
+    }
     size_t sbytes = 0;
-    cub::DeviceRadixSort::SortPairsDescending(nullptr, sbytes, L.count, x->tiles_keys2.as<int>(),
+    cub::DeviceRadixSort::SortPairsDescending(nullptr, sbytes, keys, x->tiles_keys2.as<int>(),
                                               vals_in, vals_out, nray, 0, 32, s);
     CK(x->scan_tmp.reserve(std::max(sbytes, tmp_bytes) + 16));
-    cub::DeviceRadixSort::SortPairsDescending(x->scan_tmp.p, sbytes, L.count,
+    cub::DeviceRadixSort::SortPairsDescending(x->scan_tmp.p, sbytes, keys,
                                               x->tiles_keys2.as<int>(), vals_in, vals_out, nray,
                                               0, 32, s);
     long long* tpts = x->tiles_off.as<long long>() + ntile + 1;
@@ -388,8 +407,8 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
     Pm.perm = x->tiles_perm.as<int>();
     Pm.tlen = x->tiles_len.as<int>();
     Pm.toff = toff;
-    k_tiles<<<(ntile + 127) / 128, 128, 0, s>>>(nray, ntile, x->tiles_keys2.as<int>(), vals_out,
-                                                 Pm.perm, Pm.tlen, tpts);
+    k_tiles<<<(ntile + 127) / 128, 128, 0, s>>>(nray, ntile, L.count, vals_out, Pm.perm, Pm.tlen,
+                                                 tpts);
     CK(cudaMemsetAsync(toff, 0, sizeof(long long), s));
     size_t sb2 = 0;
     cub::DeviceScan::InclusiveSum(nullptr, sb2, tpts, toff + 1, ntile, s);
@@ -751,6 +770,9 @@ int fd_core(jgb_ctx* x, const FdLayout& H, const FdInput& in, const std::vector<
     b.tau = tau_e;
     b.tp = tp_e;
     b.mask = x->kx_mask.as<unsigned char>();
+    // only measured (finite) entries enter K; with a field of view every
+    // pencil beam may feed a measured neighbour
+    b.skip_masked = c.fov ? 0 : 1;
     k_ray_obs<<<(ne + 127) / 128, 128, 0, s>>>(ne, x->kx_rayoff.as<int>(), x->kx_rayobs.as<int>());
     const long long nm = (long long)c.nd * nray_e;
     k_mask<<<(unsigned)((nm + 255) / 256), 256, 0, s>>>(nm, rad_e, x->kx_mask.as<unsigned char>());

@@ -168,6 +168,9 @@ struct BatchDev {
   // [nobs] 1 = observation not computed: its rays get no LOS and its
   // outputs (rad, tau, tp) and pressures are left untouched (nullptr: none)
   const unsigned char* obs_skip;
+  // 1: masked (ray, channel) pairs need no radiance (their outputs are only
+  // NaN-masked), so the path loop skips them; 0: every pair is computed
+  unsigned char skip_masked;
 };
 
 // Lines of sight, ray-major with per-ray offsets, SoA planes of FP64.

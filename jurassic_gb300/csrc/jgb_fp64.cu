@@ -489,7 +489,7 @@ __global__ void k_path_fp64(CtlDev c, TblDev T, ChanDev ch, BatchDev b, LosDev L
   const int r = (int)(gid % nray);
   const int o = b.ray_obs[r];
   if (b.obs_skip && b.obs_skip[o]) return;
-  const int n = L.count[r];
+  const int n = b.skip_masked && b.mask[gid] ? 0 : L.count[r];  // gid = id * nray + r
   const long long base = L.off[r];
   const double nu = ch.nu[id];
   const double* cc = ch.ctm + (long long)id * kCtmStride;

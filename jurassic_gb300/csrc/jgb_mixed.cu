@@ -363,7 +363,8 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
   if (tile >= P.ntile || id >= c.nd) return;
   int r = P.perm[tile * 32 + lane];
   if (r >= 0 && b.obs_skip && b.obs_skip[b.ray_obs[r]]) r = -1;  // lane idle, outputs untouched
-  const int n = r >= 0 ? L.count[r] : 0;
+  const bool skip = r >= 0 && b.skip_masked && b.mask[(long long)id * b.nray + r];
+  const int n = r >= 0 && !skip ? L.count[r] : 0;
   const Fields F = fields_of(c, P.brmask);
   const float* base = P.data + P.toff[tile] * (long long)F.n * 32 + lane;
   constexpr bool cga = CGA;
@@ -629,7 +630,8 @@ __global__ void __launch_bounds__(128) k_path_gas(CtlDev c, TblDev T, BatchDev b
   const int id = rem / ng, g = rem - id * ng;
   int r = P.perm[tile * 32 + lane];
   if (r >= 0 && b.obs_skip && b.obs_skip[b.ray_obs[r]]) r = -1;
-  const int n = r >= 0 ? L.count[r] : 0;
+  const bool skip = r >= 0 && b.skip_masked && b.mask[(long long)id * b.nray + r];
+  const int n = r >= 0 && !skip ? L.count[r] : 0;
   const Fields F = fields_of(c, P.brmask);
   const float* base = P.data + P.toff[tile] * (long long)F.n * 32 + lane;
   constexpr bool cga = CGA;

@@ -76,6 +76,8 @@ def test_kernel_batch_nadir_vs_oracle(built_lib, built_oracle):
     ctx = native.Context(ctl, w.tables, w.filters)
     b = w.batch.fresh_outputs()
     b.rad[2, 3] = np.nan  # one masked channel
+    b.rad[3:, 1] = np.nan  # observation 1 measures channels 0-2 only: the
+    # perturbed forward models skip its other channels
     Ks, out = ctx.kernel_batch(b, native.FP64)
     for i in range(b.nobs):
         atm, obs = b.item(w.ctl, i)
