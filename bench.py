@@ -413,7 +413,8 @@ def run_serving(args, device):
     closed = serving.serve(engine(native.MIXED), ctl, reqs, np.inf)
     rate = args.serve_load * closed["retrievals_per_s"]
     pois = serving.serve(engine(native.MIXED), ctl, reqs, rate, seed=7)
-    sub_mixed = serving.serve(engine(native.MIXED), ctl, reqs[:m], np.inf)
+    m = min(m, n)
+    sub_mixed = closed if m == n else serving.serve(engine(native.MIXED), ctl, reqs[:m], np.inf)
     sub_fp64 = serving.serve(engine(native.FP64), ctl, reqs[:m], np.inf)
     dev = []
     for a, b in zip(sub_fp64["results"], sub_mixed["results"]):
@@ -422,8 +423,8 @@ def run_serving(args, device):
     out.update({
         "mixed_closed_loop": strip(closed),
         "mixed_poisson": dict(strip(pois), load=args.serve_load),
-        "fp64_closed_loop_subset": strip(sub_fp64),
-        "mixed_closed_loop_subset": strip(sub_mixed),
+        "fp64_closed_loop": dict(strip(sub_fp64), requests=m),
+        "mixed_closed_loop_same_requests": dict(strip(sub_mixed), requests=m),
         "retrievals_per_s_mixed_over_fp64": sub_mixed["retrievals_per_s"] / sub_fp64["retrievals_per_s"],
         "mixed_vs_fp64_max_dx_over_sigma": max(dev) if dev else None,
         "mem_budget_gb": args.serve_budget_gb})
@@ -444,7 +445,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=48)
-    ap.add_argument("--serve-fp64-requests", type=int, default=12)
+    ap.add_argument("--serve-fp64-requests", type=int, default=48,
+                    help="requests of the stream run through the FP64 engine for the "
+                         "mixed/FP64 retrievals/s ratio (all of them by default)")
     ap.add_argument("--serve-load", type=float, default=0.7,
                     help="Poisson arrival rate as a fraction of the closed-loop capacity")
     ap.add_argument("--serve-budget-gb", type=float, default=64.0)

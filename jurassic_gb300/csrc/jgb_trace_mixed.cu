@@ -103,14 +103,23 @@ __device__ inline float lev_find(const AtmM& a, double z, Lev& L) {
 }
 
 __device__ inline void lev_pt(const Lev& L, float dl, float* p, float* t) {
-  *p = L.plog ? L.p0 * expf(L.sp * dl) : L.p0 + L.sp * dl;
+  *p = L.plog ? L.p0 * __expf(L.sp * dl) : L.p0 + L.sp * dl;
   *t = L.t0 + L.st * dl;
+}
+
+// exp(x) - 1 for the small exponents of the refraction finite differences:
+// the Taylor series to x^4 where |x| < 1/64 (truncation below x^4/120
+// relative, far under FP32 rounding), else expm1f.
+__device__ inline float expm1_small(float x) {
+  if (fabsf(x) < 0.015625f)
+    return x * (1.f + x * (0.5f + x * (0.16666667f + x * 0.041666668f)));
+  return expm1f(x);
 }
 
 // N(z + dl) - N(z) inside one level, from p, T at z (no cancellation).
 __device__ inline float dN_in(const Lev& L, float p, float t, float dl) {
   const float t2 = t + L.st * dl;
-  if (L.plog) return kRefracC * p / (t * t2) * (t * expm1f(L.sp * dl) - L.st * dl);
+  if (L.plog) return kRefracC * p / (t * t2) * (t * expm1_small(L.sp * dl) - L.st * dl);
   return kRefracC * dl * (L.sp * t - p * L.st) / (t * t2);
 }
 
@@ -132,10 +141,16 @@ struct GeoKeep {
   bool want_p1;
 };
 
+// Threads per block of the trace kernels (the fill pass keeps per-thread
+// level caches in shared memory with this stride).
+constexpr int kTraceThreads = 64;
+
+// qc: the fill pass's cache of the current level's emitter and window values
+// and slopes (qc[k * kTraceThreads], qc[(ng + nw + k) * kTraceThreads]).
 template <bool STORE>
 __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long nray, int r,
                       const LosDev& L, long long base, int cap, double* sft_out, GeoKeep* gk,
-                      unsigned* err) {
+                      float* qc, unsigned* err) {
   const float h = 0.02f;
   const double zrefrac = 60;
   *sft_out = -999;
@@ -187,7 +202,8 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
 
   Lev lv;
   lv.i = -1;
-  int n = 0, stop = 0;
+  int n = 0, stop = 0, qc_level = -1;
+  const int nqk = c.ng + c.nw;
   double last_z = 0, x_last[3] = {0, 0, 0};
   const float rayds = (float)c.rayds, raydz = (float)c.raydz;
   for (;;) {
@@ -233,15 +249,21 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
       L.t[s] = t;
       L.ds[s] = step;
       const int i = lv.i;
-      for (int ig = 0; ig < c.ng; ig++) {
-        const float q0 = (float)a.q[ig * a.stride + i], q1 = (float)a.q[ig * a.stride + i + 1];
-        L.u[ig * L.cap + s] = q0 + (q1 - q0) / lv.dz * dl;
+      if (i != qc_level) {  // a new level: its values and slopes q0 + (q1 - q0) / dz * dl
+        qc_level = i;
+        for (int k = 0; k < nqk; k++) {
+          const double* src = k < c.ng ? a.q + k * a.stride : a.k + (k - c.ng) * a.stride;
+          const float v0 = (float)src[i], v1 = (float)src[i + 1];
+          qc[k * kTraceThreads] = v0;
+          qc[(nqk + k) * kTraceThreads] = (v1 - v0) / lv.dz;
+        }
       }
+      for (int ig = 0; ig < c.ng; ig++)
+        L.u[ig * L.cap + s] = qc[ig * kTraceThreads] + qc[(nqk + ig) * kTraceThreads] * dl;
       if (c.ig_h2o >= 0) L.qh2o[s] = L.u[c.ig_h2o * L.cap + s];
-      for (int iw = 0; iw < c.nw; iw++) {
-        const float k0 = (float)a.k[iw * a.stride + i], k1 = (float)a.k[iw * a.stride + i + 1];
-        L.kw[iw * L.cap + s] = k0 + (k1 - k0) / lv.dz * dl;
-      }
+      for (int iw = 0; iw < c.nw; iw++)
+        L.kw[iw * L.cap + s] = qc[(c.ng + iw) * kTraceThreads] +
+                               qc[(nqk + c.ng + iw) * kTraceThreads] * dl;
       if (c.ncl > 0 && a.cldz > 0) {
         const float v = (float)((z - a.clz) / a.cldz);
         L.aux[s] = expf(-0.5f * v * v);
@@ -351,7 +373,8 @@ __global__ void k_trace_count_m(CtlDev c, BatchDev b, LosDev L, unsigned* err) {
   }
   const AtmM a = atm_m(b, c, b.ray_obs[r]);
   double sft;
-  const int n = walk_m<false>(c, a, b.geo, b.nray, r, L, 0, c.nlos_max, &sft, nullptr, err);
+  const int n = walk_m<false>(c, a, b.geo, b.nray, r, L, 0, c.nlos_max, &sft, nullptr, nullptr,
+                              err);
   L.count[r] = n < 0 ? 0 : n;
 }
 
@@ -436,7 +459,9 @@ __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, unsigned* err) {
   gk.imin = 0;
   gk.zmin_seen = 0;
   for (int i = 0; i < 3; i++) gk.x_m1[i] = gk.x_p1[i] = gk.x_first[i] = gk.x_last[i] = 0;
-  const int n = walk_m<true>(c, a, b.geo, b.nray, r, L, base, cap, &sft, &gk, err);
+  __shared__ float qcache[2 * (kMaxG + kMaxW) * kTraceThreads];
+  const int n = walk_m<true>(c, a, b.geo, b.nray, r, L, base, cap, &sft, &gk,
+                             qcache + threadIdx.x, err);
   L.sft[r] = sft;
   if (n > 0) L.count[r] = n;
   const long long nr = b.nray;
@@ -529,7 +554,7 @@ __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, unsigned* err) {
 
 void launch_trace_count_mixed(const CtlDev& c, const BatchDev& b, const LosDev& L, unsigned* err,
                               cudaStream_t s) {
-  const int bs = 64;
+  const int bs = kTraceThreads;
   k_trace_count_m<<<(b.nray + bs - 1) / bs, bs, 0, s>>>(c, b, L, err);
 }
 
@@ -541,7 +566,7 @@ void launch_los_bound_mixed(const CtlDev& c, const BatchDev& b, double scale, in
 
 void launch_trace_fill_mixed(const CtlDev& c, const BatchDev& b, const LosDev& L, unsigned* err,
                              cudaStream_t s) {
-  const int bs = 64;
+  const int bs = kTraceThreads;
   k_trace_fill_m<<<(b.nray + bs - 1) / bs, bs, 0, s>>>(c, b, L, err);
 }
 
