@@ -126,6 +126,7 @@ TblDev tbl_view(const jgb_ctx* x) {
   T.pf = x->t_pf.as<float>();
   T.tf = x->t_tf.as<float>();
   T.rowmeta = x->t_meta.as<float4>();
+  T.ue = x->t_ue.as<float2>();
   T.sr = x->s_sr.as<double>();
   T.srf = x->s_srf.as<float>();
   T.st = x->s_st.as<double>();
@@ -373,7 +374,7 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
         }
       launch_rowmeta((long long)c.nd * c.ng * x->tp * x->tt, x->tu, x->t_nu.as<int>(),
                      x->t_u.as<float>(), x->t_eps.as<float>(), x->t_tf.as<float>(),
-                     x->t_meta.as<float4>(), s);
+                     x->t_meta.as<float4>(), x->t_ue.as<float2>(), s);
       x->meta_stale = false;
     }
     // tile plan: rays sorted by LOS length, 32 per tile
@@ -945,7 +946,7 @@ void jgb_destroy(jgb_ctx* x) {
   if (x->stream) cudaStreamSynchronize(x->stream);
   DevBuf* bufs[] = {&x->d_nu, &x->d_window, &x->d_clnu, &x->d_sfnu, &x->d_ctm, &x->t_np,
                     &x->t_p, &x->t_nt, &x->t_t, &x->t_nu, &x->t_u, &x->t_eps, &x->t_pf,
-                    &x->t_tf, &x->t_meta, &x->s_st, &x->s_sr, &x->s_srf, &x->b_levoff, &x->b_rayoff,
+                    &x->t_tf, &x->t_meta, &x->t_ue, &x->s_st, &x->s_sr, &x->s_srf, &x->b_levoff, &x->b_rayoff,
                     &x->b_rayobs, &x->b_lev, &x->b_scal, &x->b_geo, &x->b_rad, &x->b_tau,
                     &x->b_tp, &x->b_mask, &x->b_p, &x->los_off, &x->los_cnt, &x->los_cnt64,
                     &x->los_sft, &x->los_ends, &x->los_planes, &x->scan_tmp, &x->err_word,
@@ -992,6 +993,7 @@ int jgb_tables_init(jgb_ctx* x, int tp, int tt, int tu) {
   CK(x->t_pf.reserve(sizeof(float) * std::max<size_t>(ndg * tp, 1)));
   CK(x->t_tf.reserve(sizeof(float) * std::max<size_t>(ndg * tp * tt, 1)));
   CK(x->t_meta.reserve(2 * sizeof(float4) * std::max<size_t>(ndg * tp * tt, 1)));
+  CK(x->t_ue.reserve(sizeof(float2) * std::max<size_t>(ndg * tp * tt * tu, 1)));
   x->meta_stale = true;
   CK(cudaMemcpy(x->t_np.p, x->h_np.data(), sizeof(int) * ndg, cudaMemcpyHostToDevice));
   CK(cudaMemset(x->t_nt.p, 0, sizeof(int) * ndg * tp));

@@ -61,7 +61,7 @@ struct jgb_ctx {
   // field of view: nfov samples (dz, w) on the device, pencil-beam scratch
   int nfov = 0;
   jgb::DevBuf d_fov, fov_raw;
-  jgb::DevBuf t_np, t_p, t_nt, t_t, t_nu, t_u, t_eps, t_pf, t_tf, t_meta;
+  jgb::DevBuf t_np, t_p, t_nt, t_t, t_nu, t_u, t_eps, t_pf, t_tf, t_meta, t_ue;
   bool meta_stale = true;
   // source function
   jgb::DevBuf s_st, s_sr, s_srf;

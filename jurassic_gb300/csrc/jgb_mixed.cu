@@ -82,35 +82,49 @@ __device__ __forceinline__ RowF rowf_at(const TblDev& T, unsigned r) {
   return w;
 }
 
-// Largest i in [lo, hi-1] with g[i] <= x, given g[lo] <= x and
-// (g[hi] > x or hi == n-1).
-__device__ __forceinline__ int bisect_f(const float* g, int lo, int hi, float x) {
-  while (hi > lo + 1) {
-    const int mid = (lo + hi) >> 1;
-    if (__ldg(g + mid) > x) hi = mid; else lo = mid;
-  }
-  return lo;
-}
-
-// Bracket i of x on an ascending row of n entries with g[0] <= x <= g[n-1],
-// starting from hint h (locate_tbl semantics, jurassic.c:4152-4170), with
-// the grid values g[i], g[i+1] (reused from the probe loads on a hit).
+// A bracket index i with the grid values at i and i + 1.
 struct Bracket {
   int i;
   float a, b;
 };
 
-__device__ __forceinline__ Bracket hunt_f(const float* g, int n, float x, int h) {
+// Bracket i of x in component C (0: u, 1: eps) of an interleaved ascending
+// row of n entries with C[0] <= x <= C[n-1], from hint h (locate_tbl
+// semantics, jurassic.c:4152-4170), with both components at i and i + 1
+// (reused from the probe loads on a hit).
+struct Bracket2 {
+  int i;
+  float2 a, b;
+};
+
+template <int C>
+__device__ __forceinline__ float comp(const float2 v) {
+  return C == 0 ? v.x : v.y;
+}
+
+template <int C>
+__device__ __forceinline__ int bisect2(const float2* g, int lo, int hi, float x) {
+  const float* gc = reinterpret_cast<const float*>(g) + C;
+  while (hi > lo + 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(gc + 2 * mid) > x) hi = mid; else lo = mid;
+  }
+  return lo;
+}
+
+template <int C>
+__device__ __forceinline__ Bracket2 hunt2(const float2* g, int n, float x, int h) {
   h = min(max(h, 0), n - 2);
   const int h2 = min(h + 2, n - 1);
-  const float a = __ldg(g + h), b = __ldg(g + h + 1), c = __ldg(g + h2);
+  const float2 A = __ldg(g + h), B = __ldg(g + h + 1), D = __ldg(g + h2);
+  const float a = comp<C>(A), b = comp<C>(B), c = comp<C>(D);
   // bracket h or h + 1 (at the right end of the row, x == g[n-1] keeps n-2)
   if (a <= x && (x < c || h2 == n - 1)) {
     const bool up = x >= b && h + 1 <= n - 2;
-    return up ? Bracket{h + 1, b, c} : Bracket{h, a, b};
+    return up ? Bracket2{h + 1, B, D} : Bracket2{h, A, B};
   }
-  const int i = a <= x ? bisect_f(g, h + 2, n - 1, x) : bisect_f(g, 0, h, x);
-  return Bracket{i, __ldg(g + i), __ldg(g + i + 1)};
+  const int i = a <= x ? bisect2<C>(g, h + 2, n - 1, x) : bisect2<C>(g, 0, h, x);
+  return Bracket2{i, __ldg(g + i), __ldg(g + i + 1)};
 }
 
 // Emissivity of one table row (corner of the p-T cell) for the extended
@@ -118,7 +132,7 @@ __device__ __forceinline__ Bracket hunt_f(const float* g, int n, float x, int h)
 // intpol_tbl_eps(u) (jurassic.c:3799-3891, 3895-3967).  In EGA the bracket
 // that inverts e_path also brackets u_eq in the column row (the rows are
 // monotone), and u_eq + du usually stays inside it: then the emissivity is
-// interpolated from the four entries already loaded, with no second search.
+// interpolated from the entries already loaded, with no second search.
 // The bracket is the same either way, so the value is too.  h is the
 // search hint carried along the path: of the emissivity-row search in EGA,
 // of the column-row search in CGA (EGA's column search starts from the
@@ -126,8 +140,7 @@ __device__ __forceinline__ Bracket hunt_f(const float* g, int n, float x, int h)
 template <bool CGA>
 __device__ __forceinline__ float corner_eps(const TblDev& T, const RowF& r, float e_path, float du,
                                             float ucg, unsigned short& h) {
-  const float* ru = T.u + r.off;
-  const float* re = T.eps + r.off;
+  const float2* row = T.ue + r.off;
   float uq;
   int ib = -1;
   float u_lo = 0.f, u_hi = 0.f, e_lo = 0.f, e_hi = 0.f;
@@ -140,13 +153,13 @@ __device__ __forceinline__ float corner_eps(const TblDev& T, const RowF& r, floa
       const float a = log1pf(-r.en) / r.un;
       uq = log1pf(-e_path) / a;
     } else {
-      const Bracket k = hunt_f(re, r.n, e_path, h);
+      const Bracket2 k = hunt2<1>(row, r.n, e_path, h);
       h = (unsigned short)k.i;
       ib = k.i;
-      e_lo = k.a;
-      e_hi = k.b;
-      u_lo = __ldg(ru + k.i);
-      u_hi = __ldg(ru + k.i + 1);
+      e_lo = k.a.y;
+      e_hi = k.b.y;
+      u_lo = k.a.x;
+      u_hi = k.b.x;
       uq = u_lo + (u_hi - u_lo) / (e_hi - e_lo) * (e_path - e_lo);
     }
     uq = uq + du;
@@ -158,10 +171,9 @@ __device__ __forceinline__ float corner_eps(const TblDev& T, const RowF& r, floa
   }
   if (!CGA && ib >= 0 && uq >= u_lo && uq < u_hi)
     return e_lo + (e_hi - e_lo) / (u_hi - u_lo) * (uq - u_lo);
-  const Bracket k = hunt_f(ru, r.n, uq, CGA ? (int)h : (ib >= 0 ? ib : 0));
+  const Bracket2 k = hunt2<0>(row, r.n, uq, CGA ? (int)h : (ib >= 0 ? ib : 0));
   if (CGA) h = (unsigned short)k.i;
-  const float ya = __ldg(re + k.i), yb = __ldg(re + k.i + 1);
-  return ya + (yb - ya) / (k.b - k.a) * (uq - k.a);
+  return k.a.y + (k.b.y - k.a.y) / (k.b.x - k.a.x) * (uq - k.a.x);
 }
 
 __device__ __forceinline__ int bracket_regf(const float* g, int n, float x) {
@@ -679,11 +691,20 @@ __global__ void k_rowmeta(long long nrow, int tu, const int* nu, const float* u,
   meta[2 * r + 1] = make_float4(__int_as_float(n), tf[r], 0.f, 0.f);
 }
 
+// The rows interleaved {u[i], eps[i]}: a probe of one brings the other.
+__global__ void k_interleave(long long n, const float* u, const float* e, float2* ue) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) ue[i] = make_float2(u[i], e[i]);
+}
+
 void launch_rowmeta(long long nrow, int tu, const int* nu, const float* u, const float* e,
-                    const float* tf, float4* meta, cudaStream_t s) {
+                    const float* tf, float4* meta, float2* ue, cudaStream_t s) {
   const int bs = 256;
-  if (nrow > 0)
+  if (nrow > 0) {
     k_rowmeta<<<(unsigned)((nrow + bs - 1) / bs), bs, 0, s>>>(nrow, tu, nu, u, e, tf, meta);
+    const long long n = nrow * tu;
+    k_interleave<<<(unsigned)((n + bs - 1) / bs), bs, 0, s>>>(n, u, e, ue);
+  }
 }
 
 __global__ void k_src_to_float(int nd, const double* sr, float* srf) {
