@@ -374,7 +374,7 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
         }
       launch_rowmeta((long long)c.nd * c.ng * x->tp * x->tt, x->tu, x->t_nu.as<int>(),
                      x->t_u.as<float>(), x->t_eps.as<float>(), x->t_tf.as<float>(),
-                     x->t_meta.as<float4>(), x->t_ue.as<float2>(), s);
+                     c.formod == 0, x->t_meta.as<float4>(), x->t_ue.as<float2>(), s);
       x->meta_stale = false;
     }
     // tile plan: rays sorted by LOS length, 32 per tile

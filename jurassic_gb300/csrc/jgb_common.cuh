@@ -138,7 +138,7 @@ struct TblDev {
   const float* eps;    // [nd*ng*tp*tt*tu]
   const float* pf;     // float copies of p and t for the mixed path
   const float* tf;
-  const float4* rowmeta;  // per row, 2 x float4: {u[0], u[n-1], eps[0], eps[n-1]}, {n, t, 0, 0} (mixed path)
+  const float4* rowmeta;  // row records of the mixed path (EGA: 2 float4 per row, CGA: 1)
   const float2* ue;    // rows interleaved {u[i], eps[i]} (mixed path)
   const double* sr;    // source function [kNS][nd]
   const float* srf;    // source function, channel-major float [nd][kNS]

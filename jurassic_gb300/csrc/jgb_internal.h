@@ -59,7 +59,7 @@ void launch_path_mixed(const CtlDev& c, const TblDev& T, const ChanDev& ch, cons
 void launch_src_to_float(int nd, const double* sr, float* srf, cudaStream_t s);
 void launch_tables_to_float(long long n, const double* src, float* dst, cudaStream_t s);
 void launch_rowmeta(long long nrow, int tu, const int* nu, const float* u, const float* e,
-                    const float* tf, float4* meta, float2* ue, cudaStream_t s);
+                    const float* tf, int cga, float4* meta, float2* ue, cudaStream_t s);
 
 // jgb_api.cu: read-only view of a context for entry points defined in other
 // translation units.  Returns JGB_OK, or an error code with the context's

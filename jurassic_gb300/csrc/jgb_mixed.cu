@@ -23,9 +23,10 @@ namespace jgb {
 // Field indices of a tile plane.  br0..br0+ng-1 hold, for emitters whose
 // p-T grids are shared by all channels, the packed bracket of the point
 // (ipr | it0 << 10 | it1 << 20; kNoBracket: no table, kNoBracket | 2: no
-// temperature rows at that pressure).
+// temperature rows at that pressure), and in CGA pw0..pw0+ng-1 the
+// (log-)pressure interpolation weight in that bracket.
 struct Fields {
-  int p, t, ds, qh2o, aux, kw0, u0, cgp0, cgt0, cgu0, br0, n;
+  int p, t, ds, qh2o, aux, kw0, u0, cgp0, cgt0, cgu0, br0, pw0, n;
 };
 
 __host__ __device__ inline Fields fields_of(const CtlDev& c, unsigned brmask) {
@@ -41,7 +42,8 @@ __host__ __device__ inline Fields fields_of(const CtlDev& c, unsigned brmask) {
   f.cgt0 = f.cgp0 + c.ng;
   f.cgu0 = f.cgt0 + c.ng;
   f.br0 = c.formod == 0 ? f.cgu0 + c.ng : f.u0 + c.ng;
-  f.n = f.br0 + (brmask ? c.ng : 0);
+  f.pw0 = f.br0 + c.ng;
+  f.n = f.br0 + (brmask ? (c.formod == 0 ? 2 * c.ng : c.ng) : 0);
   return f;
 }
 
@@ -67,18 +69,33 @@ struct RowF {
   float t;               // temperature of the row
 };
 
-// Row r = (dg * tp + ip) * tt + it from its 32-byte record; 32-bit row
-// arithmetic (the table upload checks that rows x TU < 2^32).
+// Row r = (dg * tp + ip) * tt + it from its record; 32-bit row arithmetic
+// (the table upload checks that rows x TU < 2^32).  EGA records are 32
+// bytes, {u[0], u[n-1], eps[0], eps[n-1]} and {n (int bits), t, 0, 0}: both
+// ends of a row are tested before any search (the path emissivity starts
+// below the rows and saturates above them).  CGA records are 16 bytes,
+// {n, t, u[0], eps[0]}: a column above a row brackets at n-2, and the
+// search brings the row's last entries.
+template <bool CGA>
 __device__ __forceinline__ RowF rowf_at(const TblDev& T, unsigned r) {
   RowF w;
   w.off = r * (unsigned)T.tu;
-  const float4 m = __ldg(T.rowmeta + 2 * r), m2 = __ldg(T.rowmeta + 2 * r + 1);
-  w.n = __float_as_int(m2.x);
-  w.t = m2.y;
-  w.u0 = m.x;
-  w.un = m.y;
-  w.e0 = m.z;
-  w.en = m.w;
+  if (CGA) {
+    const float4 m = __ldg(T.rowmeta + r);
+    w.n = __float_as_int(m.x);
+    w.t = m.y;
+    w.u0 = m.z;
+    w.e0 = m.w;
+    w.un = w.en = 0.f;
+  } else {
+    const float4 m = __ldg(T.rowmeta + 2 * r), m2 = __ldg(T.rowmeta + 2 * r + 1);
+    w.n = __float_as_int(m2.x);
+    w.t = m2.y;
+    w.u0 = m.x;
+    w.un = m.y;
+    w.e0 = m.z;
+    w.en = m.w;
+  }
   return w;
 }
 
@@ -141,6 +158,17 @@ template <bool CGA>
 __device__ __forceinline__ float corner_eps(const TblDev& T, const RowF& r, float e_path, float du,
                                             float ucg, unsigned short& h) {
   const float2* row = T.ue + r.off;
+  if (CGA) {  // intpol_tbl_eps(ucg), the row's last entries from the search
+    const float uc = ucg;
+    if (uc < r.u0) return r.e0 / r.u0 * uc;
+    const Bracket2 k = hunt2<0>(row, r.n, uc, h);
+    h = (unsigned short)k.i;
+    if (uc > k.b.x) {
+      const float a = log1pf(-k.b.y) / k.b.x;
+      return -expm1f(a * uc);
+    }
+    return k.a.y + (k.b.y - k.a.y) / (k.b.x - k.a.x) * (uc - k.a.x);
+  }
   float uq;
   int ib = -1;
   float u_lo = 0.f, u_hi = 0.f, e_lo = 0.f, e_hi = 0.f;
@@ -232,6 +260,7 @@ __global__ void k_pack_tiles(CtlDev c, TblDev T, LosDev L, MixedPlan P, long lon
   // p-T brackets on the grids of channel 0 (identical for every channel)
   for (int g = 0; P.brmask && g < c.ng; g++) {
     unsigned wd = kNoBracket;  // no table (np < 30)
+    float pw = 0.f;
     const int np = __ldg(T.np + g);
     if (((P.brmask >> g) & 1u) && np >= 30) {
       const float pq = c.formod == 0 ? (float)L.cgp[g * L.cap + q] : (float)L.p[q];
@@ -245,9 +274,18 @@ __global__ void k_pack_tiles(CtlDev c, TblDev T, LosDev L, MixedPlan P, long lon
         const int it0 = bracket_regf(t0g, nt0, tq);
         const int it1 = bracket_regf(t0g + T.tt, nt1, tq);
         wd = (unsigned)ipr | ((unsigned)it0 << 10) | ((unsigned)it1 << 20);
+        if (c.formod == 0) {  // pressure weight of intpol_tbl_cga (log-linear)
+          const float* pg = T.pf + (long long)g * T.tp;
+          const float pa = pg[ipr], pb = pg[ipr + 1];
+          if (pq / pa > 0.f && pb / pa > 0.f)
+            pw = __logf(pq / pa) / __logf(pb / pa);
+          else
+            pw = (pq - pa) / (pb - pa);
+        }
       }
     }
     out[(F.br0 + g) * 32] = __uint_as_float(wd);
+    if (c.formod == 0) out[(F.pw0 + g) * 32] = pw;
   }
 }
 
@@ -283,11 +321,12 @@ struct GasState {
 // jurassic.c:3710-3891).  Returns the segment emissivity; *sat is set where
 // the reference's segment transmittance becomes zero.
 // brw: packed bracket precomputed for the LOS point (grids shared by all
-// channels), or kNoBracket | 1 to search here.
+// channels), or kNoBracket | 1 to search here; wpre: in CGA the pressure
+// weight precomputed with it.
 template <bool CGA>
 __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, float pq,
                                            float tq, float du, float ucg, unsigned brw,
-                                           GasState& s, bool& sat) {
+                                           float wpre, GasState& s, bool& sat) {
   constexpr bool cga = CGA;
   const bool pre = brw != (kNoBracket | 1u);
   if (pre && brw == kNoBracket) return 0.f;   // np < 30
@@ -310,8 +349,12 @@ __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, float 
     ipr = (int)(brw & 1023u);
     it0 = (int)((brw >> 10) & 1023u);
     it1 = (int)((brw >> 20) & 1023u);
-    pa = __ldg(pg + ipr);
-    pb = __ldg(pg + ipr + 1);
+    if (cga) {
+      pa = pb = 0.f;
+    } else {
+      pa = __ldg(pg + ipr);
+      pb = __ldg(pg + ipr + 1);
+    }
   } else {
     const int* ntg = T.nt + dg * T.tp;
     const Bracket pb_ = pbracket_f(pg, np, pq, s.ipr);
@@ -327,8 +370,8 @@ __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, float 
   const unsigned rp = (unsigned)dg * (unsigned)T.tp + (unsigned)ipr;
   const unsigned ra = rp * (unsigned)T.tt + (unsigned)it0;
   const unsigned rc = (rp + 1u) * (unsigned)T.tt + (unsigned)it1;
-  const RowF r00 = rowf_at(T, ra), r01 = rowf_at(T, ra + 1u);
-  const RowF r10 = rowf_at(T, rc), r11 = rowf_at(T, rc + 1u);
+  const RowF r00 = rowf_at<CGA>(T, ra), r01 = rowf_at<CGA>(T, ra + 1u);
+  const RowF r10 = rowf_at<CGA>(T, rc), r11 = rowf_at<CGA>(T, rc + 1u);
   if (r00.n < 2 || r01.n < 2 || r10.n < 2 || r11.n < 2) return 0.f;
   const float e00 = corner_eps<CGA>(T, r00, s.e, du, ucg, s.h[0]);
   const float e01 = corner_eps<CGA>(T, r01, s.e, du, ucg, s.h[1]);
@@ -338,7 +381,9 @@ __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, float 
   const float ea = e00 + (e01 - e00) / (tb - ta) * (tq - ta);
   const float eb = e10 + (e11 - e10) / (td - tc) * (tq - tc);
   float w;
-  if (cga && pq / pa > 0.f && pb / pa > 0.f)
+  if (cga && pre)
+    w = wpre;
+  else if (cga && pq / pa > 0.f && pb / pa > 0.f)
     w = __logf(pq / pa) / __logf(pb / pa);
   else
     w = (pq - pa) / (pb - pa);
@@ -494,11 +539,12 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
         const float pq = cga ? f[(F.cgp0 + g) * 32] : p;
         const float tq = cga ? f[(F.cgt0 + g) * 32] : t;
         const float ucg = cga ? f[(F.cgu0 + g) * 32] : 0.f;
-        const unsigned brw = ((P.brmask >> g) & 1u) ? __float_as_uint(f[(F.br0 + g) * 32])
-                                                     : (kNoBracket | 1u);
+        const bool brg = (P.brmask >> g) & 1u;
+        const unsigned brw = brg ? __float_as_uint(f[(F.br0 + g) * 32]) : (kNoBracket | 1u);
+        const float wpre = cga && brg ? f[(F.pw0 + g) * 32] : 0.f;
         GasState st = sload(g);
         const long long dg = dg0 + g;  // (channel, emitter)
-        eg = gas_eps_f<CGA>(T, dg, pq, tq, du, ucg, brw, st, sat);
+        eg = gas_eps_f<CGA>(T, dg, pq, tq, du, ucg, brw, wpre, st, sat);
         sstore(g, st);
       }
       E = E + (1.f - E) * eg;
@@ -664,29 +710,30 @@ __global__ void __launch_bounds__(128) k_path_gas(CtlDev c, TblDev T, BatchDev b
     const float tq = cga ? f[(F.cgt0 + g) * 32] : f[F.t * 32];
     const float ucg = cga ? f[(F.cgu0 + g) * 32] : 0.f;
     const unsigned brw = brbit ? __float_as_uint(f[(F.br0 + g) * 32]) : (kNoBracket | 1u);
+    const float wpre = cga && brbit ? f[(F.pw0 + g) * 32] : 0.f;
     bool sat = false;
-    const float eg = gas_eps_f<CGA>(T, dg, pq, tq, du, ucg, brw, st, sat);
+    const float eg = gas_eps_f<CGA>(T, dg, pq, tq, du, ucg, brw, wpre, st, sat);
     const long long o = seg0 + ip * segstride;
     P.seg_eps[o] = eg;
     P.seg_sat[o] = sat ? 1 : 0;
   }
 }
 
-// First and last entries of every table row in one float4 (rows with fewer
-// than two entries are never interpolated and get zeros).
-// Row records of the mixed path, two float4 per row (ip, it):
-// {u[0], u[n-1], eps[0], eps[n-1]} and {n (int bits), t[ip][it], 0, 0}.
+// Row records of the mixed path (layouts at rowf_at); rows with fewer than
+// two entries are never interpolated and get zeros.
 __global__ void k_rowmeta(long long nrow, int tu, const int* nu, const float* u, const float* e,
-                          const float* tf, float4* meta) {
+                          const float* tf, int cga, float4* meta) {
   const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrow) return;
   const int n = nu[r];
-  float4 m = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (n >= 2) {
-    const float* ur = u + r * tu;
-    const float* er = e + r * tu;
-    m = make_float4(ur[0], ur[n - 1], er[0], er[n - 1]);
+  const float* ur = u + r * tu;
+  const float* er = e + r * tu;
+  if (cga) {
+    meta[r] = make_float4(__int_as_float(n), tf[r], n >= 2 ? ur[0] : 0.f, n >= 2 ? er[0] : 0.f);
+    return;
   }
+  float4 m = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (n >= 2) m = make_float4(ur[0], ur[n - 1], er[0], er[n - 1]);
   meta[2 * r] = m;
   meta[2 * r + 1] = make_float4(__int_as_float(n), tf[r], 0.f, 0.f);
 }
@@ -698,10 +745,10 @@ __global__ void k_interleave(long long n, const float* u, const float* e, float2
 }
 
 void launch_rowmeta(long long nrow, int tu, const int* nu, const float* u, const float* e,
-                    const float* tf, float4* meta, float2* ue, cudaStream_t s) {
+                    const float* tf, int cga, float4* meta, float2* ue, cudaStream_t s) {
   const int bs = 256;
   if (nrow > 0) {
-    k_rowmeta<<<(unsigned)((nrow + bs - 1) / bs), bs, 0, s>>>(nrow, tu, nu, u, e, tf, meta);
+    k_rowmeta<<<(unsigned)((nrow + bs - 1) / bs), bs, 0, s>>>(nrow, tu, nu, u, e, tf, cga, meta);
     const long long n = nrow * tu;
     k_interleave<<<(unsigned)((n + bs - 1) / bs), bs, 0, s>>>(n, u, e, ue);
   }
