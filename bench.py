@@ -301,7 +301,8 @@ def run_normal(args, rank, world, local, pg):
     """Normal-equation products alone (matrix_product, retrieval.c:403-444):
     nobs problems with m = 150 measurements and n = 405 state elements
     (the shapes of the Jacobian workload), seeded K with the magnitudes of
-    radiance Jacobians; 3xTF32 (tensor cores, mma.sync m16n8k8) and FP64."""
+    radiance Jacobians; 3xTF32 (tcgen05 tensor cores, TMEM accumulators)
+    and FP64."""
     import ctypes as C
     from jurassic_gb300 import native, synth
     from jurassic_gb300.model import Ctl

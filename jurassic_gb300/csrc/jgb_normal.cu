@@ -3,16 +3,18 @@
 // (matrix_product, retrieval.c:403-444, and the gsl_blas_dgemv of
 // retrieval.c:573-577), batched over retrievals of different sizes.
 //
-// Mixed precision: 3xTF32 on the tensor cores.  Every operand x = sqrt(W)K is
-// split into a TF32 head and a TF32 residual (x = hi + lo); the product uses
+// Mixed precision: 3xTF32 on the 5th-generation tensor cores (tcgen05, FP32
+// accumulators in tensor memory).  Every operand x = sqrt(W)K is split into
+// a TF32 head and a TF32 residual (x = hi + lo); the product uses
 // hi*hi + hi*lo + lo*hi with FP32 accumulation, which recovers ~FP32
 // accuracy from TF32 inputs.  dy is appended to K as column n so that b is
-// the last column of the same product.  Only the lower triangle of output
+// the last row of the same product.  Only the lower triangle of output
 // tiles is computed; the upper one is mirrored.
 //
 // FP64: the same products on the FP64 pipes (the plain reference arithmetic).
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <map>
 #include <mutex>
 #include <utility>
@@ -25,8 +27,12 @@ namespace jgb {
 
 namespace {
 
-constexpr int kTile = 64;   // output tile (kTile x kTile) per block
-constexpr int kChunk = 32;  // rows of K per smem stage
+constexpr int kTile = 128;  // output tile (kTile x kTile) per block
+constexpr int kChunk = 16;  // rows of X per shared-memory stage
+constexpr int kPlaneBytes = kTile * kChunk * 4;  // one operand plane of a stage (8 KB)
+constexpr int kStageBytes = 4 * kPlaneBytes;     // A hi, A lo, B hi, B lo
+constexpr int kTcSmem = 2 * kStageBytes + 64;    // two stages, barriers, TMEM address
+constexpr int kHalf = kTile / 2;                 // epilogue columns per pass
 
 struct NeDesc {
   int m, n;                 // rows of K, columns of K (state size)
@@ -40,12 +46,52 @@ __device__ __forceinline__ unsigned tf32_of(float x) {
   return r;
 }
 
-__device__ __forceinline__ void mma_tf32(float* c, const unsigned* a, const unsigned* b) {
+__device__ unsigned g_tc_err;  // a tensor-core wait gave up (results invalid)
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Byte offset of element (row, k) in a 128 x kChunk K-major operand plane of
+// 8-row x 16-byte core matrices: [k / 8][row / 8][k % 8 / 4][row % 8][k % 4];
+// one MMA (K = 8 TF32) reads a [row / 8][2 core matrices] slice of 4 KB.
+__device__ __forceinline__ int tc_off(int row, int k) {
+  return (k >> 3) * 4096 + (row >> 3) * 256 + ((k & 7) >> 2) * 128 + (row & 7) * 16 + (k & 3) * 4;
+}
+
+// Shared-memory matrix descriptor of such a slice (no swizzle): start
+// address >> 4, leading byte offset 128 (the two core matrices along K),
+// stride byte offset 256 (8-row groups), descriptor version 0b001 at bit 46.
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(128u >> 4) << 16) |
+         ((uint64_t)(256u >> 4) << 32) | ((uint64_t)1 << 46);
+}
+
+// Instruction descriptor of kind::tf32: FP32 accumulator, TF32 A and B, both
+// K-major, N = M = kTile.
+constexpr uint32_t kTcIdesc = (1u << 4) | (2u << 7) | (2u << 10) |
+                              ((uint32_t)(kTile >> 3) << 17) | ((uint32_t)(kTile >> 4) << 24);
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t acc) {
   asm volatile(
-      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 "
-      "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(kTcIdesc), "r"(acc));
+}
+
+// Bounded wait for phase `parity` of an mbarrier.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+  for (int it = 0; it < (1 << 20); it++) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
 }
 
 // Exact float -> double widening with integer operations (the FP64 pipe of
@@ -62,8 +108,8 @@ __device__ __forceinline__ double f2d_bits(float f) {
 }
 
 // X = sqrt(W)[K | dy] of every problem, formed once in FP64 and split into
-// a TF32 high part and an FP32 remainder (row-major m x (n+1) per problem):
-// one block per row, threads over the columns.
+// a TF32 high part and a TF32-rounded remainder (row-major m x (n+1) per
+// problem): one block per row, threads over the columns.
 __global__ void k_split_x(const NeDesc* desc, const double* Kall, const double* wall,
                           const double* dyall, float* xhi, float* xlo) {
   const NeDesc d = desc[blockIdx.y];
@@ -77,17 +123,26 @@ __global__ void k_split_x(const NeDesc* desc, const double* Kall, const double* 
       const float x = (float)(v * wr);
       const float hi = __uint_as_float(tf32_of(x));
       xhi[o + col] = hi;
-      xlo[o + col] = x - hi;
+      xlo[o + col] = __uint_as_float(tf32_of(x - hi));
     }
   }
 }
 
-// One block: output tile (ti, tj) with ti >= tj of retrieval blockIdx.z.
-// 4 warps in a 2x2 arrangement, each a 32x32 sub-tile = 2 (M16) x 4 (N8)
-// mma tiles.
-__global__ void __launch_bounds__(128) k_normal_3xtf32(const NeDesc* desc, const float* xhi,
-                                                       const float* xlo, double* Aall,
-                                                       double* ball) {
+// One CTA: output tile (ti, tj), ti >= tj, of problem blockIdx.z, C = X^T X
+// over the augmented columns.  Rows of X stream through two shared-memory
+// stages of kChunk rows (A = columns of tile ti, B = columns of tile tj; on
+// a diagonal tile B is A), copied element by element with cp.async straight
+// into the core-matrix layout while the previous stage is multiplied.  One
+// thread issues the 3 x 2 tcgen05.mma of a stage into a 128 x 128 FP32
+// accumulator in tensor memory and commits them to the stage's mbarrier,
+// which the threads wait on before refilling the stage.  The accumulator is
+// read back with tcgen05.ld in two column halves, staged in shared memory,
+// and written as FP64 with coalesced rows (direct and mirrored).  64 KB of
+// shared memory: three CTAs per SM.
+__global__ void __launch_bounds__(128, 3) k_normal_tc(const NeDesc* desc, const float* xhi,
+                                                      const float* xlo, double* Aall,
+                                                      double* ball) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
   const NeDesc d = desc[blockIdx.z];
   const int na = d.n + 1;  // augmented columns
   const int nt = (na + kTile - 1) / kTile;
@@ -98,89 +153,146 @@ __global__ void __launch_bounds__(128) k_normal_3xtf32(const NeDesc* desc, const
     ti++;
   }
   const int tj = t;
-  if (ti >= nt) return;
+  if (ti >= nt) return;  // the whole CTA, before any barrier or tensor memory
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const bool diag = ti == tj;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(tc_smem + 2 * kStageBytes);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tc_smem + 2 * kStageBytes + 16);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[1])));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(kTile));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
   const float* XH = xhi + d.xoff;
   const float* XL = xlo + d.xoff;
-  __shared__ float hi_i[kChunk][kTile + 8], lo_i[kChunk][kTile + 8];  // +8: conflict-free fragment reads
-  __shared__ float hi_j[kChunk][kTile + 8], lo_j[kChunk][kTile + 8];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int wr = (warp >> 1) * 32, wc = (warp & 1) * 32;  // warp sub-tile origin
-  const int g = lane >> 2, tg = lane & 3;
-  float acc[2][4][4];
-#pragma unroll
-  for (int a = 0; a < 2; a++)
-#pragma unroll
-    for (int b = 0; b < 4; b++)
-#pragma unroll
-      for (int c = 0; c < 4; c++) acc[a][b][c] = 0.f;
-
-  for (int k0 = 0; k0 < d.m; k0 += kChunk) {
-    __syncthreads();
-    for (int idx = threadIdx.x; idx < kChunk * kTile; idx += blockDim.x) {
-      const int r = idx / kTile, cidx = idx % kTile;
-      const int row = k0 + r, ci = ti * kTile + cidx, cj = tj * kTile + cidx;
+  const int ci = ti * kTile + tid, cj = tj * kTile + tid;  // this thread's columns
+  const bool iin = ci < na, jin = cj < na;
+  const int nch = (d.m + kChunk - 1) / kChunk;
+  const uint32_t sbase = smem_u32(tc_smem);
+  // cp.async of chunk c into stage st (4-byte copies; out-of-range elements
+  // are zero-filled from the problem's first element)
+  auto load = [&](int c, int st) {
+    const uint32_t base = sbase + st * kStageBytes;
+#pragma unroll 4
+    for (int k = 0; k < kChunk; k++) {
+      const int row = c * kChunk + k;
       const bool rin = row < d.m;
       const long long o = (long long)row * na;
-      hi_i[r][cidx] = (rin && ci < na) ? __ldg(XH + o + ci) : 0.f;
-      lo_i[r][cidx] = (rin && ci < na) ? __ldg(XL + o + ci) : 0.f;
-      hi_j[r][cidx] = (rin && cj < na) ? __ldg(XH + o + cj) : 0.f;
-      lo_j[r][cidx] = (rin && cj < na) ? __ldg(XL + o + cj) : 0.f;
+      const uint32_t off = (uint32_t)tc_off(tid, k);
+      const uint32_t ni = rin && iin ? 4u : 0u, nj = rin && jin ? 4u : 0u;
+      const float* hi = ni ? XH + o + ci : XH;
+      const float* lo = ni ? XL + o + ci : XL;
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(base + off), "l"(hi), "r"(ni));
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(base + kPlaneBytes + off),
+                   "l"(lo), "r"(ni));
+      if (!diag) {
+        const float* hj = nj ? XH + o + cj : XH;
+        const float* lj = nj ? XL + o + cj : XL;
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(base + 2 * kPlaneBytes + off),
+                     "l"(hj), "r"(nj));
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(base + 3 * kPlaneBytes + off),
+                     "l"(lj), "r"(nj));
+      }
     }
+  };
+  bool ok = true;
+  load(0, 0);
+  asm volatile("cp.async.commit_group;");
+  for (int c = 0; c < nch; c++) {
+    const int st = c & 1;
+    if (c + 1 < nch) {
+      // the other stage's MMAs (chunk c - 1) must be done before refilling it
+      if (c >= 1) ok = mbar_wait(smem_u32(&mbar[st ^ 1]), ((c - 1) >> 1) & 1);
+      ok = __syncthreads_and(ok);
+      if (!ok) break;
+      load(c + 1, st ^ 1);
+    }
+    asm volatile("cp.async.commit_group;");
+    asm volatile("cp.async.wait_group 1;");  // chunk c has landed
+    asm volatile("fence.proxy.async.shared::cta;");  // generic writes -> tensor-core reads
     __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t a0 = sbase + st * kStageBytes;
+      const uint32_t b0 = diag ? a0 : a0 + 2 * kPlaneBytes;
 #pragma unroll
-    for (int kk = 0; kk < kChunk; kk += 8) {
-      // A fragments: rows = output rows (columns of X in tile i), cols = k
-      unsigned ah[2][4], al[2][4];
-#pragma unroll
-      for (int a = 0; a < 2; a++) {
-        const int r0 = wr + a * 16 + g;
-        ah[a][0] = tf32_of(hi_i[kk + tg][r0]);
-        ah[a][1] = tf32_of(hi_i[kk + tg][r0 + 8]);
-        ah[a][2] = tf32_of(hi_i[kk + tg + 4][r0]);
-        ah[a][3] = tf32_of(hi_i[kk + tg + 4][r0 + 8]);
-        al[a][0] = tf32_of(lo_i[kk + tg][r0]);
-        al[a][1] = tf32_of(lo_i[kk + tg][r0 + 8]);
-        al[a][2] = tf32_of(lo_i[kk + tg + 4][r0]);
-        al[a][3] = tf32_of(lo_i[kk + tg + 4][r0 + 8]);
+      for (int s = 0; s < kChunk / 8; s++) {
+        const uint64_t ah = tc_desc(a0 + s * 4096), al = tc_desc(a0 + kPlaneBytes + s * 4096);
+        const uint64_t bh = tc_desc(b0 + s * 4096), bl = tc_desc(b0 + kPlaneBytes + s * 4096);
+        tc_mma(tmem, al, bh, (c | s) != 0);
+        tc_mma(tmem, ah, bl, 1u);
+        tc_mma(tmem, ah, bh, 1u);
       }
-#pragma unroll
-      for (int bq = 0; bq < 4; bq++) {
-        const int c0 = wc + bq * 8 + g;
-        unsigned bh[2], bl[2];
-        bh[0] = tf32_of(hi_j[kk + tg][c0]);
-        bh[1] = tf32_of(hi_j[kk + tg + 4][c0]);
-        bl[0] = tf32_of(lo_j[kk + tg][c0]);
-        bl[1] = tf32_of(lo_j[kk + tg + 4][c0]);
-#pragma unroll
-        for (int a = 0; a < 2; a++) {
-          mma_tf32(acc[a][bq], al[a], bh);
-          mma_tf32(acc[a][bq], ah[a], bl);
-          mma_tf32(acc[a][bq], ah[a], bh);
-        }
-      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_u32(&mbar[st])));
     }
   }
-  // store: rows/cols < n go to A (and the mirror), column n goes to b
-  double* A = Aall + d.aoff;
-  double* bv = ball + d.boff;
+  asm volatile("cp.async.wait_all;");
+  // the last commit tracks every MMA of the tile
+  if (ok && nch > 0) ok = mbar_wait(smem_u32(&mbar[(nch - 1) & 1]), ((nch - 1) >> 1) & 1);
+  ok = __syncthreads_and(ok);
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (ok) {
+    double* A = Aall + d.aoff;
+    double* bv = ball + d.boff;
+    float* tile = reinterpret_cast<float*>(tc_smem);  // [128][kHalf + 1]
+    for (int h = 0; h < 2; h++) {
+      // accumulator rows 32 warp + lane, columns h kHalf ... -> shared tile
+      for (int c0 = 0; c0 < kHalf; c0 += 8) {
+        uint32_t r[8];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+              "=r"(r[7])
+            : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(h * kHalf + c0)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-  for (int a = 0; a < 2; a++)
-#pragma unroll
-    for (int bq = 0; bq < 4; bq++)
-#pragma unroll
-      for (int c = 0; c < 4; c++) {
-        const int row = ti * kTile + wr + a * 16 + g + (c >= 2 ? 8 : 0);
-        const int col = tj * kTile + wc + bq * 8 + 2 * tg + (c & 1);
-        const double v = f2d_bits(acc[a][bq][c]);
-        if (row < d.n && col < d.n) {
-          if (row >= col) {
+        for (int j = 0; j < 8; j++)
+          tile[(warp * 32 + lane) * (kHalf + 1) + c0 + j] = __uint_as_float(r[j]);
+      }
+      __syncthreads();
+      // rows >= columns (and b, the augmented row n), threads along a row
+      for (int r = warp; r < kTile; r += 4) {
+        const int row = ti * kTile + r;
+        for (int cc = lane; cc < kHalf; cc += 32) {
+          const int col = tj * kTile + h * kHalf + cc;
+          if (col >= d.n || row > d.n) continue;
+          const double v = f2d_bits(tile[r * (kHalf + 1) + cc]);
+          if (row == d.n)
+            bv[col] = v;
+          else if (row >= col)
             A[(long long)row * d.n + col] = v;
-            A[(long long)col * d.n + row] = v;
-          }
-        } else if (row == d.n && col < d.n) {
-          bv[col] = v;
         }
       }
+      // mirrored entries, threads along a row of the upper triangle
+      for (int cc = warp; cc < kHalf; cc += 4) {
+        const int col = tj * kTile + h * kHalf + cc;
+        for (int r = lane; r < kTile; r += 32) {
+          const int row = ti * kTile + r;
+          if (row < d.n && col < d.n && row > col)
+            A[(long long)col * d.n + row] = f2d_bits(tile[r * (kHalf + 1) + cc]);
+        }
+      }
+      __syncthreads();
+    }
+  } else if (tid == 0) {
+    atomicOr(&g_tc_err, 1u);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTile));
 }
 
 // FP64 reference products: one thread per lower-triangle element (+ b).
@@ -279,8 +391,14 @@ int normal_equations_dev(int nret, const int* m, const int* n, const double* K, 
     const NeDesc* dd = static_cast<const NeDesc*>(desc_dev);
     k_split_x<<<dim3((unsigned)(maxm < 1024 ? maxm : 1024), nsel), 128, 0, s>>>(dd, K, w, dy, xbuf,
                                                                                   xbuf + xo);
+    cudaFuncSetAttribute(k_normal_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+    const unsigned zero = 0;
+    cudaMemcpyToSymbolAsync(g_tc_err, &zero, sizeof(zero), 0, cudaMemcpyHostToDevice, s);
     dim3 grid(maxtiles, 1, nsel);
-    k_normal_3xtf32<<<grid, 128, 0, s>>>(dd, xbuf, xbuf + xo, A, b);
+    k_normal_tc<<<grid, 128, kTcSmem, s>>>(dd, xbuf, xbuf + xo, A, b);
+    unsigned herr = 0;
+    cudaMemcpyFromSymbolAsync(&herr, g_tc_err, sizeof(herr), 0, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess || herr) return JGB_ERR_CUDA;
   } else {
     const long long nel = (long long)maxn * (maxn + 1) / 2 + maxn;
     dim3 grid((unsigned)((nel + 127) / 128 < 4096 ? (nel + 127) / 128 : 4096), nsel);
