@@ -96,6 +96,9 @@ typedef struct {
                                     pass, 2 = count + fill, 3 = a capacity
                                     bound was exceeded and the rays were
                                     counted */
+  double resume_skip;            /* share of the perturbed rays' LOS points
+                                    taken from their bases (resumed
+                                    Jacobian chunks; 0 otherwise) */
 } jgb_stats;
 
 /* Context: replaces the process-global table state initialised by the first
@@ -136,6 +139,17 @@ int jgb_set_los_bound_scale(jgb_ctx *ctx, double scale);
    default) decides by that size, 0 never splits, 1 always does.  The results
    do not depend on it. */
 int jgb_set_path_split(jgb_ctx *ctx, int mode);
+
+/* Mixed-precision finite-difference Jacobians: a perturbation of a level
+   value leaves the line of sight and the path state unchanged until the ray
+   comes within half a step of the neighbouring levels, so the perturbed
+   path restarts from its unperturbed base's saved state there (exact; not
+   with hydrostatic pressures, a field of view or surface reflection).  The
+   bases run first and the lanes of a warp walk the union of their ranges,
+   so it pays on large batches: mode 1 (default) resumes a Jacobian chunk
+   when the estimated schedule of its tiles is shorter, 2 always, 0 never.
+   The results do not depend on it. */
+int jgb_set_fd_resume(jgb_ctx *ctx, int mode);
 
 /* Source function of channel id from its filter function
    (init_srcfunc, jurassic.c:3631-3681), computed on the device. */

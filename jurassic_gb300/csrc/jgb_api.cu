@@ -179,19 +179,82 @@ __global__ void k_iota(int n, int* v) {
   if (i < n) v[i] = i;
 }
 
-// tile plan from the rays in sort order (descending key)
-__global__ void k_tiles(int nray, int ntile, const int* count, const int* sorted_ray, int* perm,
-                        int* tlen, long long* tpts) {
+// tile plan from the rays in sort order (descending key): the first nfirst
+// rays fill tiles [0, tfirst), the others start a new tile (two groups that
+// never share a tile; nfirst = nray, tfirst = ntile: one group)
+__global__ void k_tiles(int nray, int ntile, int nfirst, int tfirst, const int* count,
+                        const int* sorted_ray, int* perm, int* tlen, long long* tpts) {
   const int tile = blockIdx.x * blockDim.x + threadIdx.x;
   if (tile >= ntile) return;
+  const int k0 = tile < tfirst ? tile * 32 : nfirst + (tile - tfirst) * 32;
+  const int k1 = tile < tfirst ? min(k0 + 32, nfirst) : min(k0 + 32, nray);
   int mx = 0;
   for (int l = 0; l < 32; l++) {
-    const int k = tile * 32 + l;
-    perm[tile * 32 + l] = k < nray ? sorted_ray[k] : -1;
-    if (k < nray) mx = max(mx, count[sorted_ray[k]]);
+    const int k = k0 + l;
+    perm[tile * 32 + l] = k < k1 ? sorted_ray[k] : -1;
+    if (k < k1) mx = max(mx, count[sorted_ray[k]]);
   }
   tlen[tile] = mx;
   tpts[tile] = mx;
+}
+
+// Resume point of every ray of a batch of perturbations (ResumeSpec).  A
+// perturbed level value changes the atmosphere only on the two intervals
+// next to it, [z_lo, z_hi].  The position of LOS point p + 1 depends on the
+// refraction evaluated between points p and p + 1 (the step's midpoint and
+// sub-points 20 m away), whose altitudes lie within the segment's end
+// altitudes less its curvature sag (metres) and the 20 m offsets; the data
+// of point p on its own altitude.  So while segments stay margin away from
+// [z_lo, z_hi], the perturbed ray's points and their data equal the base
+// ray's, and the path state before the first segment that comes closer is
+// the base's (one point earlier is taken as a safety margin).  Bases, and
+// perturbations of other than level values, start at 0.
+__global__ void k_resume_points(int nray, BatchDev b, LosDev L, int nbase, const int4* pert,
+                                const int* base_obs, const int* ray_off, double margin,
+                                int* start) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nray) return;
+  const int e = b.ray_obs[r];
+  const int4 pr = pert[e];
+  if (e < nbase || pr.x < 0 || pr.x > 3) {
+    start[r] = 0;
+    return;
+  }
+  const int eb = base_obs[e];
+  const int rb = ray_off[eb] + (r - ray_off[e]);
+  const int l0 = b.lev_off[e], nl = b.lev_off[e + 1] - l0;
+  const double z1 = b.z[l0 + max(pr.z - 1, 0)], z2 = b.z[l0 + min(pr.z + 1, nl - 1)];
+  const double lo = fmin(z1, z2) - margin, hi = fmax(z1, z2) + margin;
+  const int n = min(L.count[rb], L.count[r]);
+  const double* zb = L.z + L.off[rb];
+  int p0 = n;
+  for (int p = 0; p < n; p++) {
+    const double za = zb[p], zc = p + 1 < n ? zb[p + 1] : za;
+    if (fmin(za, zc) <= hi && fmax(za, zc) >= lo) {
+      p0 = p;
+      break;
+    }
+  }
+  start[r] = max(p0 - 1, 0);
+}
+
+// Sort key of a resumed batch: bases first (their tiles run first and save
+// the states), then by measured channels, by the LOS points left to do in
+// 64-point buckets (longest first, so that no long warp is left for the
+// end) and by start point in 16-point buckets (so that the lanes of a warp
+// walk nearly the same range of points).
+__global__ void k_resume_keys(int nray, int nbase_rays, int nd, const unsigned char* mask,
+                              int skip_masked, const int* count, const int* start, int* key) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nray) return;
+  int m = nd;
+  if (skip_masked) {
+    m = 0;
+    for (int id = 0; id < nd; id++) m += mask[(long long)id * nray + r] ? 0 : 1;
+  }
+  const int left = count[r] - start[r];
+  key[r] = ((r < nbase_rays ? 1 : 0) << 30) | (min(m, 511) << 21) | (min(left >> 6, 127) << 14) |
+           (min(start[r] >> 4, 255) << 6);
 }
 
 // Sort key of a batch whose masked pairs are skipped: rays with the same
@@ -222,6 +285,7 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
   const int nray = b.nray;
   CK(x->err_word.reserve(sizeof(unsigned)));
   unsigned* d_err = x->err_word.as<unsigned>();
+  x->stats.resume_skip = 0.0;
   CK(cudaMemsetAsync(d_err, 0, sizeof(unsigned), s));
   if (!timed_h2d) CK(cudaEventRecord(x->ev[1], s));
 
@@ -377,8 +441,125 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
                      c.formod == 0, x->t_meta.as<float4>(), x->t_ue.as<float2>(), s);
       x->meta_stale = false;
     }
-    // tile plan: rays sorted by LOS length, 32 per tile
-    const int ntile = (nray + 31) / 32;
+    // resumed perturbations: start points and the base rays' snapshot lists
+    const ResumeSpec* rs = x->resume;
+    const int nchb = (c.nd + 3) / 4;
+    int nbase_rays = nray, tfirst = 0;
+    double resume_skip = 0.0;
+    int* rstart = nullptr;
+    int *snap_off = nullptr, *snap_ip = nullptr, *snap_ray = nullptr;
+    if (rs) {
+      nbase_rays = rs->h_ray_off[rs->nbase];
+      CK(x->rs_start.reserve(sizeof(int) * (size_t)nray));
+      rstart = x->rs_start.as<int>();
+      k_resume_points<<<(nray + 127) / 128, 128, 0, s>>>(nray, b, L, rs->nbase, rs->pert,
+                                                          rs->base_obs, rs->ray_off,
+                                                          0.05, rstart);
+      CK(cudaGetLastError());
+      CK(x->tiles_keys.reserve(sizeof(int) * (size_t)nray));
+      k_resume_keys<<<(nray + 255) / 256, 256, 0, s>>>(nray, nbase_rays, c.nd, b.mask, b.skip_masked,
+                                                        L.count, rstart, x->tiles_keys.as<int>());
+      std::vector<int> hs(nray), ray_obs(nray), hc(nray), hk(nray);
+      CK(cudaMemcpyAsync(hs.data(), rstart, sizeof(int) * nray, cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(hc.data(), L.count, sizeof(int) * nray, cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(hk.data(), x->tiles_keys.p, sizeof(int) * nray, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      long long skipped = 0, points = 0;
+      for (int r = nbase_rays; r < nray; r++) {
+        skipped += hs[r];
+        points += hc[r];
+      }
+      resume_skip = points > 0 ? (double)skipped / (double)points : 0.0;
+      // Does resuming pay?  Lanes of a warp walk the union of their point
+      // ranges, and the base tiles run before the others.  Estimate both
+      // schedules from their tile plans: a group of tiles takes the longer
+      // of its work over the tiles the device holds at once and its longest
+      // tile.
+      const double conc = std::max(1.0, (double)x->sms * 8.0 / nchb);
+      double waves = 0;  // of the plain plan: work over the longest tile
+      auto group_time = [&](const std::vector<int>& order, int k0, int k1, bool resumed) {
+        double sum = 0, mx = 0;
+        for (int t = k0; t < k1; t += 32) {
+          int hi = 0, lo = 1 << 30;
+          for (int l = t; l < std::min(t + 32, k1); l++) {
+            hi = std::max(hi, hc[order[l]]);
+            lo = std::min(lo, resumed ? hs[order[l]] : 0);
+          }
+          sum += hi - lo;
+          mx = std::max(mx, (double)(hi - lo));
+        }
+        waves = mx > 0 ? sum / conc / mx : 0;
+        return std::max(sum / conc, mx);
+      };
+      std::vector<int> ord(nray);
+      for (int r = 0; r < nray; r++) ord[r] = r;
+      std::stable_sort(ord.begin(), ord.end(), [&](int a, int b2) { return hk[a] > hk[b2]; });
+      const double t_res = group_time(ord, 0, nbase_rays, false) + group_time(ord, nbase_rays, nray, true);
+      // the plain plan: measured channels (key bits 21-29), then LOS length
+      std::stable_sort(ord.begin(), ord.end(), [&](int a, int b2) {
+        const int ma = (hk[a] >> 21) & 511, mb = (hk[b2] >> 21) & 511;
+        return ma != mb ? ma > mb : hc[a] > hc[b2];
+      });
+      const double t_plain = group_time(ord, 0, nray, false);
+      // measured: resumed chunks win on batches of many waves (2048 nadir
+      // observations x 405 perturbations: +50 %) and lose on the dozens of
+      // requests of a serving step, where the separate base tiles and the
+      // tail of the resumed tiles cost more than the skipped points save
+      if (x->fd_resume == 1 && !(t_res < 0.9 * t_plain && waves >= 32.0)) {
+        rs = nullptr;  // run the batch plainly (the base copies are computed too)
+        nbase_rays = nray;
+        resume_skip = 0.0;
+      }
+    }
+    if (rs) {
+      std::vector<int> hs(nray), ray_obs(nray);
+      CK(cudaMemcpyAsync(hs.data(), rstart, sizeof(int) * nray, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      for (int o = 0; o < b.nobs; o++)
+        for (int r = rs->h_ray_off[o]; r < rs->h_ray_off[o + 1]; r++) ray_obs[r] = o;
+      std::vector<int> off(nray + 1, 0);
+      std::vector<int> rb_of(nray, -1);
+      for (int r = nbase_rays; r < nray; r++)
+        if (hs[r] > 0) {
+          const int e = ray_obs[r], eb = rs->h_base_obs[e];
+          rb_of[r] = rs->h_ray_off[eb] + (r - rs->h_ray_off[e]);
+          off[rb_of[r] + 1]++;
+        }
+      for (int r = 0; r < nray; r++) off[r + 1] += off[r];
+      const int nsnap = off[nray];
+      std::vector<int> sip(nsnap), sray(nsnap), fill(off.begin(), off.end() - 1);
+      for (int r = nbase_rays; r < nray; r++)
+        if (rb_of[r] >= 0) {
+          const int k = fill[rb_of[r]]++;
+          sip[k] = hs[r];
+          sray[k] = r;
+        }
+      for (int rb = 0; rb < nbase_rays; rb++) {  // each list in point order
+        std::vector<std::pair<int, int>> v;
+        for (int k = off[rb]; k < off[rb + 1]; k++) v.emplace_back(sip[k], sray[k]);
+        std::sort(v.begin(), v.end());
+        for (size_t k = 0; k < v.size(); k++) {
+          sip[off[rb] + k] = v[k].first;
+          sray[off[rb] + k] = v[k].second;
+        }
+      }
+      CK(x->rs_lists.reserve(sizeof(int) * ((size_t)nray + 1 + 2 * (size_t)std::max(nsnap, 1))));
+      snap_off = x->rs_lists.as<int>();
+      snap_ip = snap_off + nray + 1;
+      snap_ray = snap_ip + std::max(nsnap, 1);
+      CK(cudaMemcpyAsync(snap_off, off.data(), sizeof(int) * (nray + 1), cudaMemcpyHostToDevice, s));
+      if (nsnap) {
+        CK(cudaMemcpyAsync(snap_ip, sip.data(), sizeof(int) * nsnap, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(snap_ray, sray.data(), sizeof(int) * nsnap, cudaMemcpyHostToDevice, s));
+      }
+      CK(x->rs_snap.reserve(sizeof(float) * (size_t)nray * c.nd * path_state_words(c)));
+      CK(cudaStreamSynchronize(s));  // the host lists go out of scope
+      tfirst = (nbase_rays + 31) / 32;
+    }
+    // tile plan: rays sorted by LOS length, 32 per tile (resumed batches:
+    // base tiles first)
+    const int ntile = rs ? tfirst + (nray - nbase_rays + 31) / 32 : (nray + 31) / 32;
+    if (!rs) tfirst = ntile;
     CK(x->tiles_keys.reserve(sizeof(int) * (size_t)nray));
     CK(x->tiles_keys2.reserve(sizeof(int) * (size_t)nray));
     CK(x->tiles_vals.reserve(sizeof(int) * 2 * (size_t)nray));
@@ -389,7 +570,11 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
     int* vals_out = vals_in + nray;
     k_iota<<<(nray + 255) / 256, 256, 0, s>>>(nray, vals_in);
     const int* keys = L.count;
-    if (b.skip_masked) {
+    if (rs) {
+      k_resume_keys<<<(nray + 255) / 256, 256, 0, s>>>(nray, nbase_rays, c.nd, b.mask, b.skip_masked,
+                                                        L.count, rstart, x->tiles_keys.as<int>());
+      keys = x->tiles_keys.as<int>();
+    } else if (b.skip_masked) {
       k_mask_keys<<<(nray + 255) / 256, 256, 0, s>>>(nray, c.nd, b.mask, L.count,
                                                       x->tiles_keys.as<int>());
       keys = x->tiles_keys.as<int>();
@@ -408,8 +593,10 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
     Pm.perm = x->tiles_perm.as<int>();
     Pm.tlen = x->tiles_len.as<int>();
     Pm.toff = toff;
-    k_tiles<<<(ntile + 127) / 128, 128, 0, s>>>(nray, ntile, L.count, vals_out, Pm.perm, Pm.tlen,
-                                                 tpts);
+    Pm.tile0 = 0;
+    Pm.tile1 = ntile;
+    k_tiles<<<(ntile + 127) / 128, 128, 0, s>>>(nray, ntile, rs ? nbase_rays : nray, tfirst, L.count,
+                                                 vals_out, Pm.perm, Pm.tlen, tpts);
     CK(cudaMemsetAsync(toff, 0, sizeof(long long), s));
     size_t sb2 = 0;
     cub::DeviceScan::InclusiveSum(nullptr, sb2, tpts, toff + 1, ntile, s);
@@ -432,11 +619,27 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
     // a batch with too few tiles to fill the device is latency-bound: split
     // the path over the emitters (ng warps per tile and channel)
     const long long split_warps = (long long)ntile * c.nd * c.ng;
-    const bool split = c.ng > 1 && (x->path_split == 1 ||
-                                    (x->path_split < 0 && split_warps <= 32LL * x->sms));
+    const bool split = !rs && c.ng > 1 &&
+                       (x->path_split == 1 || (x->path_split < 0 && split_warps <= 32LL * x->sms));
     Pm.seg_eps = nullptr;
     Pm.seg_sat = nullptr;
-    if (split) {
+    if (rs) {
+      // bases (saving the states), then the perturbations (starting from them)
+      Pm.start = rstart;
+      Pm.snap_off = snap_off;
+      Pm.snap_ip = snap_ip;
+      Pm.snap_ray = snap_ray;
+      Pm.snap = x->rs_snap.as<float>();
+      CK(cudaEventRecord(x->ev[4], s));
+      Pm.tile0 = 0;
+      Pm.tile1 = tfirst;
+      launch_path_resume(c, T, ch, bo, L, Pm, s);
+      Pm.tile0 = tfirst;
+      Pm.tile1 = ntile;
+      launch_path_resume(c, T, ch, bo, L, Pm, s);
+      launches += 9;
+      x->stats.resume_skip = resume_skip;
+    } else if (split) {
       const size_t nseg = (size_t)std::max(tile_points, 1LL) * c.nd * c.ng * 32;
       CK(x->seg.reserve(nseg * (sizeof(float) + 1)));
       Pm.seg_eps = x->seg.as<float>();
@@ -444,7 +647,7 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
       CK(cudaEventRecord(x->ev[4], s));
       launch_path_split(c, T, ch, bo, L, Pm, refl, s);
       launches += 7;
-    } else if (x->path_variant < 0) {
+    } else if (x->path_variant < 0 && !rs) {
       // autotune: time every variant on this batch (results are identical)
       const char* force = getenv("JGB_PATH_VARIANT");
       if (force) {
@@ -466,7 +669,7 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
         }
       }
     }
-    if (!split) {
+    if (!split && !rs) {
       CK(cudaEventRecord(x->ev[4], s));
       launch_path_mixed(c, T, ch, bo, L, Pm, refl, x->path_variant, s);
       launches += 6;
@@ -549,6 +752,10 @@ __global__ void k_perturb(int ne, const int4* pert, const int* eoff, long long n
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ne) return;
   const int4 pr = pert[e];
+  if (pr.x < 0) {  // an unperturbed base copy
+    hout[e] = 0.0;
+    return;
+  }
   double* v;
   const long long l = (long long)eoff[e] + pr.z;
   switch (pr.x) {
@@ -690,6 +897,13 @@ int fd_core(jgb_ctx* x, const FdLayout& H, const FdInput& in, const std::vector<
   const int nplanes = 6 + c.ng + c.nw;
   const long long nlev = H.lev_off[H.nobs], nray = H.ray_off[H.nobs];
   const long long budget = 60000000LL;
+  // Mixed-precision perturbations resume from their base's path state
+  // (run_core with a ResumeSpec): exact when nothing but the perturbed
+  // levels' neighbourhood changes the LOS, i.e. without hydrostatic
+  // pressures, a field of view or surface reflection (its sum runs over the
+  // whole path).
+  const bool resume = precision == JGB_MIXED && x->fd_resume && c.hydz < 0 && !c.fov &&
+                      !(c.sftype >= 2 && c.nsf > 0);
   size_t i0 = 0;
   while (i0 < list.size()) {
     long long pts = 0;
@@ -704,8 +918,28 @@ int fd_core(jgb_ctx* x, const FdLayout& H, const FdInput& in, const std::vector<
       i1++;
     }
     const int nob = (int)(i1 - i0);
-    std::vector<int> eoff_l(1, 0), eoff_r(1, 0), esrc, e0(nob);
+    std::vector<int> eoff_l(1, 0), eoff_r(1, 0), esrc, e0(nob), ebase;
     std::vector<int4> pert;
+    // by default only chunks of many tile waves resume (see run_core)
+    bool res_chunk = resume;
+    if (resume && x->fd_resume == 1) {
+      long long prays = 0;
+      for (size_t q = i0; q < i1; q++) {
+        const int o = list[q];
+        prays += (long long)H.ncnt[o] * (H.ray_off[o + 1] - H.ray_off[o]);
+      }
+      const double waves = (double)((prays + 31) / 32) * ((c.nd + 3) / 4) / (8.0 * x->sms);
+      res_chunk = waves >= 32.0;
+    }
+    if (res_chunk)  // unperturbed base copies first
+      for (size_t q = i0; q < i1; q++) {
+        const int o = list[q];
+        esrc.push_back(o);
+        eoff_l.push_back(eoff_l.back() + (H.lev_off[o + 1] - H.lev_off[o]));
+        eoff_r.push_back(eoff_r.back() + (H.ray_off[o + 1] - H.ray_off[o]));
+        pert.push_back(make_int4(-1, 0, 0, 0));
+        ebase.push_back((int)(q - i0));
+      }
     for (size_t q = i0; q < i1; q++) {
       const int o = list[q];
       e0[q - i0] = (int)esrc.size();
@@ -716,6 +950,7 @@ int fd_core(jgb_ctx* x, const FdLayout& H, const FdInput& in, const std::vector<
         eoff_l.push_back(eoff_l.back() + nl);
         eoff_r.push_back(eoff_r.back() + nr);
         pert.push_back(make_int4(el.arr, el.idx, el.arr == 4 ? el.idx : el.lev, el.hkind));
+        ebase.push_back(res_chunk ? (int)(q - i0) : 0);
       }
     }
     const int ne = (int)esrc.size();
@@ -779,7 +1014,20 @@ int fd_core(jgb_ctx* x, const FdLayout& H, const FdInput& in, const std::vector<
     k_mask<<<(unsigned)((nm + 255) / 256), 256, 0, s>>>(nm, rad_e, x->kx_mask.as<unsigned char>());
     CK(cudaGetLastError());
     CK(cudaEventRecord(x->ev[0], s));
+    ResumeSpec rsp{};
+    if (res_chunk) {
+      CK(x->rs_base.reserve(sizeof(int) * (size_t)ne));
+      CK(cudaMemcpyAsync(x->rs_base.p, ebase.data(), sizeof(int) * ne, cudaMemcpyHostToDevice, s));
+      rsp.nbase = nob;
+      rsp.pert = x->kx_pert.as<int4>();
+      rsp.base_obs = x->rs_base.as<int>();
+      rsp.ray_off = x->kx_rayoff.as<int>();
+      rsp.h_ray_off = eoff_r.data();
+      rsp.h_base_obs = ebase.data();
+      x->resume = &rsp;
+    }
     int rc = run_core(x, b, precision, false);
+    x->resume = nullptr;
     if (rc) return rc;
     // finite differences
     std::vector<long long> kbl(nob + 1, 0), kdst(nob);
@@ -952,6 +1200,7 @@ void jgb_destroy(jgb_ctx* x) {
                     &x->los_sft, &x->los_ends, &x->los_planes, &x->scan_tmp, &x->err_word,
                     &x->tiles_perm, &x->tiles_keys, &x->tiles_keys2, &x->tiles_vals,
                     &x->tiles_off, &x->tiles_len, &x->tiles_data, &x->refl, &x->seg,
+                    &x->rs_start, &x->rs_lists, &x->rs_snap, &x->rs_base,
                     &x->kx_levoff, &x->kx_rayoff, &x->kx_rayobs, &x->kx_src, &x->kx_lev,
                     &x->kx_scal, &x->kx_geo, &x->kx_rad, &x->kx_tau, &x->kx_tp, &x->kx_mask,
                     &x->kx_pert, &x->kx_h, &x->kx_ymap, &x->kx_K, &x->kx_base_rayoff,
@@ -1056,6 +1305,12 @@ int jgb_set_table(jgb_ctx* x, int id, int ig, int np, const double* p, const int
                     eps + (size_t)ip * tt_cap * tu_cap, sizeof(float) * tu_cap,
                     sizeof(float) * w, ntt, cudaMemcpyHostToDevice));
   }
+  return JGB_OK;
+}
+
+int jgb_set_fd_resume(jgb_ctx* x, int mode) {
+  if (!x || mode < 0 || mode > 2) return fail(x, JGB_ERR_ARG, "bad resume setting");
+  x->fd_resume = mode;
   return JGB_OK;
 }
 

@@ -38,6 +38,17 @@ struct DevBuf {
 
 }  // namespace jgb
 
+// A batch of finite-difference perturbations whose path prefixes equal their
+// base's (see fd_core): observations [0, nbase) are the unperturbed bases.
+struct ResumeSpec {
+  int nbase;
+  const int4* pert;      // device, per observation: (array, index, level, step kind); x < 0: none
+  const int* base_obs;   // device, per observation: its base observation
+  const int* ray_off;    // device, ray offsets of the batch
+  const int* h_ray_off;  // host copies
+  const int* h_base_obs;
+};
+
 struct jgb_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -82,6 +93,10 @@ struct jgb_ctx {
   int path_variant = -1;  // mixed path kernel variant chosen by the autotuner
   double los_bound_scale = 1.0;  // factor on the per-ray LOS bound (0: count first)
   int path_split = -1;    // path split over emitters: -1 when latency-bound, 0 never, 1 always
+  int fd_resume = 1;      // resume perturbed paths from their base's state: 0 never,
+                          // 1 when the estimated schedule is shorter, 2 always
+  const ResumeSpec* resume = nullptr;  // set by fd_core for the run_core call it makes
+  jgb::DevBuf rs_start, rs_lists, rs_snap, rs_base;
   int sms = 152;          // multiprocessors of the device
   jgb::DevBuf seg;        // segment emissivities and flags of the split path
   std::vector<float> tune_ms;

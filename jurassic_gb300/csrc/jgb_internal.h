@@ -44,6 +44,17 @@ struct MixedPlan {
   // flag of every (tile point, channel, emitter, lane), else nullptr
   float* seg_eps;
   unsigned char* seg_sat;
+  // tiles [tile0, tile1) of this launch
+  int tile0, tile1;
+  // resumed forward models (finite-difference perturbations): start[r] is
+  // the LOS point ray r starts at (its state read from snap, slot r); ray r
+  // saves the path state for the rays snap_ray[k] before its point
+  // snap_ip[k], k in [snap_off[r], snap_off[r+1]); nullptr: no resume
+  const int* start;
+  const int* snap_off;
+  const int* snap_ip;
+  const int* snap_ray;
+  float* snap;          // [nray][nd][kStateWords * ng + 3]
 };
 int mixed_nfield(const CtlDev& c, unsigned brmask);
 void launch_pack_tiles_n(const CtlDev& c, const TblDev& T, const LosDev& L, const MixedPlan& P,
@@ -53,6 +64,11 @@ int path_mixed_variants();
 // emitter path states, then the combination and radiance per (tile, channel)
 void launch_path_split(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
                        const LosDev& L, const MixedPlan& P, float* refl_scratch, cudaStream_t s);
+// the path of tiles [P.tile0, P.tile1) with resume points and state snapshots
+void launch_path_resume(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
+                        const LosDev& L, const MixedPlan& P, cudaStream_t s);
+// words of one saved path state (per ray and channel)
+int path_state_words(const CtlDev& c);
 void launch_path_mixed(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
                        const LosDev& L, const MixedPlan& P, float* refl_scratch, int variant,
                        cudaStream_t s);

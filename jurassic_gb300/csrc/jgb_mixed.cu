@@ -407,7 +407,10 @@ __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, float 
 // SPLIT: the emitters' segment emissivities come from k_path_gas (P.seg_eps,
 // P.seg_sat) instead of being computed here; everything else is this same
 // code, so both forms give the same results.
-template <int MINB, bool CGA, bool SPLIT = false>
+// RESUME: rays start at P.start[r] from a saved state and save states for
+// other rays (finite-difference perturbations that leave a path prefix
+// unchanged); the arithmetic of every point is the same.
+template <int MINB, bool CGA, bool SPLIT = false, bool RESUME = false>
 __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, ChanDev ch,
                                                           BatchDev b, LosDev L, MixedPlan P,
                                                           float* refl) {
@@ -415,9 +418,9 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int nchb = (c.nd + 3) / 4;
-  const int tile = blockIdx.x / nchb;
+  const int tile = P.tile0 + blockIdx.x / nchb;
   const int id = (blockIdx.x % nchb) * 4 + warp;
-  if (tile >= P.ntile || id >= c.nd) return;
+  if (tile >= P.tile1 || id >= c.nd) return;
   int r = P.perm[tile * 32 + lane];
   if (r >= 0 && b.obs_skip && b.obs_skip[b.ray_obs[r]]) r = -1;  // lane idle, outputs untouched
   const bool skip = r >= 0 && b.skip_masked && b.mask[(long long)id * b.nray + r];
@@ -522,7 +525,32 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
   float rad = 0.f, comp = 0.f, tau = 1.f;
   const bool do_refl = refl != nullptr && r >= 0 && c.sftype >= 2 && sfeps < 1.f && L.sft[r] > 0;
 
-  for (int ip = 0; ip < n; ip++) {
+  // resume: the state words of every emitter and rad, comp, tau
+  const int sw = kStateWords * ng;
+  auto snap_write = [&](int target) {
+    float* q = P.snap + ((long long)target * c.nd + id) * (sw + 3);
+    for (int k = 0; k < sw; k++) q[k] = __uint_as_float(sh_state[k * nth + tid]);
+    q[sw] = rad;
+    q[sw + 1] = comp;
+    q[sw + 2] = tau;
+  };
+  int start = 0, sn = 0, se = 0;
+  if (RESUME && n > 0) {
+    start = P.start[r];
+    if (start > 0) {
+      const float* q = P.snap + ((long long)r * c.nd + id) * (sw + 3);
+      for (int k = 0; k < sw; k++) sh_state[k * nth + tid] = __float_as_uint(q[k]);
+      rad = q[sw];
+      comp = q[sw + 1];
+      tau = q[sw + 2];
+    }
+    sn = P.snap_off[r];
+    se = P.snap_off[r + 1];
+  }
+
+  for (int ip = start; ip < n; ip++) {
+    if (RESUME)
+      for (; sn < se && P.snap_ip[sn] == ip; sn++) snap_write(P.snap_ray[sn]);
     const float* f = base + (long long)ip * F.n * 32;
     const float p = f[F.p * 32], t = f[F.t * 32], ds = f[F.ds * 32];
     float E = 0.f;
@@ -602,6 +630,8 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
       sc[2 * ((long long)ip * c.nd + id) + 1] = eps;
     }
   }
+  if (RESUME)
+    for (; sn < se && P.snap_ip[sn] <= n; sn++) snap_write(P.snap_ray[sn]);
   if (r < 0) return;
 
   const double nud2 = ch.nu[id];
@@ -835,6 +865,28 @@ void launch_path_split(const CtlDev& c, const TblDev& T, const ChanDev& ch, cons
     launch_split<true>(c, T, ch, b, L, P, refl_scratch, smem, s);
   else
     launch_split<false>(c, T, ch, b, L, P, refl_scratch, smem, s);
+}
+
+int path_state_words(const CtlDev& c) { return kStateWords * c.ng + 3; }
+
+void launch_path_resume(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
+                        const LosDev& L, const MixedPlan& P, cudaStream_t s) {
+  const int nchb = (c.nd + 3) / 4;
+  const unsigned nblk = (unsigned)((long long)(P.tile1 - P.tile0) * nchb);
+  if (nblk == 0) return;
+  const size_t smem = sizeof(unsigned) * kStateWords * 128 * (size_t)(c.ng > 0 ? c.ng : 1) +
+                      sizeof(float) * (4 * kChanConsts + kThreadFloats * 128);
+  if (c.formod == 0) {
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(k_path_mixed<8, true, false, true>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_path_mixed<8, true, false, true><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, nullptr);
+  } else {
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(k_path_mixed<8, false, false, true>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_path_mixed<8, false, false, true><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, nullptr);
+  }
 }
 
 void launch_src_to_float(int nd, const double* sr, float* srf, cudaStream_t s) {

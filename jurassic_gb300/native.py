@@ -72,7 +72,8 @@ class Stats(C.Structure):
                 ("pack_ms", C.c_double), ("path_ms", C.c_double), ("d2h_ms", C.c_double),
                 ("total_ms", C.c_double), ("los_points", C.c_longlong),
                 ("path_launches", C.c_int), ("path_variant", C.c_int),
-                ("tune_ms", C.c_float * 8), ("trace_passes", C.c_int)]
+                ("tune_ms", C.c_float * 8), ("trace_passes", C.c_int),
+                ("resume_skip", C.c_double)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
@@ -114,6 +115,7 @@ SIGNATURES = {
     "jgb_set_fov": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp]),
     "jgb_set_los_bound_scale": (C.c_int, [C.c_void_p, C.c_double]),
     "jgb_set_path_split": (C.c_int, [C.c_void_p, C.c_int]),
+    "jgb_set_fd_resume": (C.c_int, [C.c_void_p, C.c_int]),
     "jgb_set_srcfunc": (C.c_int, [C.c_void_p, _dp]),
     "jgb_get_srcfunc": (C.c_int, [C.c_void_p, _dp, _dp]),
     "jgb_formod": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
@@ -230,6 +232,12 @@ class Context:
         """Mixed path loop split over the emitters: -1 for batches too small
         to fill the device (default), 0 never, 1 always."""
         self._check(load().jgb_set_path_split(self.h, int(mode)))
+
+    def set_fd_resume(self, mode: int):
+        """Resume perturbed paths of mixed Jacobians from their base's saved
+        state: 1 when the estimated schedule is shorter (default), 2 always,
+        0 never (the results do not depend on it)."""
+        self._check(load().jgb_set_fd_resume(self.h, int(mode)))
 
     def _check(self, rc):
         if rc != JGB_OK:
