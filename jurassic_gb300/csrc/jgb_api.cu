@@ -501,11 +501,11 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
         return ma != mb ? ma > mb : hc[a] > hc[b2];
       });
       const double t_plain = group_time(ord, 0, nray, false);
-      // measured: resumed chunks win on batches of many waves (2048 nadir
-      // observations x 405 perturbations: +50 %) and lose on the dozens of
-      // requests of a serving step, where the separate base tiles and the
-      // tail of the resumed tiles cost more than the skipped points save
-      if (x->fd_resume == 1 && !(t_res < 0.9 * t_plain && waves >= 32.0)) {
+      // measured: resumed chunks win from about ten waves on (48 serving
+      // requests: -6 %; 2048 nadir observations x 405 perturbations: +55 %
+      // throughput) and lose on a few waves, where the base tiles, which
+      // run first, cost more than the skipped points save
+      if (x->fd_resume == 1 && !(t_res < 0.9 * t_plain && waves >= 8.0)) {
         rs = nullptr;  // run the batch plainly (the base copies are computed too)
         nbase_rays = nray;
         resume_skip = 0.0;
@@ -929,7 +929,7 @@ int fd_core(jgb_ctx* x, const FdLayout& H, const FdInput& in, const std::vector<
         prays += (long long)H.ncnt[o] * (H.ray_off[o + 1] - H.ray_off[o]);
       }
       const double waves = (double)((prays + 31) / 32) * ((c.nd + 3) / 4) / (8.0 * x->sms);
-      res_chunk = waves >= 32.0;
+      res_chunk = waves >= 8.0;
     }
     if (res_chunk)  // unperturbed base copies first
       for (size_t q = i0; q < i1; q++) {

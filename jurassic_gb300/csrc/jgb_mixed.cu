@@ -548,7 +548,15 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
     se = P.snap_off[r + 1];
   }
 
-  for (int ip = start; ip < n; ip++) {
+  // resumed lanes join the warp's walk at their own start point: every
+  // iteration reads one point of the tile for all lanes (coalesced)
+  int ip0 = start;
+  if (RESUME) {
+    const unsigned wmin = __reduce_min_sync(0xffffffffu, n > 0 ? (unsigned)start : 0xffffffffu);
+    ip0 = wmin == 0xffffffffu ? 0 : (int)wmin;
+  }
+  for (int ip = ip0; ip < n; ip++) {
+    if (RESUME && ip < start) continue;
     if (RESUME)
       for (; sn < se && P.snap_ip[sn] == ip; sn++) snap_write(P.snap_ray[sn]);
     const float* f = base + (long long)ip * F.n * 32;
