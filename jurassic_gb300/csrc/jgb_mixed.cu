@@ -305,6 +305,7 @@ __device__ __forceinline__ Bracket pbracket_f(const float* g, int n, float x, in
 }
 
 constexpr int kStateWords = 5;  // t, e, ipr, 2 words of 16-bit corner hints
+constexpr float kTauStop = 1e-12f;  // path transmittance below which the walk stops
 constexpr int kChanConsts = 16;  // constants of a warp's channel
 constexpr int kThreadFloats = 2;  // per-thread values kept in shared memory
 
@@ -557,6 +558,10 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
   }
   for (int ip = ip0; ip < n; ip++) {
     if (RESUME && ip < start) continue;
+    // opaque from here on: the rest of the path adds at most max(src) tau,
+    // below 1e-10 of the radiance (not with surface reflection, whose sum
+    // needs every point)
+    if (tau < kTauStop && !do_refl) break;
     if (RESUME)
       for (; sn < se && P.snap_ip[sn] == ip; sn++) snap_write(P.snap_ray[sn]);
     const float* f = base + (long long)ip * F.n * 32;
@@ -638,8 +643,10 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
       sc[2 * ((long long)ip * c.nd + id) + 1] = eps;
     }
   }
+  // states for resume points beyond the end of this walk (a path that became
+  // opaque earlier hands its final state on, so the resumed rays stop too)
   if (RESUME)
-    for (; sn < se && P.snap_ip[sn] <= n; sn++) snap_write(P.snap_ray[sn]);
+    for (; sn < se; sn++) snap_write(P.snap_ray[sn]);
   if (r < 0) return;
 
   const double nud2 = ch.nu[id];
