@@ -337,6 +337,13 @@ void jgb_dev_free(void *p);
 int jgb_memcpy_h2d(void *dst, const void *src, unsigned long long bytes);
 int jgb_memcpy_d2h(void *dst, const void *src, unsigned long long bytes);
 
+/* Measurement helper (no reference counterpart): L2 read bandwidth of this
+   GPU in GB/s, from passes sweeps over a device buffer of the given size
+   (small enough to stay in L2) in one launch, loads that skip L1, best of
+   5 launches timed with CUDA events.  Roofline denominator for the
+   table-lookup loop, whose probes are served by L1 and L2. */
+int jgb_measure_l2_read(unsigned long long bytes, int passes, double *gbs);
+
 #ifdef __cplusplus
 }
 #endif

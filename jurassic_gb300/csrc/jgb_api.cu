@@ -1087,6 +1087,26 @@ int fd_core(jgb_ctx* x, const FdLayout& H, const FdInput& in, const std::vector<
 // ===========================================================================
 // C ABI
 
+constexpr int kL2ReadThreads = 512;
+
+// passes sweeps over a buffer small enough to stay in L2 (loads that skip
+// L1), one sum per thread written out so that no load is dropped
+__global__ void __launch_bounds__(kL2ReadThreads)
+    k_l2_read(const float4* __restrict__ a, long long n4, int passes, float* __restrict__ out) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  float sx = 0.f, sy = 0.f, sz = 0.f, sw = 0.f;
+  for (int p = 0; p < passes; p++)
+    for (long long i = t; i < n4; i += stride) {
+      const float4 v = __ldcg(a + i);
+      sx += v.x;
+      sy += v.y;
+      sz += v.z;
+      sw += v.w;
+    }
+  out[t] = sx + sy + sz + sw;
+}
+
 extern "C" {
 
 int jgb_create(const jgb_ctl* ctl, int device, jgb_ctx** out) {
@@ -1752,6 +1772,46 @@ int jgb_memcpy_h2d(void* dst, const void* src, unsigned long long bytes) {
 
 int jgb_memcpy_d2h(void* dst, const void* src, unsigned long long bytes) {
   return cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost) == cudaSuccess ? JGB_OK : JGB_ERR_CUDA;
+}
+
+int jgb_measure_l2_read(unsigned long long bytes, int passes, double* gbs) {
+  if (!gbs || bytes < 16 || passes < 1) return JGB_ERR_ARG;
+  *gbs = 0.0;
+  const long long n4 = (long long)(bytes / 16);
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return JGB_ERR_CUDA;
+  const int grid = sms * 4;
+  float4* a = nullptr;
+  float* out = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int st = JGB_ERR_CUDA;
+  if (cudaMalloc(&a, n4 * 16) == cudaSuccess &&
+      cudaMalloc(&out, (size_t)grid * kL2ReadThreads * 4) == cudaSuccess &&
+      cudaMemset(a, 0, n4 * 16) == cudaSuccess && cudaEventCreate(&e0) == cudaSuccess &&
+      cudaEventCreate(&e1) == cudaSuccess) {
+    k_l2_read<<<grid, kL2ReadThreads>>>(a, n4, 1, out);  // brings the buffer into L2
+    float best = 0.f;
+    bool ok = cudaGetLastError() == cudaSuccess;
+    for (int run = 0; ok && run < 5; run++) {
+      cudaEventRecord(e0);
+      k_l2_read<<<grid, kL2ReadThreads>>>(a, n4, passes, out);
+      cudaEventRecord(e1);
+      float ms = 0.f;
+      ok = cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
+      if (ok && (best == 0.f || ms < best)) best = ms;
+    }
+    if (ok && best > 0.f) {
+      *gbs = (double)n4 * 16.0 * passes / (best * 1e-3) / 1e9;
+      st = JGB_OK;
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(a);
+  cudaFree(out);
+  return st;
 }
 
 }  // extern "C"
