@@ -30,14 +30,22 @@ namespace {
 constexpr int kTile = 128;  // output tile (kTile x kTile) per block
 constexpr int kChunk = 16;  // rows of X per shared-memory stage
 constexpr int kPlaneBytes = kTile * kChunk * 4;  // one operand plane of a stage (8 KB)
+constexpr int kBlockFloats = 2 * kTile * kChunk;   // head + residual plane of one (tile, chunk)
 constexpr int kStageBytes = 4 * kPlaneBytes;     // A hi, A lo, B hi, B lo
-constexpr int kTcSmem = 2 * kStageBytes + 64;    // two stages, barriers, TMEM address
-constexpr int kHalf = kTile / 2;                 // epilogue columns per pass
+constexpr int kStages = 4;                       // operand stages in flight
+constexpr int kStageArea = kStages * kStageBytes;             // 128 KB
+constexpr int kStileFloats = kTile * (kTile + 1);             // epilogue staging tile
+constexpr int kBarOff = kStageArea + kStileFloats * 4;        // mbarriers
+constexpr int kNumBars = 2 * kStages + 4;        // full, empty, accumulator full / empty
+constexpr int kTcSmem = kBarOff + kNumBars * 8 + 16;          // + TMEM address
+constexpr int kEpiThreads = 512;                 // sixteen epilogue warps
+constexpr int kNeThreads = 64 + kEpiThreads;     // + copy warp, MMA warp
 
 struct NeDesc {
   int m, n;                 // rows of K, columns of K (state size)
   long long koff, moff, aoff, boff;
-  long long xoff;           // offset of the problem's X planes (m x (n+1))
+  long long xoff;           // offset (floats) of the problem's operand blocks
+  long long tile0;          // index of the problem's first output tile
 };
 
 __device__ __forceinline__ unsigned tf32_of(float x) {
@@ -108,191 +116,294 @@ __device__ __forceinline__ double f2d_bits(float f) {
 }
 
 // X = sqrt(W)[K | dy] of every problem, formed once in FP64 and split into
-// a TF32 high part and a TF32-rounded remainder (row-major m x (n+1) per
-// problem): one block per row, threads over the columns.
-__global__ void k_split_x(const NeDesc* desc, const double* Kall, const double* wall,
-                          const double* dyall, float* xhi, float* xlo) {
+// a TF32 high part and a TF32-rounded remainder, written in the operand
+// layout of the tensor-core product: per (column tile ti, chunk c of kChunk
+// rows) one block of kBlockFloats, the head plane then the residual plane,
+// each 128 columns x kChunk rows in the core-matrix order of tc_off, zero
+// outside m x (n + 1).  Block bi = ti * nch + c of a problem starts at
+// xoff + bi * kBlockFloats (16 KB apart: whole blocks go to shared memory
+// with one bulk copy).  A block is assembled in shared memory and written
+// with 16-byte stores.
+__global__ void __launch_bounds__(128) k_split_x(const NeDesc* desc, const double* Kall,
+                                                 const double* wall, const double* dyall,
+                                                 float* xbuf) {
+  __shared__ __align__(16) float blk[kBlockFloats];
   const NeDesc d = desc[blockIdx.y];
   const int na = d.n + 1;
-  for (int row = blockIdx.x; row < d.m; row += gridDim.x) {
-    const double wr = wall[d.moff + row];
-    const double* Kr = Kall + d.koff + (long long)row * d.n;
-    const long long o = d.xoff + (long long)row * na;
-    for (int col = threadIdx.x; col < na; col += blockDim.x) {
-      const double v = col < d.n ? Kr[col] : dyall[d.moff + row];
-      const float x = (float)(v * wr);
+  const int nt = (na + kTile - 1) / kTile, nch = (d.m + kChunk - 1) / kChunk;
+  const int tid = threadIdx.x;
+  for (int bi = blockIdx.x; bi < nt * nch; bi += gridDim.x) {
+    const int ti = bi / nch, c = bi - ti * nch;
+    const int col = ti * kTile + tid;
+#pragma unroll 4
+    for (int k = 0; k < kChunk; k++) {
+      const int row = c * kChunk + k;
+      float x = 0.f;
+      if (row < d.m && col < na) {
+        const double v = col < d.n ? Kall[d.koff + (long long)row * d.n + col] : dyall[d.moff + row];
+        x = (float)(v * wall[d.moff + row]);
+      }
       const float hi = __uint_as_float(tf32_of(x));
-      xhi[o + col] = hi;
-      xlo[o + col] = __uint_as_float(tf32_of(x - hi));
+      const int o = tc_off(tid, k) >> 2;
+      blk[o] = hi;
+      blk[kTile * kChunk + o] = __uint_as_float(tf32_of(x - hi));
     }
+    __syncthreads();
+    float4* dst = reinterpret_cast<float4*>(xbuf + d.xoff + (long long)bi * kBlockFloats);
+    const float4* src = reinterpret_cast<const float4*>(blk);
+    for (int i = tid; i < kBlockFloats / 4; i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
   }
 }
 
-// One CTA: output tile (ti, tj), ti >= tj, of problem blockIdx.z, C = X^T X
-// over the augmented columns.  Rows of X stream through two shared-memory
-// stages of kChunk rows (A = columns of tile ti, B = columns of tile tj; on
-// a diagonal tile B is A), copied element by element with cp.async straight
-// into the core-matrix layout while the previous stage is multiplied.  One
-// thread issues the 3 x 2 tcgen05.mma of a stage into a 128 x 128 FP32
-// accumulator in tensor memory and commits them to the stage's mbarrier,
-// which the threads wait on before refilling the stage.  The accumulator is
-// read back with tcgen05.ld in two column halves, staged in shared memory,
-// and written as FP64 with coalesced rows (direct and mirrored).  64 KB of
-// shared memory: three CTAs per SM.
-__global__ void __launch_bounds__(128, 3) k_normal_tc(const NeDesc* desc, const float* xhi,
-                                                      const float* xlo, double* Aall,
-                                                      double* ball) {
-  extern __shared__ __align__(1024) unsigned char tc_smem[];
-  const NeDesc d = desc[blockIdx.z];
-  const int na = d.n + 1;  // augmented columns
-  const int nt = (na + kTile - 1) / kTile;
-  // blockIdx.x enumerates lower-triangular tile pairs
-  int t = blockIdx.x, ti = 0;
+// Output tile g of the concatenated lower-triangular tile lists: problem
+// (last with tile0 <= g) and tile pair (ti, tj), ti >= tj.
+__device__ __forceinline__ int tile_of(const NeDesc* desc, int nsel, long long g, int& ti,
+                                       int& tj) {
+  int lo = 0, hi = nsel - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (desc[mid].tile0 <= g) lo = mid; else hi = mid - 1;
+  }
+  int t = (int)(g - desc[lo].tile0);
+  ti = 0;
   while (t > ti) {
     t -= ti + 1;
     ti++;
   }
-  const int tj = t;
-  if (ti >= nt) return;  // the whole CTA, before any barrier or tensor memory
+  tj = t;
+  return lo;
+}
+
+// AND of a flag over the epilogue warps (named barrier 1): all of them take
+// the same branch after it.
+__device__ __forceinline__ bool epi_all(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, 1, %2, p;\n"
+      " selp.u32 %0, 1, 0, q;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v), "n"(kEpiThreads)
+      : "memory");
+  return r != 0;
+}
+
+__device__ __forceinline__ void epi_sync() {
+  asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
+}
+
+// C = X^T X over the augmented columns for every output tile of every
+// problem, as a persistent kernel: one CTA per SM walks tiles blockIdx.x,
+// blockIdx.x + gridDim.x, ... with three roles that meet only at mbarriers.
+//  * copy warp (one lane): per chunk of kChunk rows, bulk copies of the
+//    operand blocks (already in the core-matrix layout; B = A on a diagonal
+//    tile) into one of kStages stages, completing on the stage's "full"
+//    barrier, after the stage's "empty" barrier says its MMAs are done;
+//  * MMA warp (one lane; it also owns the tensor memory): the 3 x 2
+//    tcgen05.mma of each chunk (3xTF32: lo*hi + hi*lo + hi*hi) into one of
+//    two 128 x 128 FP32 accumulators in tensor memory, committed to the
+//    stage's "empty" barrier, and after a tile's last chunk to the
+//    accumulator's "full" barrier;
+//  * sixteen epilogue warps, four per tensor-memory lane quarter (warp w
+//    reads lanes 32 (w % 4) ...), each with 32 of the 128 columns:
+//    tcgen05.ld of the accumulator, mirrored FP64 entries written straight
+//    from registers (lanes along a column of the upper triangle), then the
+//    accumulator is handed back ("empty") and the direct entries are written
+//    through a shared staging tile with lanes along rows.  (Four warps, one
+//    per sub-partition, left the epilogue latency-bound and the MMAs waiting
+//    for the accumulator.)
+// So the copies, the MMAs of one tile and the epilogue of the previous one
+// overlap.  Every wait is bounded; one that gives up flags the error, the
+// epilogue warps leave together (epi_all), the copy lane waits (bounded) for
+// its copies in flight and the MMA lane for its last commit, and the tensor
+// memory is freed.
+__global__ void __launch_bounds__(kNeThreads, 1) k_normal_tc(const NeDesc* desc, int nsel,
+                                                             long long ntiles, const float* xbuf,
+                                                             double* Aall, double* ball) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const bool diag = ti == tj;
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(tc_smem + 2 * kStageBytes);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tc_smem + 2 * kStageBytes + 16);
+  uint64_t* full = reinterpret_cast<uint64_t*>(tc_smem + kBarOff);  // [kStages]
+  uint64_t* empty = full + kStages;                                  // [kStages]
+  uint64_t* acc_full = empty + kStages;                              // [2]
+  uint64_t* acc_empty = acc_full + 2;                                // [2]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tc_smem + kBarOff + kNumBars * 8);
+  float* stile = reinterpret_cast<float*>(tc_smem + kStageArea);     // [kTile][kTile + 1]
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[0])));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[1])));
+    for (int i = 0; i < 2 * kStages + 2; i++)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full[i])));
+    for (int i = 0; i < 2; i++)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&acc_empty[i])),
+                   "r"(kEpiThreads));
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
-  if (warp == 0) {
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
-                 "r"(kTile));
+                 "r"(2 * kTile));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = *tmem_slot;
-  const float* XH = xhi + d.xoff;
-  const float* XL = xlo + d.xoff;
-  const int ci = ti * kTile + tid, cj = tj * kTile + tid;  // this thread's columns
-  const bool iin = ci < na, jin = cj < na;
-  const int nch = (d.m + kChunk - 1) / kChunk;
   const uint32_t sbase = smem_u32(tc_smem);
-  // cp.async of chunk c into stage st (4-byte copies; out-of-range elements
-  // are zero-filled from the problem's first element)
-  auto load = [&](int c, int st) {
-    const uint32_t base = sbase + st * kStageBytes;
-#pragma unroll 4
-    for (int k = 0; k < kChunk; k++) {
-      const int row = c * kChunk + k;
-      const bool rin = row < d.m;
-      const long long o = (long long)row * na;
-      const uint32_t off = (uint32_t)tc_off(tid, k);
-      const uint32_t ni = rin && iin ? 4u : 0u, nj = rin && jin ? 4u : 0u;
-      const float* hi = ni ? XH + o + ci : XH;
-      const float* lo = ni ? XL + o + ci : XL;
-      asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(base + off), "l"(hi), "r"(ni));
-      asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(base + kPlaneBytes + off),
-                   "l"(lo), "r"(ni));
-      if (!diag) {
-        const float* hj = nj ? XH + o + cj : XH;
-        const float* lj = nj ? XL + o + cj : XL;
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(base + 2 * kPlaneBytes + off),
-                     "l"(hj), "r"(nj));
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(base + 3 * kPlaneBytes + off),
-                     "l"(lj), "r"(nj));
-      }
-    }
-  };
   bool ok = true;
-  load(0, 0);
-  asm volatile("cp.async.commit_group;");
-  for (int c = 0; c < nch; c++) {
-    const int st = c & 1;
-    if (c + 1 < nch) {
-      // the other stage's MMAs (chunk c - 1) must be done before refilling it
-      if (c >= 1) ok = mbar_wait(smem_u32(&mbar[st ^ 1]), ((c - 1) >> 1) & 1);
-      ok = __syncthreads_and(ok);
-      if (!ok) break;
-      load(c + 1, st ^ 1);
-    }
-    asm volatile("cp.async.commit_group;");
-    asm volatile("cp.async.wait_group 1;");  // chunk c has landed
-    asm volatile("fence.proxy.async.shared::cta;");  // generic writes -> tensor-core reads
-    __syncthreads();
-    if (tid == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint32_t a0 = sbase + st * kStageBytes;
-      const uint32_t b0 = diag ? a0 : a0 + 2 * kPlaneBytes;
-#pragma unroll
-      for (int s = 0; s < kChunk / 8; s++) {
-        const uint64_t ah = tc_desc(a0 + s * 4096), al = tc_desc(a0 + kPlaneBytes + s * 4096);
-        const uint64_t bh = tc_desc(b0 + s * 4096), bl = tc_desc(b0 + kPlaneBytes + s * 4096);
-        tc_mma(tmem, al, bh, (c | s) != 0);
-        tc_mma(tmem, ah, bl, 1u);
-        tc_mma(tmem, ah, bh, 1u);
+
+  if (warp == 0 && lane == 0) {  // copies
+    long long it = 0;  // chunks issued by this CTA
+    for (long long g = blockIdx.x; g < ntiles && ok; g += gridDim.x) {
+      int ti, tj;
+      const NeDesc d = desc[tile_of(desc, nsel, g, ti, tj)];
+      const int nch = (d.m + kChunk - 1) / kChunk;
+      const bool diag = ti == tj;
+      const float* XA = xbuf + d.xoff + (long long)ti * nch * kBlockFloats;
+      const float* XB = xbuf + d.xoff + (long long)tj * nch * kBlockFloats;
+      const uint32_t bytes = diag ? 2u * kPlaneBytes : 4u * kPlaneBytes;
+      for (int c = 0; c < nch; c++) {
+        const int st = (int)(it % kStages);
+        const uint32_t ph = (uint32_t)((it / kStages) & 1);
+        if (!mbar_wait(smem_u32(&empty[st]), ph ^ 1u)) {  // a fresh stage passes at once
+          ok = false;
+          break;
+        }
+        const uint32_t fb = smem_u32(&full[st]);
+        const uint32_t dst = sbase + st * kStageBytes;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(bytes)
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                dst),
+            "l"(XA + (long long)c * kBlockFloats), "r"(2 * kPlaneBytes), "r"(fb)
+            : "memory");
+        if (!diag)
+          asm volatile(
+              "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                  dst + 2 * kPlaneBytes),
+              "l"(XB + (long long)c * kBlockFloats), "r"(2 * kPlaneBytes), "r"(fb)
+              : "memory");
+        it++;
       }
+    }
+    // the last copy of every stage has landed before the CTA exits
+    for (int st = 0; st < kStages; st++)
+      if (it > st) {
+        const long long last = st + ((it - 1 - st) / kStages) * kStages;
+        mbar_wait(smem_u32(&full[st]), (uint32_t)((last / kStages) & 1));
+      }
+  } else if (warp == 1 && lane == 0) {  // MMAs
+    long long it = 0;
+    int lt = 0;
+    uint32_t last_bar = 0, last_par = 0;  // barrier and phase of the last commit
+    for (long long g = blockIdx.x; g < ntiles && ok; g += gridDim.x, lt++) {
+      int ti, tj;
+      const NeDesc d = desc[tile_of(desc, nsel, g, ti, tj)];
+      const int nch = (d.m + kChunk - 1) / kChunk;
+      const bool diag = ti == tj;
+      const int acc = lt & 1;
+      if (!mbar_wait(smem_u32(&acc_empty[acc]), (uint32_t)((lt >> 1) & 1) ^ 1u)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t dt = tmem + (uint32_t)(acc * kTile);
+      for (int c = 0; c < nch; c++, it++) {
+        const int st = (int)(it % kStages);
+        const uint32_t ph = (uint32_t)((it / kStages) & 1);
+        if (!mbar_wait(smem_u32(&full[st]), ph)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t a0 = sbase + st * kStageBytes;
+        const uint32_t b0 = diag ? a0 : a0 + 2 * kPlaneBytes;
+#pragma unroll
+        for (int s = 0; s < kChunk / 8; s++) {
+          const uint64_t ah = tc_desc(a0 + s * 4096), al = tc_desc(a0 + kPlaneBytes + s * 4096);
+          const uint64_t bh = tc_desc(b0 + s * 4096), bl = tc_desc(b0 + kPlaneBytes + s * 4096);
+          tc_mma(dt, al, bh, (c | s) != 0);
+          tc_mma(dt, ah, bl, 1u);
+          tc_mma(dt, ah, bh, 1u);
+        }
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                smem_u32(&empty[st])));
+        last_bar = smem_u32(&empty[st]);
+        last_par = ph;
+      }
+      if (!ok) break;
       asm volatile(
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-              smem_u32(&mbar[st])));
+              smem_u32(&acc_full[acc])));
+      last_bar = smem_u32(&acc_full[acc]);
+      last_par = (uint32_t)((lt >> 1) & 1);
     }
-  }
-  asm volatile("cp.async.wait_all;");
-  // the last commit tracks every MMA of the tile
-  if (ok && nch > 0) ok = mbar_wait(smem_u32(&mbar[(nch - 1) & 1]), ((nch - 1) >> 1) & 1);
-  ok = __syncthreads_and(ok);
-  asm volatile("tcgen05.fence::after_thread_sync;");
-  if (ok) {
-    double* A = Aall + d.aoff;
-    double* bv = ball + d.boff;
-    float* tile = reinterpret_cast<float*>(tc_smem);  // [128][kHalf + 1]
-    for (int h = 0; h < 2; h++) {
-      // accumulator rows 32 warp + lane, columns h kHalf ... -> shared tile
-      for (int c0 = 0; c0 < kHalf; c0 += 8) {
-        uint32_t r[8];
+    // every MMA issued is complete before the tensor memory can be freed
+    if (last_bar && !mbar_wait(last_bar, last_par)) ok = false;
+  } else if (warp >= 2) {  // epilogue
+    const int q = warp & 3;          // tensor-memory lane quarter of this warp
+    const int r = q * 32 + lane;     // accumulator row (tile-local column ti of X)
+    const int ew = warp - 2;         // 0 .. 15
+    const int cb = (ew >> 2) * 32;   // this warp's accumulator columns cb ... cb + 31
+    int lt = 0;
+    for (long long g = blockIdx.x; g < ntiles; g += gridDim.x, lt++) {
+      int ti, tj;
+      const NeDesc d = desc[tile_of(desc, nsel, g, ti, tj)];
+      const int acc = lt & 1;
+      const bool w = mbar_wait(smem_u32(&acc_full[acc]), (uint32_t)((lt >> 1) & 1));
+      if (!epi_all(w)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      double* A = Aall + d.aoff;
+      double* bv = ball + d.boff;
+      const int row = ti * kTile + r;
+      const bool mrow = row < d.n;
+      for (int c0 = cb; c0 < cb + 32; c0 += 16) {
+        uint32_t v[16];
         asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-              "=r"(r[7])
-            : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(h * kHalf + c0)));
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+              "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+              "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+            : "r"(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * kTile + c0)));
         asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-        for (int j = 0; j < 8; j++)
-          tile[(warp * 32 + lane) * (kHalf + 1) + c0 + j] = __uint_as_float(r[j]);
-      }
-      __syncthreads();
-      // rows >= columns (and b, the augmented row n), threads along a row
-      for (int r = warp; r < kTile; r += 4) {
-        const int row = ti * kTile + r;
-        for (int cc = lane; cc < kHalf; cc += 32) {
-          const int col = tj * kTile + h * kHalf + cc;
-          if (col >= d.n || row > d.n) continue;
-          const double v = f2d_bits(tile[r * (kHalf + 1) + cc]);
-          if (row == d.n)
-            bv[col] = v;
-          else if (row >= col)
-            A[(long long)row * d.n + col] = v;
+        for (int j = 0; j < 16; j++) {
+          const float f = __uint_as_float(v[j]);
+          stile[r * (kTile + 1) + c0 + j] = f;
+          const int col = tj * kTile + c0 + j;
+          // mirrored entry (col, row) of the upper triangle: lanes along rows
+          if (mrow && col < row && col < d.n) A[(long long)col * d.n + row] = f2d_bits(f);
         }
       }
-      // mirrored entries, threads along a row of the upper triangle
-      for (int cc = warp; cc < kHalf; cc += 4) {
-        const int col = tj * kTile + h * kHalf + cc;
-        for (int r = lane; r < kTile; r += 32) {
-          const int row = ti * kTile + r;
-          if (row < d.n && col < d.n && row > col)
-            A[(long long)col * d.n + row] = f2d_bits(tile[r * (kHalf + 1) + cc]);
+      // accumulator read: hand it back to the MMA warp
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[acc]))
+                   : "memory");
+      epi_sync();
+      // direct entries, rows >= columns (and b, the augmented row n)
+      for (int rr = ew; rr < kTile; rr += kEpiThreads / 32) {
+        const int row2 = ti * kTile + rr;
+        if (row2 > d.n) break;
+        for (int cc = lane; cc < kTile; cc += 32) {
+          const int col = tj * kTile + cc;
+          if (col >= d.n) break;
+          const double x = f2d_bits(stile[rr * (kTile + 1) + cc]);
+          if (row2 == d.n)
+            bv[col] = x;
+          else if (row2 >= col)
+            A[(long long)row2 * d.n + col] = x;
         }
       }
-      __syncthreads();
+      epi_sync();  // the staging tile is free for the next tile
     }
-  } else if (tid == 0) {
-    atomicOr(&g_tc_err, 1u);
   }
+  if (!ok) atomicOr(&g_tc_err, 1u);
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
-  if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTile));
+  if (warp == 1)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kTile));
 }
 
 // FP64 reference products: one thread per lower-triangle element (+ b).
@@ -356,15 +467,16 @@ int normal_equations_dev(int nret, const int* m, const int* n, const double* K, 
   // descriptors of the selected problems (host -> device scratch provided by
   // the caller); offsets follow the concatenation of all nret problems
   NeDesc* hd = new NeDesc[nret];
-  long long ko = 0, mo = 0, ao = 0, bo = 0, xo = 0;
-  int maxtiles = 0, maxn = 0, maxm = 0, nsel = 0;
+  long long ko = 0, mo = 0, ao = 0, bo = 0, xo = 0, ntiles = 0;
+  int maxn = 0, maxblk = 0, nsel = 0;
   for (int i = 0; i < nret; i++) {
     if (!sel || sel[i]) {
-      hd[nsel++] = NeDesc{m[i], n[i], ko, mo, ao, bo, xo};
-      xo += (long long)m[i] * (n[i] + 1);
-      maxm = m[i] > maxm ? m[i] : maxm;
+      hd[nsel++] = NeDesc{m[i], n[i], ko, mo, ao, bo, xo, ntiles};
       const int nt = (n[i] + 1 + kTile - 1) / kTile;
-      maxtiles = nt * (nt + 1) / 2 > maxtiles ? nt * (nt + 1) / 2 : maxtiles;
+      const int nblk = nt * ((m[i] + kChunk - 1) / kChunk);
+      xo += (long long)nblk * kBlockFloats;
+      ntiles += (long long)nt * (nt + 1) / 2;
+      maxblk = nblk > maxblk ? nblk : maxblk;
       maxn = n[i] > maxn ? n[i] : maxn;
     }
     ko += (long long)m[i] * n[i];
@@ -385,17 +497,22 @@ int normal_equations_dev(int nret, const int* m, const int* n, const double* K, 
   delete[] hd;
   if (e != cudaSuccess) return JGB_ERR_CUDA;
   if (precision == JGB_MIXED) {
-    // X planes in a grow-only buffer of the current device (held to exit)
-    float* xbuf = split_buffer(sizeof(float) * 2 * (size_t)xo, s);
+    // operand blocks in a grow-only buffer of the current device (held to exit)
+    float* xbuf = split_buffer(sizeof(float) * (size_t)xo, s);
     if (!xbuf) return JGB_ERR_CUDA;
     const NeDesc* dd = static_cast<const NeDesc*>(desc_dev);
-    k_split_x<<<dim3((unsigned)(maxm < 1024 ? maxm : 1024), nsel), 128, 0, s>>>(dd, K, w, dy, xbuf,
-                                                                                  xbuf + xo);
+    k_split_x<<<dim3((unsigned)(maxblk < 4096 ? maxblk : 4096), nsel), 128, 0, s>>>(dd, K, w, dy,
+                                                                                      xbuf);
     cudaFuncSetAttribute(k_normal_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
     const unsigned zero = 0;
     cudaMemcpyToSymbolAsync(g_tc_err, &zero, sizeof(zero), 0, cudaMemcpyHostToDevice, s);
-    dim3 grid(maxtiles, 1, nsel);
-    k_normal_tc<<<grid, 128, kTcSmem, s>>>(dd, xbuf, xbuf + xo, A, b);
+    // persistent: one CTA per SM (or per tile when there are fewer)
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return JGB_ERR_CUDA;
+    const unsigned grid = (unsigned)(ntiles < sms ? ntiles : sms);
+    k_normal_tc<<<grid, kNeThreads, kTcSmem, s>>>(dd, nsel, ntiles, xbuf, A, b);
     unsigned herr = 0;
     cudaMemcpyFromSymbolAsync(&herr, g_tc_err, sizeof(herr), 0, cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess || herr) return JGB_ERR_CUDA;
