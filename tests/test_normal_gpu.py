@@ -43,3 +43,31 @@ def test_normal_equations_uneven_batch(built_lib, prec):
             assert np.max(np.abs(A - Ar) / np.outer(d, d)) <= 1e-12
             assert np.allclose(b, br, rtol=1e-10, atol=1e-12 * np.max(np.abs(br)))
         assert np.array_equal(A, A.T)
+
+
+def test_normal_equations_many_tiles_per_sm(built_lib):
+    """More output tiles than SMs: the persistent product kernel walks several
+    tiles per CTA, so both tensor-memory accumulators are reused and the
+    operand stages cycle across tiles of different chunk counts (m not a
+    multiple of 16, n + 1 on and around multiples of 128).  Every problem
+    meets the 3xTF32 bound, and a second call gives the same bits."""
+    rng = np.random.default_rng(11)
+    sizes = [(int(rng.integers(1, 121)), int(rng.choice([1, 127, 128, 255, 256])
+                                            if i % 7 == 0 else rng.integers(1, 300)))
+             for i in range(400)]
+    Ks = [rng.standard_normal((m, n)) * np.exp(rng.uniform(-2, 2, n))[None, :] for m, n in sizes]
+    ws = [np.exp(rng.uniform(-1, 1, m)) for m, _ in sizes]
+    dys = [rng.standard_normal(m) for m, _ in sizes]
+    tiles = sum(((n + 128) // 128) * ((n + 128) // 128 + 1) // 2 for _, n in sizes)
+    assert tiles > 3 * 152
+    ctx = _ctx()
+    As, bs = ctx.normal_equations(Ks, ws, dys, native.MIXED)
+    As2, bs2 = ctx.normal_equations(Ks, ws, dys, native.MIXED)
+    for K, w, dy, A, b, A2, b2 in zip(Ks, ws, dys, As, bs, As2, bs2):
+        Ar, br = _ref(K, w, dy)
+        d = np.sqrt(np.diag(Ar))
+        assert np.max(np.abs(A - Ar) / np.outer(d, d)) <= 1e-5
+        sdy = np.sqrt(np.sum((dy * w) ** 2))
+        assert np.max(np.abs(b - br) / (d * sdy)) <= 1e-5
+        assert np.array_equal(A, A.T)
+        assert np.array_equal(A, A2) and np.array_equal(b, b2)
