@@ -32,9 +32,11 @@ constexpr int kChunk = 16;  // rows of X per shared-memory stage
 constexpr int kPlaneBytes = kTile * kChunk * 4;  // one operand plane of a stage (8 KB)
 constexpr int kBlockFloats = 2 * kTile * kChunk;   // head + residual plane of one (tile, chunk)
 constexpr int kStageBytes = 4 * kPlaneBytes;     // A hi, A lo, B hi, B lo
-constexpr int kStages = 4;                       // operand stages in flight
-constexpr int kStageArea = kStages * kStageBytes;             // 128 KB
-constexpr int kStileFloats = kTile * (kTile + 1);             // epilogue staging tile
+constexpr int kStages = 2;                       // operand stages in flight
+constexpr int kStageArea = kStages * kStageBytes;             // 64 KB
+constexpr int kEpiCols = kTile / 2;                           // columns per epilogue pass
+constexpr int kEpiPad = kEpiCols + 4;  // staging row stride: 16-byte rows, no bank conflicts
+constexpr int kStileFloats = kTile * kEpiPad;                 // epilogue staging tile
 constexpr int kBarOff = kStageArea + kStileFloats * 4;        // mbarriers
 constexpr int kNumBars = 2 * kStages + 4;        // full, empty, accumulator full / empty
 constexpr int kTcSmem = kBarOff + kNumBars * 8 + 16;          // + TMEM address
@@ -102,17 +104,17 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
   return false;
 }
 
-// Exact float -> double widening with integer operations (the FP64 pipe of
-// GB300 is narrow); zero, subnormal, infinite and NaN inputs take the
-// conversion instruction.
+// Exact float -> double widening with integer operations on the two 32-bit
+// words (the FP64 pipe of GB300 is narrow): for a normal float the high word
+// is the sign, the exponent rebiased by 1023 - 127 and the top 20 mantissa
+// bits, the low word the last 3 mantissa bits; zero, subnormal, infinite
+// and NaN inputs take the conversion instruction.
 __device__ __forceinline__ double f2d_bits(float f) {
   const unsigned u = __float_as_uint(f);
-  const unsigned e = (u >> 23) & 0xffu;
-  if (e == 0u || e == 0xffu) return (double)f;
-  const unsigned long long s = (unsigned long long)(u >> 31) << 63;
-  const unsigned long long ex = (unsigned long long)(e + 896u) << 52;   // rebias 127 -> 1023
-  const unsigned long long mt = (unsigned long long)(u & 0x7fffffu) << 29;
-  return __longlong_as_double((long long)(s | ex | mt));
+  const unsigned e = u & 0x7f800000u;
+  if (e == 0u || e == 0x7f800000u) return (double)f;
+  const unsigned hi = (u & 0x80000000u) | (((u & 0x7fffffffu) >> 3) + (896u << 20));
+  return __hiloint2double((int)hi, (int)(u << 29));
 }
 
 // X = sqrt(W)[K | dy] of every problem, formed once in FP64 and split into
@@ -205,19 +207,22 @@ __device__ __forceinline__ void epi_sync() {
 //    stage's "empty" barrier, and after a tile's last chunk to the
 //    accumulator's "full" barrier;
 //  * sixteen epilogue warps, four per tensor-memory lane quarter (warp w
-//    reads lanes 32 (w % 4) ...), each with 32 of the 128 columns:
-//    tcgen05.ld of the accumulator, mirrored FP64 entries written straight
-//    from registers (lanes along a column of the upper triangle), then the
-//    accumulator is handed back ("empty") and the direct entries are written
-//    through a shared staging tile with lanes along rows.  (Four warps, one
-//    per sub-partition, left the epilogue latency-bound and the MMAs waiting
-//    for the accumulator.)
+//    reads lanes 32 (w % 4) ...), in two passes of 64 columns, 16 columns
+//    per warp and pass: tcgen05.ld of the accumulator, mirrored FP64 entries
+//    written straight from registers (lanes along a column of the upper
+//    triangle), the direct entries through a shared staging tile with lanes
+//    along rows; after the second pass's loads the accumulator is handed
+//    back ("empty").
 // So the copies, the MMAs of one tile and the epilogue of the previous one
-// overlap.  Every wait is bounded; one that gives up flags the error, the
+// overlap.  The epilogue sets the pace (without its stores the kernel runs
+// in about half the time, and four stages instead of two change nothing), so
+// the CTA keeps two stages and a 64-column staging tile, 97 KB of shared
+// memory, and two CTAs share an SM (32 epilogue warps, all 512 columns of
+// tensor memory).  Every wait is bounded; one that gives up flags the error, the
 // epilogue warps leave together (epi_all), the copy lane waits (bounded) for
 // its copies in flight and the MMA lane for its last commit, and the tensor
 // memory is freed.
-__global__ void __launch_bounds__(kNeThreads, 1) k_normal_tc(const NeDesc* desc, int nsel,
+__global__ void __launch_bounds__(kNeThreads, 2) k_normal_tc(const NeDesc* desc, int nsel,
                                                              long long ntiles, const float* xbuf,
                                                              double* Aall, double* ball) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];
@@ -227,7 +232,7 @@ __global__ void __launch_bounds__(kNeThreads, 1) k_normal_tc(const NeDesc* desc,
   uint64_t* acc_full = empty + kStages;                              // [2]
   uint64_t* acc_empty = acc_full + 2;                                // [2]
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tc_smem + kBarOff + kNumBars * 8);
-  float* stile = reinterpret_cast<float*>(tc_smem + kStageArea);     // [kTile][kTile + 1]
+  float* stile = reinterpret_cast<float*>(tc_smem + kStageArea);     // [kTile][kEpiPad]
   if (tid == 0) {
     for (int i = 0; i < 2 * kStages + 2; i++)
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full[i])));
@@ -343,7 +348,7 @@ __global__ void __launch_bounds__(kNeThreads, 1) k_normal_tc(const NeDesc* desc,
     const int q = warp & 3;          // tensor-memory lane quarter of this warp
     const int r = q * 32 + lane;     // accumulator row (tile-local column ti of X)
     const int ew = warp - 2;         // 0 .. 15
-    const int cb = (ew >> 2) * 32;   // this warp's accumulator columns cb ... cb + 31
+    const int cq = (ew >> 2) * 16;   // this warp's 16 columns within a pass
     int lt = 0;
     for (long long g = blockIdx.x; g < ntiles; g += gridDim.x, lt++) {
       int ti, tj;
@@ -359,7 +364,8 @@ __global__ void __launch_bounds__(kNeThreads, 1) k_normal_tc(const NeDesc* desc,
       double* bv = ball + d.boff;
       const int row = ti * kTile + r;
       const bool mrow = row < d.n;
-      for (int c0 = cb; c0 < cb + 32; c0 += 16) {
+      for (int h = 0; h < 2; h++) {
+        const int c0 = h * kEpiCols + cq;  // accumulator columns c0 ... c0 + 15
         uint32_t v[16];
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
@@ -368,35 +374,44 @@ __global__ void __launch_bounds__(kNeThreads, 1) k_normal_tc(const NeDesc* desc,
               "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
             : "r"(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * kTile + c0)));
         asm volatile("tcgen05.wait::ld.sync.aligned;");
+        if (h == 1) {  // accumulator read: hand it back to the MMA warp
+          asm volatile("tcgen05.fence::before_thread_sync;");
+          asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[acc]))
+                       : "memory");
+        }
+        float4* srow = reinterpret_cast<float4*>(stile + r * kEpiPad + cq);
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+          srow[k] = make_float4(__uint_as_float(v[4 * k]), __uint_as_float(v[4 * k + 1]),
+                                __uint_as_float(v[4 * k + 2]), __uint_as_float(v[4 * k + 3]));
 #pragma unroll
         for (int j = 0; j < 16; j++) {
-          const float f = __uint_as_float(v[j]);
-          stile[r * (kTile + 1) + c0 + j] = f;
           const int col = tj * kTile + c0 + j;
           // mirrored entry (col, row) of the upper triangle: lanes along rows
-          if (mrow && col < row && col < d.n) A[(long long)col * d.n + row] = f2d_bits(f);
+          if (mrow && col < row && col < d.n)
+            A[(long long)col * d.n + row] = f2d_bits(__uint_as_float(v[j]));
         }
-      }
-      // accumulator read: hand it back to the MMA warp
-      asm volatile("tcgen05.fence::before_thread_sync;");
-      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[acc]))
-                   : "memory");
-      epi_sync();
-      // direct entries, rows >= columns (and b, the augmented row n)
-      for (int rr = ew; rr < kTile; rr += kEpiThreads / 32) {
-        const int row2 = ti * kTile + rr;
-        if (row2 > d.n) break;
-        for (int cc = lane; cc < kTile; cc += 32) {
-          const int col = tj * kTile + cc;
-          if (col >= d.n) break;
-          const double x = f2d_bits(stile[rr * (kTile + 1) + cc]);
-          if (row2 == d.n)
-            bv[col] = x;
-          else if (row2 >= col)
-            A[(long long)row2 * d.n + col] = x;
+        epi_sync();
+        // direct entries, rows >= columns (and b, the augmented row n): two
+        // columns per lane, lanes along the row
+        const int colp = tj * kTile + h * kEpiCols + 2 * lane;
+        for (int rr = ew; rr < kTile; rr += kEpiThreads / 32) {
+          const int row2 = ti * kTile + rr;
+          if (row2 > d.n || colp >= d.n) break;
+          const float2 x2 = *reinterpret_cast<const float2*>(stile + rr * kEpiPad + 2 * lane);
+#pragma unroll
+          for (int k = 0; k < 2; k++) {
+            const int col = colp + k;
+            if (col >= d.n) break;
+            const double x = f2d_bits(k ? x2.y : x2.x);
+            if (row2 == d.n)
+              bv[col] = x;
+            else if (row2 >= col)
+              A[(long long)row2 * d.n + col] = x;
+          }
         }
+        epi_sync();  // the staging tile is free for the next pass
       }
-      epi_sync();  // the staging tile is free for the next tile
     }
   }
   if (!ok) atomicOr(&g_tc_err, 1u);
@@ -506,12 +521,12 @@ int normal_equations_dev(int nret, const int* m, const int* n, const double* K, 
     cudaFuncSetAttribute(k_normal_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
     const unsigned zero = 0;
     cudaMemcpyToSymbolAsync(g_tc_err, &zero, sizeof(zero), 0, cudaMemcpyHostToDevice, s);
-    // persistent: one CTA per SM (or per tile when there are fewer)
+    // persistent: two CTAs per SM (or one per tile when there are fewer)
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
       return JGB_ERR_CUDA;
-    const unsigned grid = (unsigned)(ntiles < sms ? ntiles : sms);
+    const unsigned grid = (unsigned)(ntiles < 2LL * sms ? ntiles : 2LL * sms);
     k_normal_tc<<<grid, kNeThreads, kTcSmem, s>>>(dd, nsel, ntiles, xbuf, A, b);
     unsigned herr = 0;
     cudaMemcpyFromSymbolAsync(&herr, g_tc_err, sizeof(herr), 0, cudaMemcpyDeviceToHost, s);
