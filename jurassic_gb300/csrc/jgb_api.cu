@@ -364,9 +364,29 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
     L.cgp = L.kw + (long long)c.nw * cap;
     L.cgt = L.cgp + (long long)c.ng * cap;
     L.cgu = L.cgt + (long long)c.ng * cap;
-    if (precision == JGB_MIXED)
-      launch_trace_fill_mixed(c, b, L, d_err, s);
-    else
+    if (precision == JGB_MIXED) {
+      // rays ordered by capacity (longest first) when the capacities are
+      // bounds of the real lengths: a warp's rays then walk similar lengths
+      const int* order = nullptr;
+      if (mode == kBound && nray > 32) {
+        CK(x->tiles_keys2.reserve(sizeof(int) * (size_t)nray));
+        CK(x->tiles_vals.reserve(sizeof(int) * 2 * (size_t)nray));
+        int* vin = x->tiles_vals.as<int>();
+        int* vout = vin + nray;
+        k_iota<<<(nray + 255) / 256, 256, 0, s>>>(nray, vin);
+        int bits = 1;
+        while (bits < 31 && (1LL << bits) <= (long long)c.nlos_max) bits++;
+        size_t sb = 0;
+        cub::DeviceRadixSort::SortPairsDescending(nullptr, sb, L.count, x->tiles_keys2.as<int>(),
+                                                  vin, vout, nray, 0, bits, s);
+        CK(x->scan_tmp.reserve(sb + 16));
+        cub::DeviceRadixSort::SortPairsDescending(x->scan_tmp.p, sb, L.count,
+                                                  x->tiles_keys2.as<int>(), vin, vout, nray, 0,
+                                                  bits, s);
+        order = vout;
+      }
+      launch_trace_fill_mixed(c, b, L, order, d_err, s);
+    } else
       launch_trace_fill(c, ch, b, L, d_err, s);
     CK(cudaGetLastError());
     passes++;

@@ -19,8 +19,8 @@ void launch_fov(const CtlDev& c, const BatchDev& b, const double* prad, const do
 // jgb_trace_mixed.cu: ray tracing of the mixed-precision forward model
 void launch_trace_count_mixed(const CtlDev& c, const BatchDev& b, const LosDev& L, unsigned* err,
                               cudaStream_t s);
-void launch_trace_fill_mixed(const CtlDev& c, const BatchDev& b, const LosDev& L, unsigned* err,
-                             cudaStream_t s);
+void launch_trace_fill_mixed(const CtlDev& c, const BatchDev& b, const LosDev& L, const int* order,
+                             unsigned* err, cudaStream_t s);
 void launch_los_bound_mixed(const CtlDev& c, const BatchDev& b, double scale, int* cap,
                             cudaStream_t s);
 void launch_trace_fill(const CtlDev& c, const ChanDev& ch, const BatchDev& b, const LosDev& L,

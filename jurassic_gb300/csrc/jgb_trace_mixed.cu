@@ -443,9 +443,13 @@ __global__ void k_los_bound_m(CtlDev c, BatchDev b, double scale, int* cap) {
   cap[r] = bound >= (double)c.nlos_max ? c.nlos_max : (int)bound;
 }
 
-__global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, unsigned* err) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= b.nray) return;
+// order (optional): thread t traces ray order[t], so that a warp's rays have
+// similar LOS capacities and finish together; each ray's outputs go to its
+// own slots, so the order does not change any result.
+__global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, const int* order, unsigned* err) {
+  const int th = blockIdx.x * blockDim.x + threadIdx.x;
+  if (th >= b.nray) return;
+  const int r = order ? order[th] : th;
   if (b.obs_skip && b.obs_skip[b.ray_obs[r]]) {
     L.count[r] = 0;
     return;
@@ -564,10 +568,10 @@ void launch_los_bound_mixed(const CtlDev& c, const BatchDev& b, double scale, in
   k_los_bound_m<<<(b.nray + bs - 1) / bs, bs, 0, s>>>(c, b, scale, cap);
 }
 
-void launch_trace_fill_mixed(const CtlDev& c, const BatchDev& b, const LosDev& L, unsigned* err,
-                             cudaStream_t s) {
+void launch_trace_fill_mixed(const CtlDev& c, const BatchDev& b, const LosDev& L, const int* order,
+                             unsigned* err, cudaStream_t s) {
   const int bs = kTraceThreads;
-  k_trace_fill_m<<<(b.nray + bs - 1) / bs, bs, 0, s>>>(c, b, L, err);
+  k_trace_fill_m<<<(b.nray + bs - 1) / bs, bs, 0, s>>>(c, b, L, order, err);
 }
 
 }  // namespace jgb
