@@ -184,12 +184,11 @@ def time_cpu(w, ora, target_s, threads):
 def run_reference(args, rank):
     if rank != 0:
         return
-    from oracle import oracle, refimpl
+    from oracle import oracle
     w = build_workload(args)
     threads = os.cpu_count() or 1
     kind = "port"
     ora = oracle.Oracle(w.ctl, w.tables, w.filters)
-    use_ref = refimpl.available("big") and os.path.isdir("/root/reference")
     per_step = []
     sample_n = None
     for step in range(args.warmup + args.steps):
