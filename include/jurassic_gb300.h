@@ -116,6 +116,25 @@ int jgb_set_table(jgb_ctx *ctx, int id, int ig, int np, const double *p, const i
                   const double *t, const int *nu, const float *u, const float *eps,
                   int tt_cap, int tu_cap);
 
+/* Table files of the reference (read_tbl, jurassic.c:4949-5110; write_tbl,
+   jurassic.c:5810-5892): tblfmt 1 = ASCII lines "p T u eps", 2 = binary.
+   jgb_read_tables reads, for every channel id and emitter ig of the context,
+   the file "<tblbase>_<nu[id] as %.4f>_<emitter[ig]>.tab" (.bin for tblfmt
+   2) on the host and uploads it with jgb_set_table; jgb_tables_init must
+   have set capacities that hold the tables (JGB_ERR_ARG otherwise).  A
+   missing file leaves that table empty, as the reference does (it warns);
+   an unreadable or truncated one returns JGB_ERR_IO.
+   jgb_read_table_file / jgb_write_table_file read or write one file into or
+   from caller arrays with the row layout of jgb_set_table (capacities tp or
+   np, tt, tu); no device work.  Reading one format and writing the other
+   converts a table (the reference's tblfmt tool). */
+int jgb_read_tables(jgb_ctx *ctx, const char *tblbase, int tblfmt);
+int jgb_read_table_file(const char *path, int tblfmt, int tp, int tt, int tu, int *np_out,
+                        double *p, int *nt, double *t, int *nu, float *u, float *eps);
+int jgb_write_table_file(const char *path, int tblfmt, int np, const double *p, const int *nt,
+                         const double *t, const int *nu, const float *u, const float *eps,
+                         int tt_cap, int tu_cap);
+
 /* Field of view (formod_fov, jurassic.c:3121-3192; FOV control parameter,
    read_shape of the FOV file): n samples of altitude offset dz [km] and
    weight w.  Every forward model of the context then convolves the pencil

@@ -30,6 +30,7 @@ UNITS = {
     "jgb_noalloc.cu": [],
     "jgb_normal.cu": ["-fmad=false"],
     "jgb_retrieval.cu": ["-fmad=false"],
+    "jgb_tblio.cu": [],
     # FP32 increments around an FP64 position and direction: approximate
     # FP32 division and square root (~2 ulp) cut the latency of a step
     "jgb_trace_mixed.cu": ["-fmad=false", "-prec-div=false", "-prec-sqrt=false"],

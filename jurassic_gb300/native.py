@@ -26,6 +26,8 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libjurassic_gb300.so")
 
 JGB_OK = 0
+# status codes of the C ABI (jurassic_gb300.h)
+ERR_ARG, ERR_CUDA, ERR_STATE, ERR_LOS, ERR_SURFACE, ERR_UNSUPPORTED, ERR_IO, ERR_NUMERIC = range(1, 9)
 FP64 = 0
 MIXED = 1
 
@@ -112,6 +114,11 @@ SIGNATURES = {
     "jgb_set_table": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _ip, _dp, _ip, _fp,
                                 _fp, C.c_int, C.c_int]),
     "jgb_set_filter": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp]),
+    "jgb_read_tables": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int]),
+    "jgb_read_table_file": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, _ip, _dp, _ip,
+                                      _dp, _ip, _fp, _fp]),
+    "jgb_write_table_file": (C.c_int, [C.c_char_p, C.c_int, C.c_int, _dp, _ip, _dp, _ip, _fp, _fp,
+                                       C.c_int, C.c_int]),
     "jgb_set_fov": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp]),
     "jgb_set_los_bound_scale": (C.c_int, [C.c_void_p, C.c_double]),
     "jgb_set_path_split": (C.c_int, [C.c_void_p, C.c_int]),
@@ -271,6 +278,14 @@ class Context:
                 e = np.ascontiguousarray(tbl.eps[id, ig], np.float32)
                 self._check(L.jgb_set_table(self.h, id, ig, n, _p(p), _p(nt, _ip), _p(t),
                                             _p(nu, _ip), _p(u, _fp), _p(e, _fp), tt, tu))
+
+    def read_tables(self, tblbase: str, tblfmt: int, tp=41, tt=30, tu=320):
+        """Emissivity tables from the reference's files (read_tbl,
+        jurassic.c:4949-5110), read by the library and uploaded; tp, tt, tu
+        are the capacities (TBLNP, TBLNT, TBLNU)."""
+        L = load()
+        self._check(L.jgb_tables_init(self.h, tp, tt, tu))
+        self._check(L.jgb_read_tables(self.h, tblbase.encode(), int(tblfmt)))
 
     def set_filters(self, filters):
         for id, (fnu, f) in enumerate(filters):

@@ -121,7 +121,7 @@ def _read_ascii_table(fn, tp, tt, tu):
                 if ip >= tp:
                     raise JurassicError("Too many pressure levels!")
                 it = -1
-            if temp != t_old:
+            if temp != t_old or it < 0:   # a level opens a row even at the last row's T
                 t_old = temp
                 it += 1
                 if it >= tt:

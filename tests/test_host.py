@@ -162,3 +162,120 @@ def test_ascii_tables_read_like_the_reference(tmp_path, built_oracle):
     # the folded lines changed the tables: they differ from the unmangled set
     orig = G.tables_from(f)
     assert not np.array_equal(tbl.u, orig.u)
+
+
+# ---------------------------------------------------------------------------
+# the library's own table-file reader and writer (jgb_read_table_file,
+# jgb_write_table_file): host functions, no device work
+
+def _c_read(L, path, fmt, tp, tt, tu):
+    import ctypes as C
+    p = np.zeros(tp)
+    nt = np.zeros(tp, np.int32)
+    t = np.zeros((tp, tt))
+    nu = np.zeros((tp, tt), np.int32)
+    u = np.zeros((tp, tt, tu), np.float32)
+    e = np.zeros((tp, tt, tu), np.float32)
+    n = C.c_int(-7)
+    ptr = lambda a, ty: a.ctypes.data_as(C.POINTER(ty))
+    rc = L.jgb_read_table_file(str(path).encode(), fmt, tp, tt, tu, C.byref(n),
+                               ptr(p, C.c_double), ptr(nt, C.c_int), ptr(t, C.c_double),
+                               ptr(nu, C.c_int), ptr(u, C.c_float), ptr(e, C.c_float))
+    return rc, n.value, p, nt, t, nu, u, e
+
+
+def _c_write(L, path, fmt, tbl, id, ig):
+    import ctypes as C
+    tp, tt, tu = tbl.u.shape[2:]
+    ptr = lambda a, ty: np.ascontiguousarray(a).ctypes.data_as(C.POINTER(ty))
+    keep = [np.ascontiguousarray(a) for a in (tbl.p[id, ig], tbl.nt[id, ig], tbl.t[id, ig],
+                                              tbl.nu[id, ig], tbl.u[id, ig], tbl.eps[id, ig])]
+    return L.jgb_write_table_file(str(path).encode(), fmt, int(tbl.np_[id, ig]),
+                                  keep[0].ctypes.data_as(C.POINTER(C.c_double)),
+                                  keep[1].ctypes.data_as(C.POINTER(C.c_int)),
+                                  keep[2].ctypes.data_as(C.POINTER(C.c_double)),
+                                  keep[3].ctypes.data_as(C.POINTER(C.c_int)),
+                                  keep[4].ctypes.data_as(C.POINTER(C.c_float)),
+                                  keep[5].ctypes.data_as(C.POINTER(C.c_float)), tt, tu)
+
+
+def _same_table(got, tbl, id, ig):
+    rc, n, p, nt, t, nu, u, e = got
+    assert rc == 0 and n == tbl.np_[id, ig]
+    assert np.array_equal(p, tbl.p[id, ig]) and np.array_equal(nt, tbl.nt[id, ig])
+    assert np.array_equal(t, tbl.t[id, ig]) and np.array_equal(nu, tbl.nu[id, ig])
+    assert np.array_equal(u, tbl.u[id, ig]) and np.array_equal(e, tbl.eps[id, ig])
+
+
+@pytest.mark.parametrize("fmt", [1, 2])
+def test_library_table_files_match_host_mirror(tmp_path, built_lib, fmt):
+    """Files written by the host mirror read by the library equal the host
+    mirror's reading; the library writes the same bytes; binary -> ASCII ->
+    binary through the library restores every value (tblfmt conversion)."""
+    import copy
+    from jurassic_gb300 import native, synth
+    from jurassic_gb300.tables import read_tbl, write_tbl
+    L = native.load()
+    w = synth.config_limb_ega()
+    ctl = copy.deepcopy(w.ctl)
+    ctl.tblbase = str(tmp_path / "tbl")
+    ctl.tblfmt = fmt
+    tbl = synth.make_tables(ctl, 5, tp=12, tt=5, tu=40)
+    write_tbl(ctl, tbl)
+    back = read_tbl(ctl, 12, 5, 40)
+    for id in range(ctl.nd):
+        for ig in range(ctl.ng):
+            fn = ctl.table_filename(id, ig)
+            _same_table(_c_read(L, fn, fmt, 12, 5, 40), back, id, ig)
+            out = tmp_path / ("c_%d_%d" % (id, ig))
+            assert _c_write(L, out, fmt, tbl, id, ig) == 0
+            assert out.read_bytes() == open(fn, "rb").read()
+            other = tmp_path / ("x_%d_%d" % (id, ig))
+            assert _c_write(L, other, 3 - fmt, tbl, id, ig) == 0
+            _same_table(_c_read(L, other, 3 - fmt, 12, 5, 40), back, id, ig)
+
+
+def test_library_reads_reference_ascii_tables(tmp_path, built_lib):
+    """The ASCII table files with skipped and folded lines that the reference
+    read (golden fixture): the library reads the same tables as the host
+    mirror, which the oracle pins to the reference's forward model."""
+    import golden_io as G
+    from jurassic_gb300 import native
+    from jurassic_gb300.tables import read_tbl
+    L = native.load()
+    f = G.load("ref_tbl_ascii.npz")
+    ctl = G.ctl_from(f["ctl"])
+    ctl.tblbase = str(tmp_path / "tbl")
+    for id in range(ctl.nd):
+        for ig in range(ctl.ng):
+            with open(ctl.table_filename(id, ig), "wb") as fo:
+                fo.write(f["tbl_%d_%d" % (id, ig)].tobytes())
+    tbl = read_tbl(ctl, 32, 6, 64)
+    for id in range(ctl.nd):
+        for ig in range(ctl.ng):
+            _same_table(_c_read(L, ctl.table_filename(id, ig), 1, 32, 6, 64), tbl, id, ig)
+
+
+def test_library_table_file_errors(tmp_path, built_lib):
+    """Missing and truncated files are JGB_ERR_IO, tables beyond the
+    capacities JGB_ERR_ARG (the reference's ERRMSG cases), a bad format
+    JGB_ERR_ARG."""
+    import copy
+    from jurassic_gb300 import native, synth
+    from jurassic_gb300.tables import write_tbl
+    L = native.load()
+    w = synth.config_limb_ega()
+    ctl = copy.deepcopy(w.ctl)
+    ctl.tblbase = str(tmp_path / "tbl")
+    ctl.tblfmt = 2
+    tbl = synth.make_tables(ctl, 5, tp=12, tt=5, tu=40)
+    write_tbl(ctl, tbl)
+    fn = ctl.table_filename(0, 0)
+    assert _c_read(L, tmp_path / "none.bin", 2, 12, 5, 40)[0] == native.ERR_IO
+    data = open(fn, "rb").read()
+    (tmp_path / "cut.bin").write_bytes(data[: len(data) // 2])
+    assert _c_read(L, tmp_path / "cut.bin", 2, 12, 5, 40)[0] == native.ERR_IO
+    assert _c_read(L, fn, 2, 11, 5, 40)[0] == native.ERR_ARG
+    assert _c_read(L, fn, 2, 12, 4, 40)[0] == native.ERR_ARG
+    assert _c_read(L, fn, 2, 12, 5, 10)[0] == native.ERR_ARG
+    assert _c_read(L, fn, 3, 12, 5, 40)[0] == native.ERR_ARG
