@@ -11,8 +11,13 @@
  *   channel-major results rad/tau [nd][nray] (obs_t, jurassic.h:766-772),
  *   emitter-major volume mixing ratios q [ng][nlev] (atm_t, jurassic.h:518).
  *
- * Threading: a context owns one CUDA stream; calls on one context must not
- * overlap (use one context per host thread).  Contexts are independent.
+ * Threading: a context owns one CUDA stream, and every entry point that takes
+ * a context (or an engine of it) holds the context's lock while it runs, so
+ * host threads may share a context: their calls run one after another, as
+ * the reference's kernel() calls formod from OpenMP threads
+ * (jurassic.c:4036).  Contexts are independent; one context per thread runs
+ * calls side by side.  jgb_last_error gives the message of the last failed
+ * call on the context, from whichever thread.
  */
 #ifndef JURASSIC_GB300_H
 #define JURASSIC_GB300_H
@@ -277,8 +282,8 @@ int jgb_retrieve_batch(jgb_ctx *ctx, const jgb_ret *ret, const jgb_batch *b, dou
    results do not depend on which other requests share its steps.  Peak
    device memory is about twice the working set (it is rebuilt into a
    second buffer when requests join or leave) plus the forward-model scratch
-   of the context.  Not thread-safe: one host thread per engine, and the
-   engine uses its context's stream. */
+   of the context.  The engine uses its context's stream, and its calls hold
+   the context's lock like every other call on the context. */
 typedef struct jgb_engine jgb_engine;
 
 typedef struct {

@@ -841,6 +841,8 @@ int ctx_view(jgb_ctx* x, CtxView* out) {
 }
 
 int ctx_fail(jgb_ctx* x, int code, const char* msg) { return fail(x, code, msg); }
+void ctx_lock(jgb_ctx* x) { x->mu.lock(); }
+void ctx_unlock(jgb_ctx* x) { x->mu.unlock(); }
 int ctx_error(jgb_ctx* x, int code, const std::string& msg) { return fail(x, code, msg); }
 
 }  // namespace jgb
@@ -1230,6 +1232,7 @@ int jgb_create(const jgb_ctl* ctl, int device, jgb_ctx** out) {
 
 void jgb_destroy(jgb_ctx* x) {
   if (!x) return;
+  { jgb::CtxLock lock(x); }  // calls still running on other threads end first
   cudaSetDevice(x->device);
   if (x->stream) cudaStreamSynchronize(x->stream);
   DevBuf* bufs[] = {&x->d_nu, &x->d_window, &x->d_clnu, &x->d_sfnu, &x->d_ctm, &x->t_np,
@@ -1259,6 +1262,7 @@ void jgb_destroy(jgb_ctx* x) {
 const char* jgb_last_error(const jgb_ctx* x) { return x ? x->err.c_str() : "null context"; }
 
 int jgb_tables_init(jgb_ctx* x, int tp, int tt, int tu) {
+  jgb::CtxLock lock(x);
   if (!x || tp < 2 || tt < 2 || tu < 2) return fail(x, JGB_ERR_ARG, "bad table capacities");
   cudaSetDevice(x->device);
   const CtlDev& c = x->c;
@@ -1296,6 +1300,7 @@ int jgb_tables_init(jgb_ctx* x, int tp, int tt, int tu) {
 int jgb_set_table(jgb_ctx* x, int id, int ig, int np, const double* p, const int* nt,
                   const double* t, const int* nu, const float* u, const float* eps, int tt_cap,
                   int tu_cap) {
+  jgb::CtxLock lock(x);
   if (!x || !x->tables_init) return fail(x, JGB_ERR_STATE, "jgb_tables_init not called");
   const CtlDev& c = x->c;
   if (id < 0 || id >= c.nd || ig < 0 || ig >= c.ng) return fail(x, JGB_ERR_ARG, "table index");
@@ -1349,24 +1354,28 @@ int jgb_set_table(jgb_ctx* x, int id, int ig, int np, const double* p, const int
 }
 
 int jgb_set_fd_resume(jgb_ctx* x, int mode) {
+  jgb::CtxLock lock(x);
   if (!x || mode < 0 || mode > 2) return fail(x, JGB_ERR_ARG, "bad resume setting");
   x->fd_resume = mode;
   return JGB_OK;
 }
 
 int jgb_set_path_split(jgb_ctx* x, int mode) {
+  jgb::CtxLock lock(x);
   if (!x || mode < -1 || mode > 1) return fail(x, JGB_ERR_ARG, "bad path split mode");
   x->path_split = mode;
   return JGB_OK;
 }
 
 int jgb_set_los_bound_scale(jgb_ctx* x, double scale) {
+  jgb::CtxLock lock(x);
   if (!x || !(scale >= 0) || scale > 1e6) return fail(x, JGB_ERR_ARG, "bad LOS bound scale");
   x->los_bound_scale = scale;
   return JGB_OK;
 }
 
 int jgb_set_fov(jgb_ctx* x, int n, const double* dz, const double* w) {
+  jgb::CtxLock lock(x);
   if (!x || n < 0 || (n > 0 && (!dz || !w))) return fail(x, JGB_ERR_ARG, "bad field of view");
   if (n == 1) return fail(x, JGB_ERR_ARG, "Could not read any data!");  // read_shape needs >= 2
   if (n > 20000) return fail(x, JGB_ERR_ARG, "Too many data points!");  // NSHAPE
@@ -1381,6 +1390,7 @@ int jgb_set_fov(jgb_ctx* x, int n, const double* dz, const double* w) {
 }
 
 int jgb_set_filter(jgb_ctx* x, int id, int n, const double* fnu, const double* f) {
+  jgb::CtxLock lock(x);
   if (!x || id < 0 || id >= x->c.nd || n < 2 || !fnu || !f)
     return fail(x, JGB_ERR_ARG, "bad filter function");
   cudaSetDevice(x->device);
@@ -1404,6 +1414,7 @@ int jgb_set_filter(jgb_ctx* x, int id, int n, const double* fnu, const double* f
 }
 
 int jgb_set_srcfunc(jgb_ctx* x, const double* sr) {
+  jgb::CtxLock lock(x);
   if (!x || !sr) return fail(x, JGB_ERR_ARG, "null source function");
   cudaSetDevice(x->device);
   CK(cudaMemcpy(x->s_sr.p, sr, sizeof(double) * kNS * x->c.nd, cudaMemcpyHostToDevice));
@@ -1413,6 +1424,7 @@ int jgb_set_srcfunc(jgb_ctx* x, const double* sr) {
 }
 
 int jgb_get_srcfunc(jgb_ctx* x, double* st, double* sr) {
+  jgb::CtxLock lock(x);
   if (!x) return JGB_ERR_ARG;
   cudaSetDevice(x->device);
   if (st) CK(cudaMemcpy(st, x->s_st.p, sizeof(double) * kNS, cudaMemcpyDeviceToHost));
@@ -1427,6 +1439,7 @@ int jgb_get_srcfunc(jgb_ctx* x, double* st, double* sr) {
 // the first chunk's inputs and the last chunk's results move while the
 // device waits.  Rays are independent, so the results are those of one batch.
 int jgb_formod_batch(jgb_ctx* x, const jgb_batch* hb, int precision) {
+  jgb::CtxLock lock(x);
   if (!x || !hb || hb->nobs <= 0) return fail(x, JGB_ERR_ARG, "empty batch");
   if (precision != JGB_FP64 && precision != JGB_MIXED) return fail(x, JGB_ERR_ARG, "precision");
   int rc = check_ready(x);
@@ -1617,6 +1630,7 @@ int jgb_formod_batch(jgb_ctx* x, const jgb_batch* hb, int precision) {
 }
 
 int jgb_formod_batch_dev(jgb_ctx* x, const jgb_batch* db, int precision) {
+  jgb::CtxLock lock(x);
   if (!x || !db || db->nobs <= 0) return fail(x, JGB_ERR_ARG, "empty batch");
   if (precision != JGB_FP64 && precision != JGB_MIXED) return fail(x, JGB_ERR_ARG, "precision");
   int rc = check_ready(x);
@@ -1674,6 +1688,7 @@ int jgb_formod(jgb_ctx* x, int np, const double* time, const double* z, const do
                const double* lat, double* p, const double* t, const double* q, const double* k,
                const double* scal, int nr, const double* geo, double* rad, double* tau,
                double* tp, int precision) {
+  jgb::CtxLock lock(x);
   const int lev_off[2] = {0, np};
   const int ray_off[2] = {0, nr};
   jgb_batch b{};
@@ -1697,6 +1712,7 @@ int jgb_formod(jgb_ctx* x, int np, const double* time, const double* z, const do
 }
 
 int jgb_kernel_sizes(jgb_ctx* x, const jgb_batch* hb, int* m, int* n) {
+  jgb::CtxLock lock(x);
   if (!x || !hb || !m || !n || hb->nobs <= 0) return fail(x, JGB_ERR_ARG, "bad arguments");
   const CtlDev& c = x->c;
   const int nray = hb->ray_off[hb->nobs];
@@ -1714,6 +1730,7 @@ int jgb_kernel_sizes(jgb_ctx* x, const jgb_batch* hb, int* m, int* n) {
 }
 
 int jgb_kernel_batch(jgb_ctx* x, const jgb_batch* hb, double* kmat, int precision) {
+  jgb::CtxLock lock(x);
   if (!x || !hb || !kmat || hb->nobs <= 0) return fail(x, JGB_ERR_ARG, "bad arguments");
   cudaSetDevice(x->device);
   const CtlDev& c = x->c;
@@ -1761,6 +1778,7 @@ int jgb_kernel_batch(jgb_ctx* x, const jgb_batch* hb, double* kmat, int precisio
 }
 
 int jgb_get_stats(const jgb_ctx* x, jgb_stats* out) {
+  jgb::CtxLock lock(x);
   if (!x || !out) return JGB_ERR_ARG;
   *out = x->stats;
   return JGB_OK;
@@ -1843,6 +1861,7 @@ int jgb_measure_l2_read(unsigned long long bytes, int passes, double* gbs) {
 // variants of every observation run as one batch.
 extern "C" int jgb_formod_contrib(jgb_ctx* x, const jgb_batch* hb, double* rad_out,
                                   double* tau_out, int precision) {
+  jgb::CtxLock lock(x);
   if (!x || !hb || hb->nobs <= 0 || !rad_out) return fail(x, JGB_ERR_ARG, "bad arguments");
   const CtlDev c = x->c;
   const int nobs = hb->nobs, ng = c.ng, nw = c.nw, nv = ng + 1;

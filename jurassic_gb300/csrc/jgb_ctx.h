@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -102,6 +103,9 @@ struct jgb_ctx {
   std::vector<float> tune_ms;
   jgb_stats stats{};
   std::string err;
+  // serialises the public entry points of the context (recursive: one entry
+  // point may call another), so that host threads may share a context
+  std::recursive_mutex mu;
 };
 
 namespace jgb {

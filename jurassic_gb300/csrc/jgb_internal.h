@@ -99,4 +99,20 @@ int normal_equations_dev(int nret, const int* m, const int* n, const double* K, 
 size_t normal_desc_bytes(int nret);
 int ctx_fail(jgb_ctx* x, int code, const char* msg);
 
+// The context's (recursive) lock for the duration of a public call: host
+// threads may share a context, and their calls run one after another.
+void ctx_lock(jgb_ctx* x);
+void ctx_unlock(jgb_ctx* x);
+struct CtxLock {
+  jgb_ctx* x;
+  explicit CtxLock(const jgb_ctx* c) : x(const_cast<jgb_ctx*>(c)) {
+    if (x) ctx_lock(x);
+  }
+  ~CtxLock() {
+    if (x) ctx_unlock(x);
+  }
+  CtxLock(const CtxLock&) = delete;
+  CtxLock& operator=(const CtxLock&) = delete;
+};
+
 }  // namespace jgb

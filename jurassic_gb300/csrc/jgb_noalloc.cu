@@ -102,6 +102,7 @@ __global__ void k_noalloc_scan(int n, const int* count, long long* off) {
 using namespace jgb;
 
 extern "C" int jgb_formod_batch_dev_noalloc(jgb_ctx* x, const jgb_batch* db) {
+  jgb::CtxLock lock(x);
   if (!x || !db || db->nobs <= 0) return ctx_fail(x, JGB_ERR_ARG, "empty batch");
   CtxView v;
   int rc = ctx_view(x, &v);

@@ -549,6 +549,7 @@ using namespace jgb;
 extern "C" int jgb_normal_equations(jgb_ctx* x, int nret, const int* m, const int* n,
                                     const double* K, const double* w, const double* dy,
                                     double* A, double* b, int precision) {
+  jgb::CtxLock lock(x);
   if (!x || nret <= 0 || !m || !n || !K || !w || !dy || !A || !b)
     return ctx_fail(x, JGB_ERR_ARG, "bad arguments");
   CtxView v;
@@ -592,6 +593,7 @@ extern "C" int jgb_normal_equations(jgb_ctx* x, int nret, const int* m, const in
 extern "C" int jgb_normal_equations_dev(jgb_ctx* x, int nret, const int* m, const int* n,
                                         const double* K, const double* w, const double* dy,
                                         double* A, double* b, int precision, float* kernel_ms) {
+  jgb::CtxLock lock(x);
   if (!x || nret <= 0 || !m || !n || !K || !w || !dy || !A || !b)
     return ctx_fail(x, JGB_ERR_ARG, "bad arguments");
   if (nret > 65535) return ctx_fail(x, JGB_ERR_ARG, "at most 65535 problems per call");

@@ -1485,6 +1485,7 @@ int engine_step(jgb_engine* E) {
 extern "C" int jgb_engine_create(jgb_ctx* x, const jgb_ret* ret, int precision,
                                  unsigned long long mem_budget, int max_active, int keep_gain,
                                  jgb_engine** out) {
+  jgb::CtxLock lock(x);
   if (!x || !ret || !out) return ctx_error(x, JGB_ERR_ARG, "bad arguments");
   *out = nullptr;
   if (ret->conv_itmax < 0 || ret->kernel_recomp <= 0) return ctx_error(x, JGB_ERR_ARG, "bad retrieval settings");
@@ -1520,6 +1521,7 @@ extern "C" int jgb_engine_create(jgb_ctx* x, const jgb_ret* ret, int precision,
 }
 
 extern "C" void jgb_engine_destroy(jgb_engine* E) {
+  jgb::CtxLock lock(E ? E->x : nullptr);
   if (!E) return;
   cudaSetDevice(E->x->device);
   cudaStreamSynchronize(E->x->stream);
@@ -1527,6 +1529,7 @@ extern "C" void jgb_engine_destroy(jgb_engine* E) {
 }
 
 extern "C" int jgb_engine_submit(jgb_engine* E, const jgb_batch* hb, unsigned long long* ids) {
+  jgb::CtxLock lock(E ? E->x : nullptr);
   if (!E || !hb || hb->nobs <= 0) return ctx_error(E ? E->x : nullptr, JGB_ERR_ARG, "bad arguments");
   jgb_ctx* x = E->x;
   const CtlDev& c = x->c;
@@ -1576,6 +1579,7 @@ extern "C" int jgb_engine_submit(jgb_engine* E, const jgb_batch* hb, unsigned lo
 }
 
 extern "C" int jgb_engine_step(jgb_engine* E, int* n_active, int* n_queued, int* n_done) {
+  jgb::CtxLock lock(E ? E->x : nullptr);
   if (!E) return JGB_ERR_ARG;
   const int rc = engine_step(E);
   if (n_active) *n_active = (int)E->active.size();
@@ -1585,6 +1589,7 @@ extern "C" int jgb_engine_step(jgb_engine* E, int* n_active, int* n_queued, int*
 }
 
 extern "C" int jgb_engine_finished(jgb_engine* E, unsigned long long* ids, int max, int* count) {
+  jgb::CtxLock lock(E ? E->x : nullptr);
   if (!E || !count) return JGB_ERR_ARG;
   int k = 0;
   for (auto it = E->done.begin(); it != E->done.end() && k < max; ++it) ids[k++] = it->first;
@@ -1593,6 +1598,7 @@ extern "C" int jgb_engine_finished(jgb_engine* E, unsigned long long* ids, int m
 }
 
 extern "C" int jgb_engine_sizes(jgb_engine* E, unsigned long long id, int* n, int* m, int* np, int* nr) {
+  jgb::CtxLock lock(E ? E->x : nullptr);
   if (!E) return JGB_ERR_ARG;
   auto it = E->done.find(id);
   if (it == E->done.end()) return ctx_error(E->x, JGB_ERR_ARG, "unknown or unfinished request");
@@ -1605,6 +1611,7 @@ extern "C" int jgb_engine_sizes(jgb_engine* E, unsigned long long id, int* n, in
 }
 
 extern "C" int jgb_engine_result(jgb_engine* E, unsigned long long id, jgb_ret_out* o) {
+  jgb::CtxLock lock(E ? E->x : nullptr);
   if (!E || !o) return JGB_ERR_ARG;
   auto it = E->done.find(id);
   if (it == E->done.end()) return ctx_error(E->x, JGB_ERR_ARG, "unknown or unfinished request");
@@ -1635,6 +1642,7 @@ extern "C" int jgb_engine_result(jgb_engine* E, unsigned long long id, jgb_ret_o
 }
 
 extern "C" int jgb_engine_get_stats(const jgb_engine* E, jgb_engine_stats* out) {
+  jgb::CtxLock lock(E ? E->x : nullptr);
   if (!E || !out) return JGB_ERR_ARG;
   *out = E->st;
   out->active = (int)E->active.size();
@@ -1649,6 +1657,7 @@ extern "C" int jgb_engine_get_stats(const jgb_engine* E, jgb_engine_stats* out) 
 extern "C" int jgb_retrieve_batch(jgb_ctx* x, const jgb_ret* ret, const jgb_batch* hb,
                                   double* x_out, double* cov_out, double* costs, int* iters,
                                   int precision) {
+  jgb::CtxLock lock(x);
   if (!x || !ret || !hb || !x_out || hb->nobs <= 0) return ctx_error(x, JGB_ERR_ARG, "bad arguments");
   if (hb->nobs > 65535) return ctx_error(x, JGB_ERR_ARG, "at most 65535 retrievals per batch");
   const CtlDev& c = x->c;

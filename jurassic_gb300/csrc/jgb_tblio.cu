@@ -245,6 +245,7 @@ extern "C" int jgb_write_table_file(const char* path, int tblfmt, int np, const 
 }
 
 extern "C" int jgb_read_tables(jgb_ctx* x, const char* tblbase, int tblfmt) {
+  jgb::CtxLock lock(x);
   if (!x) return JGB_ERR_ARG;
   if (!tblbase || (tblfmt != 1 && tblfmt != 2))
     return ctx_fail(x, JGB_ERR_ARG, "Unknown look-up table format!");
