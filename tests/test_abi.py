@@ -48,3 +48,83 @@ def test_invalid_control_is_rejected_without_gpu(built_lib):
     h = ctypes.c_void_p()
     assert L.jgb_create(ctypes.byref(c), 0, ctypes.byref(h)) == 1
     assert not h.value
+
+
+C_CONSUMER = r"""
+/* A C99 consumer of the ABI: the header compiles as C, the library links,
+   and host-only calls run (no device work). */
+#include <stdio.h>
+#include <string.h>
+#include "jurassic_gb300.h"
+
+static int same(int np, const double *p, const int *nt, const double *t, const int *nu,
+                const float *u, const float *e, const double *p2, const int *nt2,
+                const double *t2, const int *nu2, const float *u2, const float *e2) {
+  int ip, it;
+  for (ip = 0; ip < np; ip++) {
+    if (p[ip] != p2[ip] || nt[ip] != nt2[ip]) return 0;
+    for (it = 0; it < nt[ip]; it++) {
+      int r = ip * 2 + it;
+      if (t[r] != t2[r] || nu[r] != nu2[r]) return 0;
+      if (memcmp(u + r * 3, u2 + r * 3, sizeof(float) * nu[r]) != 0) return 0;
+      if (memcmp(e + r * 3, e2 + r * 3, sizeof(float) * nu[r]) != 0) return 0;
+    }
+  }
+  return 1;
+}
+
+int main(int argc, char **argv) {
+  double p[2] = {1.0, 10.0}, t[4] = {200.0, 250.0, 220.0, 0.0};
+  int nt[2] = {2, 1}, nu[4] = {3, 2, 3, 0};
+  float u[12], e[12];
+  double p2[2], t2[4];
+  int nt2[2], nu2[4], np2 = -1, fmt, i;
+  float u2[12], e2[12];
+  jgb_ctl c;
+  jgb_ctx *ctx = NULL;
+  char path[4096];
+  if (argc < 2) return 1;
+  for (i = 0; i < 12; i++) {
+    u[i] = 1e18f * (float)(i % 3 + 1);
+    e[i] = 0.1f * (float)(i % 3 + 1);
+  }
+  for (fmt = 1; fmt <= 2; fmt++) {
+    snprintf(path, sizeof path, "%s.%d", argv[1], fmt);
+    if (jgb_write_table_file(path, fmt, 2, p, nt, t, nu, u, e, 2, 3) != JGB_OK) return 2;
+    if (jgb_read_table_file(path, fmt, 2, 2, 3, &np2, p2, nt2, t2, nu2, u2, e2) != JGB_OK) return 3;
+    if (np2 != 2 || !same(2, p, nt, t, nu, u, e, p2, nt2, t2, nu2, u2, e2)) return 4;
+  }
+  memset(&c, 0, sizeof c);
+  c.ng = -1;
+  if (jgb_create(&c, 0, &ctx) != JGB_ERR_ARG || ctx != NULL) return 5;
+  if (jgb_read_table_file(path, 3, 2, 2, 3, &np2, p2, nt2, t2, nu2, u2, e2) != JGB_ERR_ARG) return 6;
+  puts("ok");
+  return 0;
+}
+"""
+
+
+def test_c_consumer_compiles_links_and_runs(tmp_path, built_lib):
+    """The header compiles as strict C99 (the reference is C), a C program
+    links against the library, and its host-only calls (table files, the
+    argument checks of jgb_create) run without a GPU."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    from jurassic_gb300 import native
+    src = tmp_path / "consumer.c"
+    src.write_text(C_CONSUMER)
+    exe = tmp_path / "consumer"
+    libdir = os.path.dirname(native.LIB_PATH)
+    r = subprocess.run([cc, "-std=c99", "-pedantic", "-Wall", "-Wextra", "-Werror",
+                        "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+                        "-L", libdir, "-ljurassic_gb300", "-Wl,-rpath," + libdir],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    env = dict(os.environ)
+    cuda_lib = "/usr/local/cuda/lib64"
+    env["LD_LIBRARY_PATH"] = ":".join(x for x in (env.get("LD_LIBRARY_PATH", ""), cuda_lib) if x)
+    r = subprocess.run([str(exe), str(tmp_path / "tbl")], capture_output=True, text=True, env=env)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", (r.returncode, r.stdout, r.stderr)
