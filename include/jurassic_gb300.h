@@ -349,7 +349,9 @@ int jgb_get_stats(const jgb_ctx *ctx, jgb_stats *out);
    - The first call on a device resolves the array's address on that device;
      make that first call before any stream capture.
    - All calls on a device share the array and it keeps the previous call's
-     contents: calls that overlap on the GPU race and must be serialised. */
+     contents: calls on one context run one after another (the context's
+     lock), but calls from different contexts on one device that overlap on
+     the GPU race and must be serialised by the caller. */
 int jgb_formod_batch_dev_noalloc(jgb_ctx *ctx, const jgb_batch *b);
 
 /* Page-locked host memory for fast transfers (cudaHostAlloc). */
@@ -367,6 +369,13 @@ int jgb_memcpy_d2h(void *dst, const void *src, unsigned long long bytes);
    5 launches timed with CUDA events.  Roofline denominator for the
    table-lookup loop, whose probes are served by L1 and L2. */
 int jgb_measure_l2_read(unsigned long long bytes, int passes, double *gbs);
+
+/* Self-test of the device-side bounded wait (the mbarrier wait of the
+   tensor-core kernels, limited to about one second of the global timer):
+   one thread waits for a barrier phase that completes at once (arrive = 1)
+   or never (arrive = 0).  *timed_out = 1 when the wait gave up, *seconds =
+   how long it waited.  The device stays usable either way. */
+int jgb_selftest_bounded_wait(int device, int arrive, int *timed_out, double *seconds);
 
 #ifdef __cplusplus
 }

@@ -89,9 +89,20 @@ __device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t a, uint64_t b, ui
       "l"(a), "l"(b), "r"(kTcIdesc), "r"(acc));
 }
 
-// Bounded wait for phase `parity` of an mbarrier.
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // one second
+
+// Bounded wait for phase `parity` of an mbarrier: gives up after about a
+// second of the global timer (checked every 64 polls; a poll may suspend the
+// thread for a while), or after 2^30 polls should the timer not advance.
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
-  for (int it = 0; it < (1 << 20); it++) {
+  const unsigned long long t0 = global_ns();
+  for (int it = 0; it < (1 << 30); it++) {
     uint32_t ok;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
@@ -100,8 +111,26 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
         : "r"(mbar), "r"(parity)
         : "memory");
     if (ok) return true;
+    if ((it & 63) == 63 && global_ns() - t0 > kWaitLimitNs) return false;
   }
   return false;
+}
+
+// Self-test of mbar_wait: one thread initialises an mbarrier for one
+// arrival and waits for its first phase; with arrive != 0 it arrives first
+// (the wait succeeds at once), otherwise nothing ever arrives and the wait
+// must give up.  Records the outcome and the waiting time.
+__global__ void k_wait_selftest(int arrive, unsigned long long* out) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar)));
+  asm volatile("fence.mbarrier_init.release.cluster;");
+  if (arrive)
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&bar)) : "memory");
+  const unsigned long long t0 = global_ns();
+  const bool ok = mbar_wait(smem_u32(&bar), 0);
+  out[0] = ok ? 0ull : 1ull;
+  out[1] = global_ns() - t0;
 }
 
 // Exact float -> double widening with integer operations on the two 32-bit
@@ -541,9 +570,30 @@ int normal_equations_dev(int nret, const int* m, const int* n, const double* K, 
 
 size_t normal_desc_bytes(int nret) { return sizeof(NeDesc) * (size_t)nret; }
 
+int wait_selftest(int device, int arrive, int* timed_out, double* seconds) {
+  if (!timed_out || !seconds) return JGB_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return JGB_ERR_CUDA;
+  unsigned long long* d = nullptr;
+  if (cudaMalloc(&d, 2 * sizeof(unsigned long long)) != cudaSuccess) return JGB_ERR_CUDA;
+  unsigned long long h[2] = {2, 0};
+  k_wait_selftest<<<1, 32>>>(arrive, d);
+  int rc = cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess &&
+                   cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost) == cudaSuccess
+               ? JGB_OK
+               : JGB_ERR_CUDA;
+  cudaFree(d);
+  *timed_out = (int)h[0];
+  *seconds = (double)h[1] * 1e-9;
+  return rc;
+}
+
 }  // namespace jgb
 
 using namespace jgb;
+
+extern "C" int jgb_selftest_bounded_wait(int device, int arrive, int* timed_out, double* seconds) {
+  return wait_selftest(device, arrive, timed_out, seconds);
+}
 
 // Host-buffer entry point: copies in, computes, copies out.
 extern "C" int jgb_normal_equations(jgb_ctx* x, int nret, const int* m, const int* n,

@@ -154,6 +154,7 @@ SIGNATURES = {
     "jgb_host_free": (None, [C.c_void_p]),
     "jgb_dev_alloc": (C.c_void_p, [C.c_ulonglong]),
     "jgb_measure_l2_read": (C.c_int, [C.c_ulonglong, C.c_int, C.POINTER(C.c_double)]),
+    "jgb_selftest_bounded_wait": (C.c_int, [C.c_int, C.c_int, _ip, C.POINTER(C.c_double)]),
     "jgb_dev_free": (None, [C.c_void_p]),
     "jgb_memcpy_h2d": (C.c_int, [C.c_void_p, C.c_void_p, C.c_ulonglong]),
     "jgb_memcpy_d2h": (C.c_int, [C.c_void_p, C.c_void_p, C.c_ulonglong]),

@@ -71,3 +71,25 @@ def test_normal_equations_many_tiles_per_sm(built_lib):
         assert np.max(np.abs(b - br) / (d * sdy)) <= 1e-5
         assert np.array_equal(A, A.T)
         assert np.array_equal(A, A2) and np.array_equal(b, b2)
+
+
+def test_bounded_wait_gives_up_and_device_stays_usable(built_lib):
+    """The tensor-core kernels' mbarrier waits are bounded: a wait for a phase
+    that nothing completes gives up after about a second of the global timer
+    and reports it (the kernel's error word turns into a status on the host);
+    a phase that completes is seen at once; the device keeps working."""
+    import ctypes as C
+    L = native.load()
+    to, sec = C.c_int(-1), C.c_double(-1.0)
+    assert L.jgb_selftest_bounded_wait(0, 1, C.byref(to), C.byref(sec)) == 0
+    assert to.value == 0 and sec.value < 0.01
+    assert L.jgb_selftest_bounded_wait(0, 0, C.byref(to), C.byref(sec)) == 0
+    assert to.value == 1 and 0.9 <= sec.value < 5.0
+    rng = np.random.default_rng(3)
+    K = [rng.standard_normal((40, 70))]
+    w = [np.ones(40)]
+    dy = [rng.standard_normal(40)]
+    A, b = _ctx().normal_equations(K, w, dy, native.MIXED)
+    Ar, br = _ref(K[0], w[0], dy[0])
+    d = np.sqrt(np.diag(Ar))
+    assert np.max(np.abs(A[0] - Ar) / np.outer(d, d)) <= 1e-5
