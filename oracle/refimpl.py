@@ -24,6 +24,11 @@ def lib_path(tag="std"):
     return os.path.join(REF_DIR, "libjref_%s.so" % tag)
 
 
+def source_dir():
+    """The reference tree (present in the build container only)."""
+    return os.environ.get("JURASSIC_REF_DIR", "/root/reference")
+
+
 def available(tag="std"):
     return os.path.exists(lib_path(tag))
 

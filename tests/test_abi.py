@@ -128,3 +128,28 @@ def test_c_consumer_compiles_links_and_runs(tmp_path, built_lib):
     env["LD_LIBRARY_PATH"] = ":".join(x for x in (env.get("LD_LIBRARY_PATH", ""), cuda_lib) if x)
     r = subprocess.run([str(exe), str(tmp_path / "tbl")], capture_output=True, text=True, env=env)
     assert r.returncode == 0 and r.stdout.strip() == "ok", (r.returncode, r.stdout, r.stderr)
+
+
+def test_integration_binding_compiles_against_reference_header(tmp_path):
+    """The binding shown in INTEGRATION.md (jur_unified_init and
+    jur_unified_formod_multiple_packages on top of this library, the seam of
+    formod.c:60-76) compiles against the reference's own jurassic.h (its
+    ctl_t, atm_t, obs_t and dimensions) and this header, warnings as errors.
+    Skipped where the reference tree is absent."""
+    import shutil
+    import subprocess
+    from oracle import refimpl
+    cc = shutil.which("gcc") or shutil.which("cc")
+    src_dir = os.path.join(refimpl.source_dir(), "src")
+    if cc is None or not os.path.isfile(os.path.join(src_dir, "jurassic.h")):
+        pytest.skip("reference tree or C compiler not available")
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    start = text.index("/* jurassic_unified_library.c")
+    code = text[start:text.index("```", start)]
+    src = tmp_path / "jurassic_unified_library.c"
+    src.write_text(code)
+    r = subprocess.run([cc, "-std=gnu99", "-Wall", "-Wextra", "-Werror", "-fopenmp",
+                        "-isystem", src_dir, "-isystem", os.path.join(ROOT, "oracle", "gsl_shim"),
+                        "-I", os.path.join(ROOT, "include"), "-c", str(src),
+                        "-o", str(tmp_path / "binding.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
