@@ -260,8 +260,9 @@ extern "C" int jgb_read_tables(jgb_ctx* x, const char* tblbase, int tblfmt) {
     for (int ig = 0; ig < ng; ig++) {
       // file name of read_tbl (jurassic.c:4968)
       char fn[4096];
-      std::snprintf(fn, sizeof fn, "%s_%.4f_%s.%s", tblbase, x->nu[id], x->emitter[ig].c_str(),
-                    tblfmt == 1 ? "tab" : "bin");
+      const int len = std::snprintf(fn, sizeof fn, "%s_%.4f_%s.%s", tblbase, x->nu[id],
+                                    x->emitter[ig].c_str(), tblfmt == 1 ? "tab" : "bin");
+      if (len < 0 || len >= (int)sizeof fn) return ctx_fail(x, JGB_ERR_ARG, "table file name too long");
       int np = -1;
       FILE* probe = std::fopen(fn, "rb");
       if (probe) {  // a missing file leaves the table empty (the reference warns)
