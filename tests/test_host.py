@@ -279,3 +279,26 @@ def test_library_table_file_errors(tmp_path, built_lib):
     assert _c_read(L, fn, 2, 12, 4, 40)[0] == native.ERR_ARG
     assert _c_read(L, fn, 2, 12, 5, 10)[0] == native.ERR_ARG
     assert _c_read(L, fn, 3, 12, 5, 40)[0] == native.ERR_ARG
+
+
+def test_ascii_table_level_starting_at_previous_temperature(tmp_path, built_lib):
+    """A pressure level whose first point repeats the last temperature of the
+    level before opens a temperature row (the reference's temperature index
+    would stay at -1 there): both readers give the same two levels of one row
+    each, with nothing written out of range."""
+    from jurassic_gb300 import native
+    from jurassic_gb300.model import Ctl
+    from jurassic_gb300.tables import read_tbl
+    L = native.load()
+    ctl = Ctl(emitter=["CO2"], nu=[700.0])
+    ctl.tblbase = str(tmp_path / "tbl")
+    ctl.tblfmt = 1
+    with open(ctl.table_filename(0, 0), "w") as f:
+        f.write("1.0 250.0 1e18 0.1\n1.0 250.0 2e18 0.2\n"
+                "2.0 250.0 1e18 0.15\n2.0 250.0 3e18 0.3\n")
+    tbl = read_tbl(ctl, 4, 3, 5)
+    assert tbl.np_[0, 0] == 2 and list(tbl.nt[0, 0, :2]) == [1, 1]
+    assert list(tbl.nu[0, 0, :2, 0]) == [2, 2]
+    assert tbl.t[0, 0, 1, 0] == 250.0 and tbl.eps[0, 0, 1, 0, 1] == np.float32(0.3)
+    got = _c_read(L, ctl.table_filename(0, 0), 1, 4, 3, 5)
+    _same_table(got, tbl, 0, 0)
