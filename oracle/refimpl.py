@@ -72,7 +72,6 @@ def _child(args):
     dims = np.zeros(8, np.int32)
     L.jref_dims(dims.ctypes.data_as(C.POINTER(C.c_int)))
     out = []
-    P = lambda a: np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(dp)
     for job in jobs:
         kind, atm, geo, rad = job["kind"], job["atm"], job["geo"], job["rad"]
         npl = len(atm["z"])

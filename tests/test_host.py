@@ -187,7 +187,6 @@ def _c_read(L, path, fmt, tp, tt, tu):
 def _c_write(L, path, fmt, tbl, id, ig):
     import ctypes as C
     tp, tt, tu = tbl.u.shape[2:]
-    ptr = lambda a, ty: np.ascontiguousarray(a).ctypes.data_as(C.POINTER(ty))
     keep = [np.ascontiguousarray(a) for a in (tbl.p[id, ig], tbl.nt[id, ig], tbl.t[id, ig],
                                               tbl.nu[id, ig], tbl.u[id, ig], tbl.eps[id, ig])]
     return L.jgb_write_table_file(str(path).encode(), fmt, int(tbl.np_[id, ig]),
