@@ -153,3 +153,28 @@ def test_integration_binding_compiles_against_reference_header(tmp_path):
                         "-I", os.path.join(ROOT, "include"), "-c", str(src),
                         "-o", str(tmp_path / "binding.o")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_new_entry_points_check_arguments_without_gpu(built_lib):
+    """Bad arguments of the table-file, measurement and self-test entry
+    points return JGB_ERR_ARG before any device work."""
+    from jurassic_gb300 import native
+    L = native.load()
+    n = ctypes.c_int(0)
+    assert L.jgb_read_table_file(None, 2, 1, 1, 1, ctypes.byref(n), None, None, None, None,
+                                 None, None) == native.ERR_ARG
+    p = (ctypes.c_double * 1)(1.0)
+    nt = (ctypes.c_int * 1)(3)          # more temperatures than the capacity
+    t = (ctypes.c_double * 2)(200.0, 210.0)
+    nu = (ctypes.c_int * 2)(1, 1)
+    u = (ctypes.c_float * 2)(1.0, 2.0)
+    e = (ctypes.c_float * 2)(0.1, 0.2)
+    assert L.jgb_write_table_file(b"/nonexistent/x.bin", 2, 1, p, nt, t, nu, u, e, 2, 1) == \
+        native.ERR_ARG
+    assert L.jgb_write_table_file(b"/nonexistent/x.bin", 5, 0, None, None, None, None, None,
+                                  None, 2, 1) == native.ERR_ARG
+    g = ctypes.c_double(0.0)
+    assert L.jgb_measure_l2_read(0, 1, ctypes.byref(g)) == native.ERR_ARG
+    assert L.jgb_measure_l2_read(1 << 20, 0, ctypes.byref(g)) == native.ERR_ARG
+    assert L.jgb_selftest_bounded_wait(0, 0, None, None) == native.ERR_ARG
+    assert L.jgb_read_tables(None, b"tbl", 2) == native.ERR_ARG
