@@ -62,7 +62,9 @@ def _array(body, name, n):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("JURASSIC_REF_DIR")
+    if not ref:
+        raise SystemExit("usage: make_continua.py <reference tree> (or set JURASSIC_REF_DIR)")
     src = open(os.path.join(ref, "src", "jurassic.c")).read()
     parts = [_array(_function_body(src, fn), arr, n) for fn, arr, n in ORDER]
     blob = np.concatenate(parts).tobytes()

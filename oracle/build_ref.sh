@@ -11,9 +11,17 @@
 # usage: oracle/build_ref.sh <tag> [extra -D dimension flags]
 #   e.g. oracle/build_ref.sh std
 #        oracle/build_ref.sh big -DND=320 -DNG=5 -DNR=64
+#        oracle/build_ref.sh --where     (prints the reference tree used)
+# The reference tree is $JURASSIC_REF_DIR; unset, it is the build
+# container's read-only mount below (the only place in the repository that
+# names it).  The GPU machine has no reference tree.
 set -euo pipefail
 REF=${JURASSIC_REF_DIR:-/root/reference}
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+if [ "${1:-}" = "--where" ]; then
+  if [ -f "$REF/src/jurassic.c" ]; then echo "$REF"; exit 0; fi
+  exit 3
+fi
 TAG=${1:-std}
 shift || true
 OUT="$HERE/_ref"

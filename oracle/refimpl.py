@@ -25,8 +25,12 @@ def lib_path(tag="std"):
 
 
 def source_dir():
-    """The reference tree (present in the build container only)."""
-    return os.environ.get("JURASSIC_REF_DIR", "/root/reference")
+    """The reference tree as the build recipe resolves it ($JURASSIC_REF_DIR,
+    else the build container's mount), or None where there is none (the GPU
+    box)."""
+    r = subprocess.run(["bash", os.path.join(HERE, "build_ref.sh"), "--where"],
+                       capture_output=True, text=True)
+    return r.stdout.strip() if r.returncode == 0 and r.stdout.strip() else None
 
 
 def available(tag="std"):

@@ -247,7 +247,9 @@ def retrieval_case():
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else refimpl.source_dir()
+    if not ref:
+        raise SystemExit("usage: make_golden.py <reference tree> (or set JURASSIC_REF_DIR)")
     if not refimpl.available("std"):
         refimpl.build("std")
     reftests(ref)
