@@ -340,18 +340,23 @@ int jgb_get_stats(const jgb_ctx *ctx, jgb_stats *out);
    point has no counterpart in the reference.  It is for callers that cannot
    allocate GPU memory while they run (a fixed memory budget handed over at
    start-up, an allocator owned by another runtime, sections where allocation
-   is forbidden): all scratch comes from one 64 MiB device array that the
-   library holds on every GPU where it is loaded until the process exits, and
-   no cudaMalloc/cudaFree or allocating library routine is called.  Same
+   is forbidden): all scratch comes from one 64 MiB device array, and no
+   cudaMalloc/cudaFree or allocating library routine is called.  Same
    arguments and results as jgb_formod_batch_dev with JGB_FP64.
+   - The array is part of the library's device code.  jgb_create loads it,
+     with the kernels this entry point launches, onto the context's device
+     and resolves its address there, so the calls themselves load and
+     allocate nothing; it stays on every device where it was loaded until the
+     process exits.
    - A batch whose rays and LOS points need more than 64 MiB of scratch is
-     rejected with JGB_ERR_ARG (jgb_last_error names the bytes needed).
-   - The first call on a device resolves the array's address on that device;
-     make that first call before any stream capture.
+     rejected with JGB_ERR_ARG (jgb_last_error names the bytes needed); a
+     field of view is not available here (JGB_ERR_UNSUPPORTED).
    - All calls on a device share the array and it keeps the previous call's
      contents: calls on one context run one after another (the context's
      lock), but calls from different contexts on one device that overlap on
-     the GPU race and must be serialised by the caller. */
+     the GPU race and must be serialised by the caller.
+   - jgb_get_stats then reports the call's LOS points, kernel launches and
+     total device time; its per-stage times are zero. */
 int jgb_formod_batch_dev_noalloc(jgb_ctx *ctx, const jgb_batch *b);
 
 /* Page-locked host memory for fast transfers (cudaHostAlloc). */

@@ -1151,6 +1151,10 @@ int jgb_create(const jgb_ctl* ctl, int device, jgb_ctx** out) {
     jgb_destroy(x);
     return JGB_ERR_CUDA;
   }
+  // the allocation-free entry point's scratch array and kernels go onto the
+  // device here, so that its calls load nothing (a failure is retried and
+  // reported by its first call)
+  (void)jgb::noalloc_prepare(device);
   CtlDev& c = x->c;
   c.ng = ctl->ng;
   c.nd = ctl->nd;

@@ -14,6 +14,7 @@
 //                 (3026-3071); one thread per (ray, channel).
 //   k_srcfunc     init_srcfunc (jurassic.c:3631-3681) on the device.
 //   k_hydrostatic hydrostatic (jurassic.c:3520-3582), one thread per profile.
+#include "../../include/jurassic_gb300.h"
 #include "jgb_common.cuh"
 #include "jgb_internal.h"
 
@@ -728,6 +729,18 @@ void launch_fov(const CtlDev& c, const BatchDev& b, const double* prad, const do
 void launch_hydrostatic(const CtlDev& c, const BatchDev& b, double* p_out, cudaStream_t s) {
   const int bs = 64;
   k_hydrostatic<<<(b.nobs + bs - 1) / bs, bs, 0, s>>>(c, b, p_out);
+}
+
+// Loads the FP64 forward-model kernels onto the current device (CUDA loads
+// modules lazily, at a kernel's first launch or attribute query), so that a
+// later first launch allocates no device memory for their code.
+int preload_fp64_kernels() {
+  cudaFuncAttributes a;
+  const void* fns[] = {(const void*)k_trace_count, (const void*)k_trace_fill,
+                       (const void*)k_path_fp64, (const void*)k_hydrostatic};
+  for (const void* f : fns)
+    if (cudaFuncGetAttributes(&a, f) != cudaSuccess) return JGB_ERR_CUDA;
+  return JGB_OK;
 }
 
 }  // namespace jgb

@@ -30,6 +30,14 @@ void launch_path_fp64(const CtlDev& c, const TblDev& T, const ChanDev& ch, const
 void launch_srcfunc(int nd, int id0, int nch, const int* fn_off, const double* fnu,
                     const double* f, const double* st, double* sr, cudaStream_t s);
 void launch_hydrostatic(const CtlDev& c, const BatchDev& b, double* p_out, cudaStream_t s);
+// loads the kernels above onto the current device (JGB_OK or JGB_ERR_CUDA)
+int preload_fp64_kernels();
+
+// jgb_noalloc.cu: loads the allocation-free entry point's scratch array and
+// kernels onto the device and resolves the array's address there (called by
+// jgb_create with the device current; a failure is reported by the entry
+// point's first call, which retries)
+int noalloc_prepare(int device);
 
 // jgb_mixed.cu
 struct MixedPlan {

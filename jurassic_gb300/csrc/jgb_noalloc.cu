@@ -7,20 +7,25 @@
 // runtime that must not see cudaMalloc/cudaFree traffic, or code that
 // drives the GPU from a section where allocation is forbidden.  For them
 // this entry point takes every scratch buffer (per-ray bookkeeping, the
-// LOS arrays, the reflection scratch) from one file-scope device array that
-// exists from library load until process exit, instead of the context's
-// grow-on-demand buffers.  The caller still owns all inputs and outputs.
+// LOS arrays, the reflection scratch) from one file-scope device array
+// instead of the context's grow-on-demand buffers.  The caller still owns
+// all inputs and outputs.
 //
 // Limits and rules:
-//  * the scratch array holds kNoAllocBytes (64 MiB) on every GPU on which
-//    the library is loaded; a batch whose rays and LOS points do not fit is
-//    rejected with JGB_ERR_ARG and a message naming the bytes it needs;
-//  * the first call on a device resolves the array's device address with
-//    cudaGetSymbolAddress (once per device, with that device current);
-//    make that first call before any stream capture;
+//  * the scratch array holds kNoAllocBytes (64 MiB); a batch whose rays and
+//    LOS points do not fit is rejected with JGB_ERR_ARG and a message naming
+//    the bytes it needs;
+//  * the array is part of this file's device code, which CUDA loads onto a
+//    device lazily; jgb_create loads it (and the kernels this entry point
+//    launches) onto the context's device and resolves the array's address
+//    there with cudaGetSymbolAddress, with that device current, so a call
+//    itself loads and allocates nothing.  The array then stays on that
+//    device until the process exits.  Should that set-up fail at
+//    jgb_create, the first call retries it and returns JGB_ERR_CUDA if it
+//    still fails;
 //  * every call on a device shares the same array and it keeps the previous
-//    call's contents; calls that overlap on the GPU (two host threads, two
-//    contexts of one device) race on it and must be serialised by the caller;
+//    call's contents; calls that overlap on the GPU (two contexts of one
+//    device) race on it and must be serialised by the caller;
 //  * nothing here calls cudaMalloc, cudaFree or an allocating library
 //    routine; the cumulative sum over rays uses a kernel of this file instead
 //    of a library scan with temporary storage.
@@ -29,6 +34,7 @@
 
 #include "../../include/jurassic_gb300.h"
 #include "jgb_common.cuh"
+#include "jgb_ctx.h"
 #include "jgb_internal.h"
 
 namespace jgb {
@@ -97,6 +103,19 @@ __global__ void k_noalloc_scan(int n, const int* count, long long* off) {
 }
 
 }  // namespace
+
+int noalloc_prepare(int device) {
+  unsigned char* p = nullptr;
+  const int rc = scratch_address(device, &p);
+  if (rc != JGB_OK) return rc;
+  cudaFuncAttributes a;
+  const void* fns[] = {(const void*)k_noalloc_ray_obs, (const void*)k_noalloc_mask,
+                       (const void*)k_noalloc_scan};
+  for (const void* f : fns)
+    if (cudaFuncGetAttributes(&a, f) != cudaSuccess) return JGB_ERR_CUDA;
+  return preload_fp64_kernels();
+}
+
 }  // namespace jgb
 
 using namespace jgb;
@@ -176,6 +195,8 @@ extern "C" int jgb_formod_batch_dev_noalloc(jgb_ctx* x, const jgb_batch* db) {
   L.nw = c.nw;
   L.cga = c.formod == 0;
 
+  x->stats = jgb_stats{};
+  cudaEventRecord(x->ev[0], s);
   // the error word must start at zero; everything else is written before read
   if (cudaMemsetAsync(d_err, 0, sizeof(unsigned), s) != cudaSuccess)
     return ctx_fail(x, JGB_ERR_CUDA, "cudaMemsetAsync failed");
@@ -227,7 +248,14 @@ extern "C" int jgb_formod_batch_dev_noalloc(jgb_ctx* x, const jgb_batch* db) {
   launch_trace_fill(c, v.ch, b, L, d_err, s);
   double* refl = need_refl ? reinterpret_cast<double*>(base + o_refl) : nullptr;
   launch_path_fp64(c, v.T, v.ch, b, L, refl, s);
+  cudaEventRecord(x->ev[1], s);
   if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
     return ctx_fail(x, JGB_ERR_CUDA, "forward-model kernels failed");
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, x->ev[0], x->ev[1]);
+  x->stats.total_ms = ms;
+  x->stats.los_points = total;
+  x->stats.trace_passes = 2;
+  x->stats.path_launches = 6 + (c.hydz >= 0 ? 1 : 0);  // kernels of this call
   return JGB_OK;
 }
