@@ -336,6 +336,24 @@ int jgb_engine_get_stats(const jgb_engine *e, jgb_engine_stats *out);
 
 int jgb_get_stats(const jgb_ctx *ctx, jgb_stats *out);
 
+/* State vector of one atmosphere of np levels in the order of the
+   context's RET* windows (atm2x, jurassic.c:29-83: p, T, q per emitter, k
+   per window on the levels inside each window, then the retrieved cloud and
+   surface scalars), and back (x2atm, jurassic.c:5896-5946).  Arrays have
+   the layouts of jgb_batch for one observation (q[ng][np], k[nw][np],
+   scal[5+ncl+nsf]); an array whose elements are not retrieved may be NULL.
+   jgb_atm2x sets *n (and writes x[n] when x is not NULL). */
+int jgb_atm2x(jgb_ctx *ctx, int np, const double *z, const double *p, const double *t,
+              const double *q, const double *k, const double *scal, double *x, int *n);
+int jgb_x2atm(jgb_ctx *ctx, int np, const double *z, const double *x, double *p, double *t,
+              double *q, double *k, double *scal);
+
+/* Shape function file (read_shape, jurassic.c:4907-4945): filter functions
+   "<tblbase>_<nu %.4f>.filt" and the field of view.  Lines of two numbers
+   x y are read, other lines skipped; more than nmax points is JGB_ERR_ARG,
+   a missing file or fewer than two points JGB_ERR_IO.  Host only. */
+int jgb_read_shape(const char *path, int nmax, double *x, double *y, int *n);
+
 /* Allocation-free FP64 forward model of a device-resident batch.  This entry
    point has no counterpart in the reference.  It is for callers that cannot
    allocate GPU memory while they run (a fixed memory budget handed over at

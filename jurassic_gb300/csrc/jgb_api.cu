@@ -1788,6 +1788,74 @@ int jgb_get_stats(const jgb_ctx* x, jgb_stats* out) {
   return JGB_OK;
 }
 
+// The slot of one state element in the caller's arrays (atm2x / x2atm
+// order, jurassic.c:29-83 and 5896-5946): p, t, q[ig][ip], k[iw][ip], or
+// the scalar block clz cldz clk[] sfz sfp sft sfeps[].
+static double* state_slot(const jgb::Elem& e, int np, double* p, double* t, double* q, double* k,
+                          double* scal) {
+  switch (e.arr) {
+    case 0: return p ? p + e.lev : nullptr;
+    case 1: return t ? t + e.lev : nullptr;
+    case 2: return q ? q + (long long)e.idx * np + e.lev : nullptr;
+    case 3: return k ? k + (long long)e.idx * np + e.lev : nullptr;
+    default: return scal ? scal + e.idx : nullptr;
+  }
+}
+
+int jgb_atm2x(jgb_ctx* x, int np, const double* z, const double* p, const double* t,
+              const double* q, const double* k, const double* scal, double* xv, int* n) {
+  jgb::CtxLock lock(x);
+  if (!x || np <= 0 || !z || !n) return JGB_ERR_ARG;
+  std::vector<Elem> lay;
+  state_layout(x, z, np, lay);
+  *n = (int)lay.size();
+  if (!xv) return JGB_OK;
+  for (size_t j = 0; j < lay.size(); j++) {
+    double* s = state_slot(lay[j], np, const_cast<double*>(p), const_cast<double*>(t),
+                           const_cast<double*>(q), const_cast<double*>(k), const_cast<double*>(scal));
+    if (!s) return ctx_fail(x, JGB_ERR_ARG, "state element in an array that was not given");
+    xv[j] = *s;
+  }
+  return JGB_OK;
+}
+
+int jgb_x2atm(jgb_ctx* x, int np, const double* z, const double* xv, double* p, double* t,
+              double* q, double* k, double* scal) {
+  jgb::CtxLock lock(x);
+  if (!x || np <= 0 || !z || !xv) return JGB_ERR_ARG;
+  std::vector<Elem> lay;
+  state_layout(x, z, np, lay);
+  for (size_t j = 0; j < lay.size(); j++) {
+    double* s = state_slot(lay[j], np, p, t, q, k, scal);
+    if (!s) return ctx_fail(x, JGB_ERR_ARG, "state element in an array that was not given");
+    *s = xv[j];
+  }
+  return JGB_OK;
+}
+
+int jgb_read_shape(const char* path, int nmax, double* xs, double* ys, int* n) {
+  if (!path || nmax < 2 || !xs || !ys || !n) return JGB_ERR_ARG;
+  *n = 0;
+  FILE* in = fopen(path, "r");
+  if (!in) return JGB_ERR_IO;
+  // lines of two numbers; other lines (comments, headers) are skipped
+  std::vector<char> line(1 << 16);
+  while (fgets(line.data(), (int)line.size(), in)) {
+    double a, b;
+    if (sscanf(line.data(), "%lg %lg", &a, &b) == 2) {
+      if (*n >= nmax) {
+        fclose(in);
+        return JGB_ERR_ARG;
+      }
+      xs[*n] = a;
+      ys[*n] = b;
+      (*n)++;
+    }
+  }
+  fclose(in);
+  return *n < 2 ? JGB_ERR_IO : JGB_OK;
+}
+
 void* jgb_host_alloc(unsigned long long bytes) {
   void* p = nullptr;
   if (cudaHostAlloc(&p, bytes, cudaHostAllocDefault) != cudaSuccess) return nullptr;

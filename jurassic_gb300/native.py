@@ -150,6 +150,9 @@ SIGNATURES = {
     "jgb_engine_result": (C.c_int, [C.c_void_p, C.c_ulonglong, C.POINTER(_RetOut)]),
     "jgb_engine_get_stats": (C.c_int, [C.c_void_p, C.POINTER(EngineStats)]),
     "jgb_formod_batch_dev_noalloc": (C.c_int, [C.c_void_p, C.POINTER(_Batch)]),
+    "jgb_atm2x": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip]),
+    "jgb_x2atm": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "jgb_read_shape": (C.c_int, [C.c_char_p, C.c_int, _dp, _dp, _ip]),
     "jgb_host_alloc": (C.c_void_p, [C.c_ulonglong]),
     "jgb_host_free": (None, [C.c_void_p]),
     "jgb_dev_alloc": (C.c_void_p, [C.c_ulonglong]),

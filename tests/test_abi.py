@@ -130,28 +130,148 @@ def test_c_consumer_compiles_links_and_runs(tmp_path, built_lib):
     assert r.returncode == 0 and r.stdout.strip() == "ok", (r.returncode, r.stdout, r.stderr)
 
 
-def test_integration_binding_compiles_against_reference_header(tmp_path):
-    """The binding shown in INTEGRATION.md (jur_unified_init and
-    jur_unified_formod_multiple_packages on top of this library, the seam of
-    formod.c:60-76) compiles against the reference's own jurassic.h (its
-    ctl_t, atm_t, obs_t and dimensions) and this header, warnings as errors.
-    Skipped where the reference tree is absent."""
-    import shutil
-    import subprocess
+BINDING = os.path.join(ROOT, "jurassic_gb300", "binding", "jurassic_unified_library.c")
+REFABI = os.path.join(ROOT, "tests", "refabi")
+DIMS = ["-DND=16", "-DNG=4", "-DNW=2", "-DNP=128", "-DNR=16", "-DNCL=8", "-DNSF=8", "-DLEN=4096"]
+
+
+def _reference_src():
     from oracle import refimpl
-    cc = shutil.which("gcc") or shutil.which("cc")
-    src_dir = os.path.join(refimpl.source_dir() or "", "src")
-    if cc is None or not os.path.isfile(os.path.join(src_dir, "jurassic.h")):
+    d = os.path.join(refimpl.source_dir() or "", "src")
+    return d if os.path.isfile(os.path.join(d, "jurassic.h")) else None
+
+
+def _cc():
+    import shutil
+    return shutil.which("gcc") or shutil.which("cc")
+
+
+def test_binding_compiles_against_reference_header(tmp_path):
+    """The reference-side binding (jur_unified_init,
+    jur_unified_formod_multiple_packages, the kernel() and
+    optimal_estimation drop-ins; the seam of formod.c:26-27, 60-76) compiles
+    against the reference's own jurassic.h (its ctl_t, atm_t, obs_t,
+    dimensions and GSL types) and this library's header, warnings as errors,
+    with the reference's default dimensions and with small ones.  Skipped
+    where the reference tree is absent."""
+    import subprocess
+    src_dir, cc = _reference_src(), _cc()
+    if cc is None or src_dir is None:
         pytest.skip("reference tree or C compiler not available")
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    start = text.index("/* jurassic_unified_library.c")
-    code = text[start:text.index("```", start)]
-    src = tmp_path / "jurassic_unified_library.c"
-    src.write_text(code)
-    r = subprocess.run([cc, "-std=gnu99", "-Wall", "-Wextra", "-Werror", "-fopenmp",
-                        "-isystem", src_dir, "-isystem", os.path.join(ROOT, "oracle", "gsl_shim"),
-                        "-I", os.path.join(ROOT, "include"), "-c", str(src),
-                        "-o", str(tmp_path / "binding.o")], capture_output=True, text=True)
+    for dims in ([], DIMS):
+        r = subprocess.run([cc, "-std=gnu99", "-Wall", "-Wextra", "-Werror", "-fopenmp"] + dims +
+                           ["-isystem", src_dir, "-isystem", os.path.join(ROOT, "oracle", "gsl_shim"),
+                            "-I", os.path.join(ROOT, "include"), "-c", BINDING,
+                            "-o", str(tmp_path / "binding.o")], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+
+
+RET_PATCH = r"""
+/* the reference's retrieval driver with the optimal_estimation drop-in: its
+   own ret_t filled into a jgb_ret by the binding's macro */
+#define main jref_retrieval_main_unused
+#include "retrieval.c"
+#undef main
+#include "jurassic_unified_library.h"
+void retrieve_on_gpu(ret_t *ret, obs_t *obs_meas, obs_t *obs_i, atm_t *atm_apr, atm_t *atm_i,
+                     gsl_matrix *cov) {
+  jgb_ret r;
+  JUR_UNIFIED_RET_FROM(ret, &r);
+  jur_unified_optimal_estimation(&r, obs_meas, obs_i, atm_apr, atm_i, cov);
+}
+"""
+
+
+def test_ret_conversion_compiles_inside_reference_retrieval(tmp_path):
+    """JUR_UNIFIED_RET_FROM expands against the reference's own ret_t (it is
+    private to retrieval.c, so the test compiles retrieval.c with a function
+    that uses the macro appended), warnings in the added code as errors."""
+    import subprocess
+    src_dir, cc = _reference_src(), _cc()
+    if cc is None or src_dir is None:
+        pytest.skip("reference tree or C compiler not available")
+    src = tmp_path / "ret_patch.c"
+    src.write_text(RET_PATCH)
+    r = subprocess.run([cc, "-std=gnu99", "-fopenmp", "-Werror=incompatible-pointer-types",
+                        "-Werror=int-conversion", "-Werror=implicit-function-declaration",
+                        "-isystem", src_dir, "-I", src_dir,
+                        "-isystem", os.path.join(ROOT, "oracle", "gsl_shim"),
+                        "-I", os.path.join(ROOT, "include"),
+                        "-I", os.path.join(ROOT, "jurassic_gb300", "binding"), "-c", str(src),
+                        "-o", str(tmp_path / "ret_patch.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+LAYOUT_PROBE = r"""
+#include <stddef.h>
+#include <stdio.h>
+#include "jurassic.h"
+#define F(T, m) printf("%s.%s %zu %zu\n", #T, #m, offsetof(T, m), sizeof(((T *)0)->m))
+int main(void) {
+  printf("atm_t %zu\nobs_t %zu\nctl_t %zu\n", sizeof(atm_t), sizeof(obs_t), sizeof(ctl_t));
+  F(atm_t, np); F(atm_t, time); F(atm_t, z); F(atm_t, lon); F(atm_t, lat); F(atm_t, p);
+  F(atm_t, t); F(atm_t, q); F(atm_t, k); F(atm_t, clz); F(atm_t, cldz); F(atm_t, clk);
+  F(atm_t, sfz); F(atm_t, sfp); F(atm_t, sft); F(atm_t, sfeps);
+  F(obs_t, nr); F(obs_t, time); F(obs_t, obsz); F(obs_t, obslon); F(obs_t, obslat);
+  F(obs_t, vpz); F(obs_t, vplon); F(obs_t, vplat); F(obs_t, tpz); F(obs_t, tplon);
+  F(obs_t, tplat); F(obs_t, tau); F(obs_t, rad);
+  F(ctl_t, ng); F(ctl_t, emitter); F(ctl_t, nd); F(ctl_t, nu); F(ctl_t, nw); F(ctl_t, window);
+  F(ctl_t, ncl); F(ctl_t, clnu); F(ctl_t, nsf); F(ctl_t, sfnu); F(ctl_t, sftype);
+  F(ctl_t, sfsza); F(ctl_t, tblbase); F(ctl_t, tblfmt); F(ctl_t, hydz); F(ctl_t, ctm_co2);
+  F(ctl_t, ctm_h2o); F(ctl_t, ctm_n2); F(ctl_t, ctm_o2); F(ctl_t, refrac); F(ctl_t, rayds);
+  F(ctl_t, raydz); F(ctl_t, fov); F(ctl_t, retp_zmin); F(ctl_t, retp_zmax);
+  F(ctl_t, rett_zmin); F(ctl_t, rett_zmax); F(ctl_t, retq_zmin); F(ctl_t, retq_zmax);
+  F(ctl_t, retk_zmin); F(ctl_t, retk_zmax); F(ctl_t, ret_clz); F(ctl_t, ret_cldz);
+  F(ctl_t, ret_clk); F(ctl_t, ret_sfz); F(ctl_t, ret_sfp); F(ctl_t, ret_sft);
+  F(ctl_t, ret_sfeps); F(ctl_t, write_bbt); F(ctl_t, write_matrix); F(ctl_t, formod);
+  return 0;
+}
+"""
+
+
+def test_restated_struct_layouts_match_reference(tmp_path):
+    """tests/refabi/jurassic.h (used to run the binding where the reference
+    tree is absent) gives ctl_t, atm_t and obs_t the same size and member
+    offsets as the reference's jurassic.h, for the dimensions the GPU test
+    uses and for the reference's defaults.  Skipped where the reference tree
+    is absent."""
+    import subprocess
+    src_dir, cc = _reference_src(), _cc()
+    if cc is None or src_dir is None:
+        pytest.skip("reference tree or C compiler not available")
+    probe = tmp_path / "probe.c"
+    probe.write_text(LAYOUT_PROBE)
+    for dims in ([], DIMS):
+        outs = []
+        for inc in (src_dir, REFABI):
+            exe = tmp_path / "probe"
+            r = subprocess.run([cc, "-std=gnu99", "-w", "-fopenmp"] + dims +
+                               ["-I", inc, "-isystem", os.path.join(ROOT, "oracle", "gsl_shim"),
+                                str(probe), "-o", str(exe), "-lm"], capture_output=True, text=True)
+            assert r.returncode == 0, r.stderr
+            outs.append(subprocess.run([str(exe)], capture_output=True, text=True).stdout)
+        assert outs[0] == outs[1] and len(outs[0].splitlines()) > 60, (dims, outs)
+
+
+def test_binding_and_driver_build_with_restated_header(tmp_path, built_lib):
+    """The binding and the GPU test's driver compile against the restated
+    header and link with the library (the GPU test builds them the same way
+    on the GPU machine)."""
+    import subprocess
+    cc = _cc()
+    if cc is None:
+        pytest.skip("no C compiler")
+    fill = tmp_path / "fill.c"
+    fill.write_text('#include "jurassic.h"\nvoid drv_fill_ctl(ctl_t *c) { c->ng = 0; }\n')
+    libdir = os.path.join(ROOT, "jurassic_gb300")
+    r = subprocess.run([cc, "-std=gnu99", "-fPIC", "-shared", "-Wall", "-Wextra", "-Werror"] + DIMS +
+                       ["-I", REFABI, "-isystem", os.path.join(ROOT, "oracle", "gsl_shim"),
+                        "-I", os.path.join(ROOT, "include"),
+                        "-I", os.path.join(ROOT, "jurassic_gb300", "binding"),
+                        os.path.join(REFABI, "driver.c"), BINDING, str(fill),
+                        "-o", str(tmp_path / "lib.so"), "-L", libdir, "-ljurassic_gb300",
+                        "-Wl,--no-undefined", "-lm", "-Wl,-rpath," + libdir,
+                        "-L/usr/local/cuda/lib64", "-lcudart"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
 
 
