@@ -13,10 +13,18 @@ Reported line (one JSON object, rank 0):
                host->device and device->host copies inside the timed region
   fp64         the plain FP64 GPU form (rounding-level agreement with the
                reference) on the same batch
-  roofline     path kernel: byte model / CUDA-event time vs measured HBM peak
-  cpu_baseline the CPU oracle (restatement of the reference) on a bounded
-               sample of the same workload with all host threads
+  roofline     path kernel: warp-instruction issue rate against the SMs'
+               issue peak at the sampled clock (the bound ncu shows), with
+               the compulsory-byte HBM fraction beside it
+  cpu_baseline the CPU oracle (restatement of the reference) on a bounded,
+               stratified sample of the same workload with all host threads
   accuracy     |BT_mixed - BT_oracle| and FP64 relative error on that sample
+  limb_cga     the uneven limb CGA batch (2e4 observations, 32 channels,
+               3 emitters, 50-400 LOS points per ray): mixed and FP64
+               radiances/s, accuracy against the oracle
+  jacobian     the batched FD Jacobian (2048 nadir profiles x 405 state
+               elements, 150 channels) and its 3xTF32 normal equations
+  serving      retrieval stream: retrievals/s, p50/p99 latency, mixed/FP64
 
 --impl reference times the reference's CPU implementation instead (the
 reference build when present, else the CPU restatement) on a bounded sample.
@@ -132,24 +140,76 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def l2_read_gbs(L):
-    """L2 read bandwidth measured here: 40 sweeps over a 48 MB device buffer
-    (inside the 129 MB L2) in one launch, loads that skip L1, best of 5."""
+# ncu counters of k_path_mixed per LOS point of the nadir workload (all 100
+# channels, 5 emitters), from one capture of the 4000-observation launch
+# with the same channels, emitters and tables (the nadir observations are
+# alike, so the counters scale with the LOS points):
+#   ncu --set full --clock-control none -k regex:k_path_mixed -s 7 -c 1 -o path \
+#       python bench.py --nobs 4000 --steps 2 --warmup 1 --fp64-steps 0 --no-cpu \
+#       --serve-requests 0 --no-extra
+#   smsp__inst_executed.sum 3.6857e10, dram__bytes_read.sum + write.sum 359.8 MB,
+#   4,004,179 LOS points in the launch.
+PATH_NCU_NADIR = {"warp_inst_per_los_point": 36856860952 / 4004179,
+                  "dram_bytes_per_los_point": 359.773440e6 / 4004179}
+
+
+def sm_count(device=0):
+    """Multiprocessors of the device (CUDA runtime attribute 16)."""
     import ctypes
-    g = ctypes.c_double(0.0)
-    if L.jgb_measure_l2_read(48 << 20, 40, ctypes.byref(g)) != 0:
+    rt = ctypes.CDLL("libcudart.so.13")
+    v = ctypes.c_int(0)
+    if rt.cudaDeviceGetAttribute(ctypes.byref(v), 16, device) != 0:
         return None
-    return g.value
+    return v.value
 
 
-def path_bytes_model(ctl, tables, los_points):
-    """Algorithmic bytes of the path kernel: per (LOS point, channel) 8
-    lookups per emitter (EGA; 4 for CGA), each ceil(log2 nu)+4 float probes,
-    plus two FP64 source-function entries."""
-    tu = tables.u.shape[-1]
-    lookups = 8 if ctl.formod == 1 else 4
-    per = ctl.ng * lookups * (int(np.ceil(np.log2(tu))) + 4) * 4 + 16
-    return float(los_points) * ctl.nd * per
+def path_fields(ctl):
+    """Float fields per LOS point of the path kernel's tile planes: p, t, ds,
+    q_H2O, cloud factor, extinction per window, column per emitter (EGA) or
+    CG pressure, temperature and column per emitter (CGA, plus the column),
+    and the per-point p-T bracket (+ pressure weight in CGA) per emitter."""
+    ng, nw = ctl.ng, ctl.nw
+    return 5 + nw + ng + (3 * ng if ctl.formod == 0 else 0) + (2 * ng if ctl.formod == 0 else ng)
+
+
+def compulsory_bytes(ctl, tables, los_points, nray):
+    """Bytes the path kernel cannot avoid moving: its LOS inputs once (FP32
+    fields per point), every table entry once ({u, eps} float pairs and the
+    row records), the source-function table, and the FP64 radiance and
+    transmittance of every ray-channel."""
+    tp, tt, tu = tables.u.shape[2:]
+    rows = ctl.nd * ctl.ng * tp * tt
+    rec = 32 if ctl.formod == 1 else 16
+    return (float(los_points) * path_fields(ctl) * 4 + rows * (tu * 8 + rec)
+            + ctl.nd * 1200 * 4 + float(nray) * ctl.nd * 16)
+
+
+def issue_roofline(los_points, path_ms, sm_mhz, sms, ctl, tables, nray, hbm, hbm_kind):
+    """Binding roofline of k_path_mixed: warp instructions issued per second
+    (ncu instructions per LOS point x the launch's LOS points / CUDA-event
+    time) against the issue peak of the SMs (4 schedulers x SMs x the SM
+    clock sampled during the timed region); the compulsory-byte HBM
+    fraction beside it."""
+    inst = PATH_NCU_NADIR["warp_inst_per_los_point"] * los_points
+    t = path_ms / 1e3
+    achieved = inst / t / 1e9
+    peak = 4.0 * sms * sm_mhz * 1e6 / 1e9 if sm_mhz and sms else None
+    comp = compulsory_bytes(ctl, tables, los_points, nray)
+    return {"bound": "issue", "kernel": "k_path_mixed", "achieved": achieved,
+            "peak": peak, "unit": "G warp-instructions/s",
+            "frac": achieved / peak if peak else None,
+            "traffic": PATH_NCU_NADIR["dram_bytes_per_los_point"] * los_points,
+            "traffic_note": "ncu dram__bytes_read+write per LOS point (4000-observation capture) "
+                            "x LOS points of this launch",
+            "warp_instructions_per_launch": inst,
+            "peak_note": "4 warp schedulers x %d SMs x %.0f MHz (median SM clock sampled in "
+                         "the timed region)" % (sms or 0, sm_mhz or 0),
+            "hbm": {"bound": "hbm", "achieved": comp / t / 1e9, "peak": hbm, "unit": "GB/s",
+                    "frac": comp / t / 1e9 / hbm, "peak_kind": hbm_kind,
+                    "bytes_per_launch": comp,
+                    "bytes_note": "compulsory: LOS inputs once (%d FP32 fields per point), every "
+                                  "table entry and row record once, source function, FP64 "
+                                  "rad+tau per ray-channel" % path_fields(ctl)}}
 
 
 def build_workload(args):
@@ -161,23 +221,51 @@ def build_workload(args):
     raise SystemExit("unknown workload " + args.workload)
 
 
-def cpu_sample(w, nsample):
-    b = w.batch
-    items = [b.item(w.ctl, i) for i in range(nsample)]
+SAMPLE_SEED = 11
+
+
+def stratified_indices(nobs, n, seed=SAMPLE_SEED):
+    """One observation drawn uniformly from each of n equal strata of the
+    batch (numpy default_rng(seed)), ascending."""
+    n = max(1, min(n, nobs))
+    rng = np.random.default_rng(seed)
+    edges = (np.arange(n + 1, dtype=np.int64) * nobs) // n
+    return edges[:-1] + (rng.random(n) * (edges[1:] - edges[:-1])).astype(np.int64)
+
+
+def sample_batch(w, idx):
     from jurassic_gb300 import synth
-    return synth.pack(w.ctl, items)
+    b = w.batch
+    return synth.pack(w.ctl, [b.item(w.ctl, int(i)) for i in idx])
 
 
-def time_cpu(w, ora, target_s, threads):
-    """Time the oracle on a growing sample until ~target_s of work."""
-    n = 8
+def sample_rays(b, idx):
+    """Ray indices of the sampled observations, in sample order."""
+    return np.concatenate([np.arange(b.ray_off[i], b.ray_off[i + 1]) for i in idx])
+
+
+def sample_record(idx, nobs):
+    import hashlib
+    idx = np.asarray(idx, dtype=np.int64)
+    return {"rule": "stratified: one observation uniform in each of %d equal strata of the "
+                    "%d observations, numpy default_rng(%d)" % (len(idx), nobs, SAMPLE_SEED),
+            "observations": int(len(idx)), "indices_head": idx[:12].tolist(),
+            "indices_tail": idx[-4:].tolist(),
+            "indices_sha256": hashlib.sha256(idx.tobytes()).hexdigest()[:16]}
+
+
+def time_cpu(w, ora, target_s, threads, n0=8):
+    """Time the oracle on a growing stratified sample until ~target_s of work.
+    Returns (indices, sample batch, oracle output, seconds)."""
+    n = n0
     while True:
-        s = cpu_sample(w, n)
+        idx = stratified_indices(w.batch.nobs, n)
+        s = sample_batch(w, idx)
         t0 = time.perf_counter()
         out = ora.formod_batch(s.fresh_outputs(), nthreads=threads)
         dt = time.perf_counter() - t0
         if dt >= target_s or n >= w.batch.nobs:
-            return s, out, dt
+            return idx, s, out, dt
         n = min(w.batch.nobs, max(n * 2, int(n * target_s / max(dt, 1e-3) * 1.05)))
 
 
@@ -192,11 +280,11 @@ def run_reference(args, rank):
     per_step = []
     sample_n = None
     for step in range(args.warmup + args.steps):
-        s, out, dt = time_cpu(w, ora, args.cpu_seconds / max(args.steps, 1), threads)
+        idx, s, out, dt = time_cpu(w, ora, args.cpu_seconds / max(args.steps, 1), threads)
         sample_n = s.nobs
         if step >= args.warmup:
             per_step.append(dt)
-    units = sample_n * w.ctl.nd
+    units = s.nray * w.ctl.nd
     value = units / statistics.mean(per_step)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup,
@@ -204,66 +292,89 @@ def run_reference(args, rank):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": w.name, "sample_observations": sample_n},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
-                             "sample": "%d of %d observations x %d channels per step" % (
-                                 sample_n, w.batch.nobs, w.ctl.nd)},
+                             "sample": "%d of %d observations (stratified over the batch) x %d "
+                                       "channels per step" % (sample_n, w.batch.nobs, w.ctl.nd)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def run_jacobian(args, rank, world, local, pg):
+def jacobian_measure(local, nobs, steps, warmup, fp64_nobs, pg=None, world=1):
     """Batched FD Jacobian + normal equations (kernel(), jurassic.c:4004-4099,
-    and K^T Se^-1 K, retrieval.c:403-444): nadir profiles, 81 levels on
-    0-80 km, 150 channels on 650-2400 cm^-1, CO2 + H2O + O3 + CH4, state =
-    T and the four gases on all levels (n = 405), Se diagonal from a 0.2 K
-    noise-equivalent brightness temperature at 250 K."""
-    import copy
+    and K^T Se^-1 K, retrieval.c:403-444) of the Jacobian workload, Se
+    diagonal from a 0.2 K noise-equivalent brightness temperature at 250 K.
+    The mixed form runs on all nobs profiles through jgb_kernel_batch (host
+    buffers, copies inside the timed call); the FP64 form, which is ~20x
+    slower, on the first fp64_nobs profiles, with the mixed form timed on the
+    same profiles for the ratio and the mixed-vs-FP64 Jacobian error."""
     import ctypes as C
-    from jurassic_gb300 import native, synth
-    nobs = args.nobs if args.nobs != 100000 else 2048
-    w = synth.config_nadir(nobs, seed=4, nd=150, nlev=81, ztop=80.0,
-                           emitters=("CO2", "H2O", "O3", "CH4"))
-    ctl = copy.deepcopy(w.ctl)
-    ctl.rett_zmin, ctl.rett_zmax = 0.0, 80.0
-    ctl.retq_zmin = np.zeros(ctl.ng)
-    ctl.retq_zmax = np.full(ctl.ng, 80.0)
+    from jurassic_gb300 import model, native, synth
+    w = synth.config_jacobian(nobs)
+    ctl = w.ctl
     ctx = native.Context(ctl, w.tables, w.filters, device=local)
     L = native.load()
     m, n = ctx.kernel_sizes(w.batch)
     units = int(np.sum(m.astype(np.int64) * (n + 1)))
     small = synth.pack(ctl, [w.batch.item(ctl, i) for i in range(min(8, nobs))])
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         ctx.kernel_batch(small, native.MIXED)
     barrier(pg)
     ms = []
     with ClockSampler(local) as clk:
-        for _ in range(args.steps):
+        for _ in range(steps):
             t0 = time.perf_counter()
             Ks, _ = ctx.kernel_batch(w.batch, native.MIXED)
             ms.append(1e3 * (time.perf_counter() - t0))
     barrier(pg)
     ms_step = allmax(pg, statistics.mean(ms))
     value = units * world / (ms_step / 1e3)
+    stats = ctx.stats()
+    # FP64 against mixed on a subset of the profiles
+    fp64 = None
+    if fp64_nobs > 0:
+        k = min(fp64_nobs, nobs)
+        sub = synth.pack(ctl, [w.batch.item(ctl, i) for i in range(k)])
+        sunits = int(np.sum(m[:k].astype(np.int64) * (n[:k] + 1)))
+        ctx.kernel_batch(small, native.FP64)
+        t0 = time.perf_counter()
+        K64, fm64 = ctx.kernel_batch(sub, native.FP64)
+        t64 = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        K32, _ = ctx.kernel_batch(sub, native.MIXED)
+        t32 = time.perf_counter() - t0
+        # error of the finite-difference radiance changes K_ij h_j relative
+        # to the radiance y_i (columns of upper levels are rounding noise
+        # relative to their own size in any finite difference)
+        fd = 0.0
+        for i in range(k):
+            atm, _ = sub.item(ctl, i)
+            x, kind = model.atm2x(ctl, atm)
+            h = model.fd_steps(ctl, x, kind)
+            y = model.obs2y(fm64.rad[:, sub.ray_off[i]:sub.ray_off[i + 1]])
+            fd = max(fd, float(np.max(np.abs(K32[i] - K64[i]) * h[None, :] / np.abs(y)[:, None])))
+        fp64 = {"profiles": k, "value": sunits / t64, "unit": UNIT,
+                "mixed_same_profiles": sunits / t32,
+                "speedup_mixed_over_fp64": t64 / t32,
+                "mixed_vs_fp64_max_fd_radiance_change_rel": fd}
     # normal equations on the device
     nu = np.asarray(ctl.nu)
     x = 1.43877506 * nu / 250.0
     dbdt = 1.19104259e-8 * nu ** 3 * x * np.exp(x) / (250.0 * np.expm1(x) ** 2)
     sig = 0.2 * dbdt
     rng = np.random.default_rng(5)
-    Kc = np.ascontiguousarray(np.concatenate([k.ravel() for k in Ks]))
+    Kc = np.ascontiguousarray(np.concatenate([k_.ravel() for k_ in Ks]))
     wv = np.concatenate([1.0 / sig[:mi] for mi in m])
     dy = rng.standard_normal(wv.size) / wv
     nA, nb = int(np.sum(n.astype(np.int64) ** 2)), int(np.sum(n))
     dev = {}
-    for k, a in (("K", Kc), ("w", wv), ("dy", dy)):
-        dev[k] = L.jgb_dev_alloc(a.nbytes)
-        L.jgb_memcpy_h2d(dev[k], a.ctypes.data, a.nbytes)
+    for key, a in (("K", Kc), ("w", wv), ("dy", dy)):
+        dev[key] = L.jgb_dev_alloc(a.nbytes)
+        L.jgb_memcpy_h2d(dev[key], a.ctypes.data, a.nbytes)
     dev["A"] = L.jgb_dev_alloc(8 * nA)
     dev["b"] = L.jgb_dev_alloc(8 * nb)
     mi = np.ascontiguousarray(m, np.int32)
     ni = np.ascontiguousarray(n, np.int32)
     flops = float(np.sum(2.0 * m * (n + 1.0) ** 2))
-    ne = {}
-    A = {}
+    ne, A = {}, {}
     for name, prec in (("mixed_3xtf32", native.MIXED), ("fp64", native.FP64)):
         kms = C.c_float(0)
         ctx._check(L.jgb_normal_equations_dev(ctx.h, nobs, mi.ctypes.data_as(C.POINTER(C.c_int)),
@@ -274,8 +385,8 @@ def run_jacobian(args, rank, world, local, pg):
         L.jgb_memcpy_d2h(a.ctypes.data, dev["A"], a.nbytes)
         A[name] = a
         ne[name] = {"kernel_ms": kms.value, "tflops": flops / (kms.value / 1e3) / 1e12}
-    for p in dev.values():
-        L.jgb_dev_free(p)
+    for ptr in dev.values():
+        L.jgb_dev_free(ptr)
     rel = float(np.max(np.abs(A["mixed_3xtf32"] - A["fp64"])) / np.max(np.abs(A["fp64"])))
     try:
         bf16 = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"]
@@ -283,27 +394,40 @@ def run_jacobian(args, rank, world, local, pg):
     except (OSError, KeyError, ValueError):
         bf16, kind = 1900.0, "fallback"
     peak = bf16 / 2 / 3     # dense TF32 = half the bf16 rate; 3xTF32 = three products
+    ctx.close()
+    return {"value": value, "unit": UNIT, "ms_per_step": ms_step, "steps": steps,
+            "workload": "fd_jacobian_nadir_%dobs_81lev_150ch_4gas_n405" % nobs,
+            "observations": nobs, "state_elements": int(n[0]), "radiances_per_step": units,
+            "resume_skip": stats.get("resume_skip"),
+            "h2d_bytes_per_step": int(w.batch.nlev * 8 * (6 + ctl.ng + ctl.nw)),
+            "d2h_bytes_per_step": int(8 * Kc.size), "fp64": fp64,
+            "normal_equations": dict(ne, flops=flops, problems=nobs, m=int(m[0]),
+                                     n=int(n[0]), mixed_vs_fp64_max_rel=rel,
+                                     roofline={"bound": "tensor", "peak": peak,
+                                               "unit": "TFLOP/s", "peak_kind": kind,
+                                               "peak_note": "bf16 dense / 2 (TF32) / 3 (3xTF32)",
+                                               "frac": ne["mixed_3xtf32"]["tflops"] / peak}),
+            "clocks": clk.summary()}
+
+
+def run_jacobian(args, rank, world, local, pg):
+    nobs = args.nobs if args.nobs != 100000 else 2048
+    r = jacobian_measure(local, nobs, args.steps, args.warmup, args.c4_fp64_nobs, pg, world)
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32 path loop, f64 perturbation bookkeeping", "data": "synthetic (seeded)",
-                "config": {"workload": "fd_jacobian_nadir_%dobs_81lev_150ch_4gas_n405" % nobs,
-                           "observations": nobs, "state_elements": int(n[0]),
-                           "radiances_per_step": units,
+                "config": {"workload": r["workload"], "observations": nobs,
+                           "state_elements": r["state_elements"],
+                           "radiances_per_step": r["radiances_per_step"],
                            "l2_policy": "inputs larger than L2 (129 MB); no flush"},
-                "e2e": {"value": value, "unit": UNIT,
-                        "h2d_bytes_per_step": int(w.batch.nlev * 8 * (6 + ctl.ng + ctl.nw)),
-                        "d2h_bytes_per_step": int(8 * Kc.size)},
-                "normal_equations": dict(ne, flops=flops, problems=nobs, m=int(m[0]),
-                                         n=int(n[0]), mixed_vs_fp64_max_rel=rel,
-                                         roofline={"bound": "tensor", "peak": peak,
-                                                   "unit": "TFLOP/s", "peak_kind": kind,
-                                                   "peak_note": "bf16 dense / 2 (TF32) / 3 (3xTF32)",
-                                                   "frac": ne["mixed_3xtf32"]["tflops"] / peak}),
-                "clocks": clk.summary()}
+                "e2e": {"value": r["value"], "unit": UNIT,
+                        "h2d_bytes_per_step": r["h2d_bytes_per_step"],
+                        "d2h_bytes_per_step": r["d2h_bytes_per_step"]},
+                "fp64": r["fp64"], "normal_equations": r["normal_equations"],
+                "clocks": r["clocks"]}
         print(json.dumps(line), flush=True)
-    ctx.close()
 
 
 def run_normal(args, rank, world, local, pg):
@@ -375,39 +499,14 @@ def run_normal(args, rank, world, local, pg):
     ctx.close()
 
 
-def serving_workload(seed=5):
-    """Retrieval serving stream: a 300-channel context (650-2400 cm^-1,
-    CO2 + H2O + O3), requests with 50-300 measured channels, 41-101 levels
-    on 0-100 km, nadir (1 ray) and limb (5 rays) alternating; T retrieved on
-    0-60 km and H2O on 0-20 km; diagonal S_a (2 K, 30 %, 3 km vertical
-    correlation length without a horizontal one, so no correlation,
-    retrieval.c:901), up to 10 LM iterations, kernel recomputed every
-    iteration, covariance and averaging-kernel analysis on."""
-    from jurassic_gb300 import synth
-    from jurassic_gb300.model import Ctl, Ret
-    ctl = Ctl(emitter=["CO2", "H2O", "O3"], nu=np.linspace(650.0, 2400.0, 300))
-    ctl.rett_zmin, ctl.rett_zmax = 0.0, 60.0
-    ctl.retq_zmin = np.array([-999.0, 0.0, -999.0])
-    ctl.retq_zmax = np.array([-999.0, 20.0, -999.0])
-    ret = Ret(kernel_recomp=1, conv_itmax=10, conv_dmin=0.1, err_ana=1,
-              err_noise=np.full(ctl.nd, 1e-4), err_formod=np.full(ctl.nd, 0.5),
-              err_temp=2.0, err_temp_cz=3.0, err_temp_ch=-999.0,
-              err_q=np.array([0.0, 30.0, 0.0]), err_q_cz=np.array([-999.0, 3.0, -999.0]),
-              err_q_ch=np.array([-999.0, -999.0, -999.0]))
-    return ctl, ret, synth.make_tables(ctl, seed + 100), synth.make_filters(ctl)
-
-
 def run_serving(args, device):
     """Closed-loop capacity and Poisson-arrival latency of the retrieval
     engine, mixed precision and FP64, on the serving stream."""
-    from jurassic_gb300 import native, serving, synth
-    ctl, ret, tables, filters = serving_workload()
+    from jurassic_gb300 import native, serving
+    ctl, ret, tables, filters = serving.stream_workload()
     ctx = native.Context(ctl, tables, filters, device=device)
     n, m = args.serve_requests, args.serve_fp64_requests
-    rng = np.random.default_rng(55)
-    nch = rng.integers(50, 301, n)
-    reqs = synth.retrieval_requests(ctl, lambda b: ctx.formod_batch(b.fresh_outputs(), native.FP64),
-                                    n, 55, nlev=(41, 101), ztop=100.0, nch=nch, limb_rays=5)
+    reqs = serving.stream_requests(ctl, lambda b: ctx.formod_batch(b.fresh_outputs(), native.FP64), n)
     out = {"workload": "retrieval stream: %d requests, 50-300 of 300 channels, 41-101 levels, "
                        "nadir/limb(5 rays) alternating, CO2+H2O+O3, T+H2O retrieved" % n}
 
@@ -442,6 +541,141 @@ def run_serving(args, device):
     return out
 
 
+class DeviceBatch:
+    """A synthetic batch copied once into device memory (the inputs of the
+    device-resident "value" path) and, on request, into page-locked host
+    buffers (the e2e path)."""
+
+    def __init__(self, L, ctl, b):
+        self.L, self.b = L, b
+        self.fields = {k: np.ascontiguousarray(getattr(b, k), dtype=np.float64)
+                       for k in ("time", "z", "lon", "lat", "p", "t", "q", "k", "scal", "geo")}
+        self.fields["rad"] = np.zeros((ctl.nd, b.nray))
+        self.fields["tau"] = np.zeros((ctl.nd, b.nray))
+        self.fields["tp"] = np.zeros((3, b.nray))
+        self.ints = {"lev_off": np.ascontiguousarray(b.lev_off, np.int32),
+                     "ray_off": np.ascontiguousarray(b.ray_off, np.int32)}
+        self.dptr, self.hb = {}, {}
+        for k, a in self.items():
+            p = L.jgb_dev_alloc(max(a.nbytes, 8))
+            assert p, "device allocation failed"
+            L.jgb_memcpy_h2d(p, a.ctypes.data, a.nbytes)
+            self.dptr[k] = p
+
+    def items(self):
+        return list(self.fields.items()) + list(self.ints.items())
+
+    def step(self, ctx, prec):
+        """One forward model of the device-resident batch (fresh mask)."""
+        f = self.fields["rad"]
+        self.L.jgb_memcpy_h2d(self.dptr["rad"], f.ctypes.data, f.nbytes)
+        ctx.formod_batch_ptrs(self.dptr, self.b.nobs, prec, device=True)
+        return ctx.stats()
+
+    def rad(self):
+        out = np.zeros_like(self.fields["rad"])
+        self.L.jgb_memcpy_d2h(out.ctypes.data, self.dptr["rad"], out.nbytes)
+        return out
+
+    def host(self):
+        import ctypes as C
+        for k, a in self.items():
+            p = self.L.jgb_host_alloc(max(a.nbytes, 8))
+            C.memmove(p, a.ctypes.data, a.nbytes)
+            self.hb[k] = p
+        h2d = sum(self.fields[k].nbytes for k in ("time", "z", "lon", "lat", "p", "t", "q", "k",
+                                                    "scal", "geo", "rad")) + 2 * self.ints["lev_off"].nbytes
+        d2h = sum(self.fields[k].nbytes for k in ("rad", "tau", "tp"))
+        return self.hb, h2d, d2h
+
+    def free(self):
+        for p in self.dptr.values():
+            self.L.jgb_dev_free(p)
+        for p in self.hb.values():
+            self.L.jgb_host_free(p)
+
+
+def accuracy_block(ctl, rad_mixed, rad_fp64, b, idx, ref):
+    """Mixed |dBT| and FP64 relative radiance error against the oracle on
+    the sampled observations (ref = oracle output of the sample batch)."""
+    from jurassic_gb300.model import brightness
+    rays = sample_rays(b, idx)
+    nu = np.asarray(ctl.nu)[:, None]
+    fin = np.isfinite(ref.rad)
+    bt_ref = brightness(ref.rad, nu)
+    dbt = np.abs(brightness(rad_mixed[:, rays], nu) - bt_ref)[fin]
+    rel32 = (np.abs(rad_mixed[:, rays] - ref.rad) / np.abs(ref.rad))[fin]
+    out = {"sample": sample_record(idx, b.nobs), "sample_rays": int(len(rays)),
+           "mixed_max_abs_dBT_mK": 1e3 * float(np.max(dbt)),
+           "mixed_p99_abs_dBT_mK": 1e3 * float(np.percentile(dbt, 99)),
+           "mixed_max_rel_rad": float(np.max(rel32)), "gate_mK": 10.0,
+           "mixed_within_gate": bool(np.max(dbt) <= 0.010)}
+    if rad_fp64 is not None:
+        out["fp64_max_rel_rad"] = float(np.max((np.abs(rad_fp64[:, rays] - ref.rad) /
+                                                np.abs(ref.rad))[fin]))
+    return out
+
+
+def limb_cga_measure(local, nobs, steps, warmup, fp64_steps, cpu_seconds):
+    """The uneven limb CGA batch: nobs single-ray observations with tangent
+    heights uniform on 5-60 km (50-400 LOS points per ray at RAYDZ 0.5 km),
+    32 channels, 3 emitters.  Mixed and FP64 device-resident radiances/s,
+    the LOS point spread, the compulsory-byte HBM fraction of the path
+    kernel and the accuracy of both forms against the oracle on a stratified
+    sample."""
+    from jurassic_gb300 import native, synth
+    from oracle import oracle
+    w = synth.config_limb_cga(nobs)
+    ctl, b = w.ctl, w.batch
+    ctx = native.Context(ctl, w.tables, w.filters, device=local)
+    L = native.load()
+    db = DeviceBatch(L, ctl, b)
+    units = b.nray * ctl.nd
+    for _ in range(warmup):
+        db.step(ctx, native.MIXED)
+    ms, path = [], []
+    for _ in range(steps):
+        st = db.step(ctx, native.MIXED)
+        ms.append(st["total_ms"])
+        path.append(st["path_ms"])
+    rad32 = db.rad()
+    los = st["los_points"]
+    rad64, ms64 = None, []
+    if fp64_steps > 0:
+        db.step(ctx, native.FP64)
+        for _ in range(fp64_steps):
+            ms64.append(db.step(ctx, native.FP64)["total_ms"])
+        rad64 = db.rad()
+    hbm, kind = peaks()
+    comp = compulsory_bytes(ctl, w.tables, los, b.nray)
+    t_path = statistics.mean(path) / 1e3
+    ora = oracle.Oracle(ctl, w.tables, w.filters)
+    idx, sb, ref, dt = time_cpu(w, ora, cpu_seconds, os.cpu_count() or 1, n0=64)
+    # LOS points per ray of the sample, from the oracle's ray tracing
+    pts = [len(ora.raytrace(*sb.item(ctl, i), 0)[0]) for i in range(sb.nobs)]
+    ora.close()
+    out = {"workload": w.name, "observations": nobs, "rays": b.nray, "channels": ctl.nd,
+           "emitters": ctl.ng, "method": "CGA", "raydz_km": ctl.raydz, "los_points": los,
+           "value": units / (statistics.mean(ms) / 1e3), "unit": UNIT,
+           "ms_per_step": statistics.mean(ms), "steps": steps,
+           "stage_ms": {k: st[k] for k in ("trace_ms", "pack_ms", "path_ms")},
+           "fp64": None if not ms64 else {
+               "value": units / (statistics.mean(ms64) / 1e3), "unit": UNIT,
+               "ms_per_step": statistics.mean(ms64),
+               "speedup_mixed_over_fp64": statistics.mean(ms64) / statistics.mean(ms)},
+           "hbm_compulsory": {"achieved": comp / t_path / 1e9, "peak": hbm, "unit": "GB/s",
+                              "frac": comp / t_path / 1e9 / hbm, "peak_kind": kind,
+                              "bytes_per_launch": comp},
+           "cpu_baseline": {"value": sb.nray * ctl.nd / dt, "unit": UNIT,
+                            "cores": os.cpu_count() or 1, "kind": "port"},
+           "accuracy": accuracy_block(ctl, rad32, rad64, b, idx, ref),
+           "los_points_per_ray_sample": {"min": int(min(pts)), "max": int(max(pts)),
+                                         "mean": float(np.mean(pts))}}
+    db.free()
+    ctx.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -454,10 +688,18 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--serve-requests", type=int, default=48)
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the limb CGA and FD Jacobian configurations of the default run")
+    ap.add_argument("--c3-nobs", type=int, default=20000,
+                    help="observations of the limb CGA configuration")
+    ap.add_argument("--c4-nobs", type=int, default=2048,
+                    help="profiles of the FD Jacobian configuration")
+    ap.add_argument("--c4-fp64-nobs", type=int, default=128,
+                    help="profiles of the FD Jacobian timed in FP64 (and mixed) for the ratio")
+    ap.add_argument("--serve-requests", type=int, default=512)
     ap.add_argument("--serve-fp64-requests", type=int, default=48,
-                    help="requests of the stream run through the FP64 engine for the "
-                         "mixed/FP64 retrievals/s ratio (all of them by default)")
+                    help="first requests of the stream also run through the FP64 engine for "
+                         "the mixed/FP64 retrievals/s ratio and the accuracy")
     ap.add_argument("--serve-load", type=float, default=0.7,
                     help="Poisson arrival rate as a fraction of the closed-loop capacity")
     ap.add_argument("--serve-budget-gb", type=float, default=64.0)
@@ -469,7 +711,6 @@ def main():
         return
 
     from jurassic_gb300 import native
-    from jurassic_gb300.model import brightness
     native.load()
     if args.workload in ("jacobian", "normal"):
         (run_jacobian if args.workload == "jacobian" else run_normal)(args, rank, world, local, pg)
@@ -481,55 +722,27 @@ def main():
     ctx = native.Context(ctl, w.tables, w.filters, device=local)
     L = native.load()
     units = b.nray * ctl.nd
-
-    # device-resident copies of the batch inputs (the "value" path)
-    import ctypes as C
-    fields = {k: np.ascontiguousarray(getattr(b, k), dtype=np.float64)
-              for k in ("time", "z", "lon", "lat", "p", "t", "q", "k", "scal", "geo")}
-    fields["rad"] = np.zeros((ctl.nd, b.nray))
-    fields["tau"] = np.zeros((ctl.nd, b.nray))
-    fields["tp"] = np.zeros((3, b.nray))
-    ints = {"lev_off": np.ascontiguousarray(b.lev_off, np.int32),
-            "ray_off": np.ascontiguousarray(b.ray_off, np.int32)}
-    dptr = {}
-    for k, a in list(fields.items()) + list(ints.items()):
-        p = L.jgb_dev_alloc(max(a.nbytes, 8))
-        assert p, "device allocation failed"
-        L.jgb_memcpy_h2d(p, a.ctypes.data, a.nbytes)
-        dptr[k] = p
-
-    def dev_step(prec):
-        L.jgb_memcpy_h2d(dptr["rad"], fields["rad"].ctypes.data, fields["rad"].nbytes)
-        ctx.formod_batch_ptrs(dptr, b.nobs, prec, device=True)
-        return ctx.stats()
+    db = DeviceBatch(L, ctl, b)
 
     # ---- mixed precision, device-resident (value) ----
     for _ in range(args.warmup):
-        dev_step(native.MIXED)
+        db.step(ctx, native.MIXED)
     barrier(pg)
     ms, path_ms, stats = [], [], None
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            stats = dev_step(native.MIXED)
+            stats = db.step(ctx, native.MIXED)
             ms.append(stats["total_ms"])
             path_ms.append(stats["path_ms"])
         wall = time.perf_counter() - t0
     barrier(pg)
     ms_step = allmax(pg, statistics.mean(ms))
     value = units * world / (ms_step / 1e3)
-    rad_mixed = np.zeros((ctl.nd, b.nray))
-    L.jgb_memcpy_d2h(rad_mixed.ctypes.data, dptr["rad"], rad_mixed.nbytes)
+    rad_mixed = db.rad()
 
     # ---- e2e through the public C ABI with page-locked host buffers ----
-    hb = {}
-    for k, a in list(fields.items()) + list(ints.items()):
-        p = L.jgb_host_alloc(max(a.nbytes, 8))
-        C.memmove(p, a.ctypes.data, a.nbytes)
-        hb[k] = p
-    h2d = sum(fields[k].nbytes for k in ("time", "z", "lon", "lat", "p", "t", "q", "k", "scal",
-                                           "geo", "rad")) + 2 * ints["lev_off"].nbytes
-    d2h = fields["rad"].nbytes + fields["tau"].nbytes + fields["tp"].nbytes
+    hb, h2d, d2h = db.host()
     for _ in range(max(1, args.warmup - 1)):
         ctx.formod_batch_ptrs(hb, b.nobs, native.MIXED, device=False)
     e2e_ms, e2e_st = [], []
@@ -543,38 +756,28 @@ def main():
     # ---- plain FP64 GPU form ----
     fp64_ms, fp64_value, rad_fp64 = [], None, None
     if args.fp64_steps > 0:
-        dev_step(native.FP64)
+        db.step(ctx, native.FP64)
         for _ in range(args.fp64_steps):
-            fp64_ms.append(dev_step(native.FP64)["total_ms"])
+            fp64_ms.append(db.step(ctx, native.FP64)["total_ms"])
         fp64_value = units * world / (allmax(pg, statistics.mean(fp64_ms)) / 1e3)
-        rad_fp64 = np.zeros((ctl.nd, b.nray))
-        L.jgb_memcpy_d2h(rad_fp64.ctypes.data, dptr["rad"], rad_fp64.nbytes)
+        rad_fp64 = db.rad()
 
     line = None
     if rank == 0:
         hbm, peak_kind = peaks()
-        l2 = l2_read_gbs(L)
-        bytes_alg = path_bytes_model(ctl, w.tables, stats["los_points"])
-        achieved = bytes_alg / (statistics.mean(path_ms) / 1e3) / 1e9
-        # DRAM bytes per LOS point of k_path_mixed from the committed ncu
-        # summary (captured on a 4000-observation nadir batch with the same
-        # channels and emitters), scaled by the LOS points of this launch
-        traffic_per_launch = None
-        if args.workload == "nadir":
-            try:
-                for ln in open(os.path.join(ROOT, "profiles", "k_path_mixed_nadir4000.md")):
-                    if "dram_bytes_per_los_point:" in ln:
-                        per = float(ln.split("dram_bytes_per_los_point:")[1].split("`")[0])
-                        traffic_per_launch = per * stats["los_points"]
-            except (OSError, ValueError, IndexError):
-                traffic_per_launch = None
+        clocks = clk.summary()
+        roof = issue_roofline(stats["los_points"], statistics.mean(path_ms), clocks["sm_mhz"],
+                              sm_count(local), ctl, w.tables, b.nray, hbm, peak_kind)
+        if args.workload != "nadir":   # the instruction counts are the nadir launch's
+            roof.update(achieved=None, frac=None, traffic=None, warp_instructions_per_launch=None)
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32 path loop (compensated), f64 ray tracing",
                 "data": "synthetic (seeded)",
                 "config": {"workload": w.name, "observations": b.nobs, "rays": b.nray,
-                           "channels": ctl.nd, "emitters": ctl.ng, "levels_per_profile": 101 if args.workload == "nadir" else None,
+                           "channels": ctl.nd, "emitters": ctl.ng,
+                           "levels_per_profile": int(b.lev_off[1] - b.lev_off[0]),
                            "method": "EGA" if ctl.formod == 1 else "CGA",
                            "los_points": stats["los_points"],
                            "l2_policy": "inputs and tables larger than L2 (129 MB); no flush",
@@ -595,44 +798,32 @@ def main():
                     "value": fp64_value, "unit": UNIT, "ms_per_step": statistics.mean(fp64_ms),
                     "speedup_mixed_over_fp64": value / fp64_value},
                 "gpu_launches": int(stats["path_launches"]) * args.steps,
-                "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                             "frac": achieved / hbm, "traffic": traffic_per_launch,
-                             "traffic_note": "ncu dram bytes per LOS point (4000-observation capture) x LOS points; the byte model counts table probes mostly served by L1/L2",
-                             "kernel": "k_path_mixed", "bytes_model": "per (LOS point, channel): ng*8*(ceil(log2 TU)+4)*4 + 16 B",
-                             "bytes_per_launch": bytes_alg, "peak_kind": peak_kind,
-                             "l2": None if l2 is None else {
-                                 "achieved": achieved, "peak": l2, "unit": "GB/s", "frac": achieved / l2,
-                                 "peak_kind": "measured in this run (48 MB L2-resident buffer, 40 sweeps, L1 bypassed)"}},
-                "clocks": clk.summary()}
+                "roofline": roof,
+                "clocks": clocks}
 
-    # ---- CPU baseline + accuracy on a bounded sample ----
+    # ---- CPU baseline + accuracy on a bounded, stratified sample ----
     if rank == 0 and not args.no_cpu:
         from oracle import oracle
         ora = oracle.Oracle(ctl, w.tables, w.filters)
         threads = os.cpu_count() or 1
-        s, ref, dt = time_cpu(w, ora, args.cpu_seconds, threads)
-        n = s.nobs
-        line["cpu_baseline"] = {"value": n * ctl.nd / dt, "unit": UNIT, "cores": threads,
+        idx, s, ref, dt = time_cpu(w, ora, args.cpu_seconds, threads)
+        line["cpu_baseline"] = {"value": s.nray * ctl.nd / dt, "unit": UNIT, "cores": threads,
                                 "kind": "port",
-                                "sample": "first %d of %d observations x %d channels" % (n, b.nobs, ctl.nd)}
-        nu = np.asarray(ctl.nu)[:, None]
-        sl = slice(0, s.nray)
-        bt_ref = brightness(ref.rad, nu)
-        dbt = np.abs(brightness(rad_mixed[:, sl], nu) - bt_ref)
-        rel64 = (np.abs(rad_fp64[:, sl] - ref.rad) / np.abs(ref.rad)) if rad_fp64 is not None else np.array([np.nan])
-        line["accuracy"] = {"sample_rays": int(s.nray), "mixed_max_abs_dBT_mK": 1e3 * float(np.max(dbt)),
-                            "mixed_p99_abs_dBT_mK": 1e3 * float(np.percentile(dbt, 99)),
-                            "mixed_max_rel_rad": float(np.max(np.abs(rad_mixed[:, sl] - ref.rad) / np.abs(ref.rad))),
-                            "fp64_max_rel_rad": float(np.max(rel64))}
+                                "sample": "%d of %d observations, stratified over the batch, x %d "
+                                          "channels" % (s.nobs, b.nobs, ctl.nd)}
+        line["accuracy"] = accuracy_block(ctl, rad_mixed, rad_fp64, b, idx, ref)
+        ora.close()
+    db.free()
+    ctx.close()
+    if rank == 0 and not args.no_extra and args.workload == "nadir":
+        line["limb_cga"] = limb_cga_measure(local, args.c3_nobs, max(3, min(args.steps, 10)),
+                                            3, 1 if args.fp64_steps > 0 else 0,
+                                            0.0 if args.no_cpu else 3.0)
+        line["jacobian"] = jacobian_measure(local, args.c4_nobs, 2, 1, args.c4_fp64_nobs)
     if rank == 0 and args.serve_requests > 0:
         line["serving"] = run_serving(args, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    for p in dptr.values():
-        L.jgb_dev_free(p)
-    for p in hb.values():
-        L.jgb_host_free(p)
-    ctx.close()
     if pg is not None:
         pg.destroy_process_group()
 

@@ -568,6 +568,83 @@ def write_obs(dirname: Optional[str], filename: str, ctl: Ctl, obs: Obs,
             f.write(" ".join(cols) + "\n")
 
 
+def atm2x(ctl: Ctl, atm: Atm):
+    """State vector of an atmosphere (atm2x, src/jurassic.c:29-83): p, T,
+    q per emitter, k per window on the levels inside each RET* window, then
+    the retrieved cloud and surface scalars.  Returns (x, kind) with kind the
+    reference's index codes: 0 p, 1 T, 2+ig q, 2+ng+iw k, then cloud height,
+    depth, extinctions, surface height, pressure, temperature, emissivities."""
+    x, kind = [], []
+    z = np.asarray(atm.z)
+    ng, nw = ctl.ng, ctl.nw
+
+    def window(lo, hi, vals, code):
+        for ip in range(len(z)):
+            if lo <= z[ip] <= hi:
+                x.append(float(vals[ip]))
+                kind.append(code)
+    window(ctl.retp_zmin, ctl.retp_zmax, atm.p, 0)
+    window(ctl.rett_zmin, ctl.rett_zmax, atm.t, 1)
+    q = np.reshape(atm.q, (ng, -1))
+    for ig in range(ng):
+        window(ctl.retq_zmin[ig], ctl.retq_zmax[ig], q[ig], 2 + ig)
+    k = np.reshape(atm.k, (nw, -1)) if nw else np.zeros((0, len(z)))
+    for iw in range(nw):
+        window(ctl.retk_zmin[iw], ctl.retk_zmax[iw], k[iw], 2 + ng + iw)
+    s = atm.scal(ctl)
+    o = 2 + ng + nw
+    flags = [(ctl.ret_clz, [0], o), (ctl.ret_cldz, [1], o + 1),
+             (ctl.ret_clk, list(range(2, 2 + ctl.ncl)), o + 2)]
+    so = 2 + ctl.ncl
+    flags += [(ctl.ret_sfz, [so], o + 2 + ctl.ncl), (ctl.ret_sfp, [so + 1], o + 3 + ctl.ncl),
+              (ctl.ret_sft, [so + 2], o + 4 + ctl.ncl),
+              (ctl.ret_sfeps, list(range(so + 3, so + 3 + ctl.nsf)), o + 5 + ctl.ncl)]
+    for on, idx, code in flags:
+        if on:
+            for j, i in enumerate(idx):
+                x.append(float(s[i]))
+                kind.append(code + (j if len(idx) > 1 else 0))
+    return np.array(x), np.array(kind, dtype=np.int64)
+
+
+def fd_steps(ctl: Ctl, x, kind):
+    """Perturbation step of every state element in kernel()
+    (src/jurassic.c:4046-4068)."""
+    ng, nw, ncl = ctl.ng, ctl.nw, ctl.ncl
+    x = np.asarray(x, dtype=np.float64)
+    h = np.empty_like(x)
+    for j, (v, c) in enumerate(zip(x, kind)):
+        o = 2 + ng + nw
+        if c == 0:
+            h[j] = max(abs(0.01 * v), 1e-7)
+        elif c == 1:
+            h[j] = 1.0
+        elif c < 2 + ng:
+            h[j] = max(abs(0.01 * v), 1e-15)
+        elif c < o:
+            h[j] = 1e-4
+        elif c in (o, o + 1):
+            h[j] = 1.0
+        elif c < o + 2 + ncl:
+            h[j] = 1e-4
+        elif c == o + 2 + ncl:
+            h[j] = 0.1
+        elif c == o + 3 + ncl:
+            h[j] = 10.0
+        elif c == o + 4 + ncl:
+            h[j] = 1.0
+        else:
+            h[j] = 1e-2
+    return h
+
+
+def obs2y(rad):
+    """Measurement vector (obs2y, src/jurassic.c:4174-4197): ray-major,
+    finite radiances only."""
+    rad = np.asarray(rad)
+    return np.array([v for col in rad.T for v in col if np.isfinite(v)])
+
+
 def brightness(rad, nu):
     """Brightness temperature (BRIGHT, src/jurassic.h:126-127)."""
     C1, C2 = 1.19104259e-8, 1.43877506

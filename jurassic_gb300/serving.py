@@ -75,3 +75,33 @@ def serve(engine, ctl, requests: Sequence, rate_hz: float, seed: int = 0,
                                             "finish_ms", "trial_fwd_ms", "trial_trace_ms",
                                             "trial_path_ms")},
                 results=results)
+
+
+def stream_workload(seed=5):
+    """Retrieval serving stream: a 300-channel context (650-2400 cm^-1,
+    CO2 + H2O + O3); T retrieved on 0-60 km and H2O on 0-20 km; diagonal S_a
+    (2 K, 30 %, 3 km vertical correlation length without a horizontal one,
+    so no correlation, retrieval.c:901), up to 10 LM iterations, kernel
+    recomputed every iteration, covariance and averaging-kernel analysis on.
+    Returns (ctl, ret, tables, filters)."""
+    from .model import Ctl, Ret
+    ctl = Ctl(emitter=["CO2", "H2O", "O3"], nu=np.linspace(650.0, 2400.0, 300))
+    ctl.rett_zmin, ctl.rett_zmax = 0.0, 60.0
+    ctl.retq_zmin = np.array([-999.0, 0.0, -999.0])
+    ctl.retq_zmax = np.array([-999.0, 20.0, -999.0])
+    ret = Ret(kernel_recomp=1, conv_itmax=10, conv_dmin=0.1, err_ana=1,
+              err_noise=np.full(ctl.nd, 1e-4), err_formod=np.full(ctl.nd, 0.5),
+              err_temp=2.0, err_temp_cz=3.0, err_temp_ch=-999.0,
+              err_q=np.array([0.0, 30.0, 0.0]), err_q_cz=np.array([-999.0, 3.0, -999.0]),
+              err_q_ch=np.array([-999.0, -999.0, -999.0]))
+    return ctl, ret, synth.make_tables(ctl, seed + 100), synth.make_filters(ctl)
+
+
+def stream_requests(ctl, forward, n, seed=55):
+    """n requests of the serving stream: 50-300 measured channels (seeded),
+    41-101 levels on 0-100 km, nadir (1 ray) and limb (5 rays) alternating;
+    ``forward`` computes the measurements of the truth batch."""
+    rng = np.random.default_rng(seed)
+    nch = rng.integers(50, 301, n)
+    return synth.retrieval_requests(ctl, forward, n, seed, nlev=(41, 101), ztop=100.0, nch=nch,
+                                    limb_rays=5)

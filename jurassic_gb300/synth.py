@@ -313,6 +313,19 @@ def config_nadir(nobs, seed=2, nd=100, nlev=101, ztop=100.0, emitters=("CO2", "H
                     make_tables(ctl, seed + 100), make_filters(ctl), b)
 
 
+def config_jacobian(nobs, seed=4) -> Workload:
+    """FD Jacobian workload: nadir profiles, 81 levels on 0-80 km, 150
+    channels on 650-2400 cm^-1, CO2 + H2O + O3 + CH4, state = T and the four
+    gases on all levels (n = 405 state elements)."""
+    w = config_nadir(nobs, seed=seed, nd=150, nlev=81, ztop=80.0,
+                     emitters=("CO2", "H2O", "O3", "CH4"))
+    w.ctl.rett_zmin, w.ctl.rett_zmax = 0.0, 80.0
+    w.ctl.retq_zmin = np.zeros(w.ctl.ng)
+    w.ctl.retq_zmax = np.full(w.ctl.ng, 80.0)
+    w.name = "fd_jacobian_nadir_%dobs_81lev_150ch_4gas_n405" % nobs
+    return w
+
+
 def config_limb_cga(nobs, seed=3, nd=32, emitters=("CO2", "H2O", "O3"), raydz=0.5,
                     zmin_t=5.0, zmax_t=60.0, nlev=81, ztop=80.0) -> Workload:
     """Batched limb CGA: `nobs` single-ray observations with tangent heights
