@@ -440,7 +440,7 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
       // emitters whose (float) p and T grids are identical for all channels:
       // their brackets are found once per LOS point in the tile packing
       x->grid_mask = 0;
-      if (x->tp <= 1023 && x->tt <= 1023)
+      if ((long long)x->tp * x->tt < 32768)  // rows of a p-T cell packed in 16 bits
         for (int g = 0; g < c.ng; g++) {
           bool same = x->h_np[g] >= 30;
           for (int id = 1; id < c.nd && same; id++) {
@@ -1290,7 +1290,9 @@ int jgb_tables_init(jgb_ctx* x, int tp, int tt, int tu) {
   CK(x->t_pf.reserve(sizeof(float) * std::max<size_t>(ndg * tp, 1)));
   CK(x->t_tf.reserve(sizeof(float) * std::max<size_t>(ndg * tp * tt, 1)));
   CK(x->t_meta.reserve(2 * sizeof(float4) * std::max<size_t>(ndg * tp * tt, 1)));
-  CK(x->t_ue.reserve(sizeof(float2) * std::max<size_t>(ndg * tp * tt * tu, 1)));
+  // one entry of padding after the last row (the row search reads a third
+  // probe that it ignores at a row's end)
+  CK(x->t_ue.reserve(sizeof(float2) * (ndg * tp * tt * tu + 1)));
   x->meta_stale = true;
   CK(cudaMemcpy(x->t_np.p, x->h_np.data(), sizeof(int) * ndg, cudaMemcpyHostToDevice));
   CK(cudaMemset(x->t_nt.p, 0, sizeof(int) * ndg * tp));

@@ -20,13 +20,17 @@
 
 namespace jgb {
 
-// Field indices of a tile plane.  br0..br0+ng-1 hold, for emitters whose
-// p-T grids are shared by all channels, the packed bracket of the point
-// (ipr | it0 << 10 | it1 << 20; kNoBracket: no table, kNoBracket | 2: no
-// temperature rows at that pressure), and in CGA pw0..pw0+ng-1 the
-// (log-)pressure interpolation weight in that bracket.
+// Field indices of a tile plane.  For emitters whose p-T grids are shared by
+// all channels, the channel-independent part of the table interpolation is
+// done once per LOS point here: br0..br0+ng-1 hold the rows of the point's
+// p-T cell within a (channel, emitter) table, ipr * tt + it0 | ((ipr + 1)
+// * tt + it1) << 16 (kNoBracket: no table, kNoBracket | 2: no temperature
+// rows at that pressure; tp * tt < 2^15), pw0..pw0+ng-1 the
+// pressure interpolation weight in that bracket (linear in EGA, log-linear
+// in CGA), and tw0 + 2g, tw0 + 2g + 1 the temperature weights at the lower
+// and upper pressure of the bracket.
 struct Fields {
-  int p, t, ds, qh2o, aux, kw0, u0, cgp0, cgt0, cgu0, br0, pw0, n;
+  int p, t, ds, qh2o, aux, kw0, u0, cgp0, cgt0, cgu0, br0, pw0, tw0, n;
 };
 
 __host__ __device__ inline Fields fields_of(const CtlDev& c, unsigned brmask) {
@@ -43,7 +47,8 @@ __host__ __device__ inline Fields fields_of(const CtlDev& c, unsigned brmask) {
   f.cgu0 = f.cgt0 + c.ng;
   f.br0 = c.formod == 0 ? f.cgu0 + c.ng : f.u0 + c.ng;
   f.pw0 = f.br0 + c.ng;
-  f.n = f.br0 + (brmask ? (c.formod == 0 ? 2 * c.ng : c.ng) : 0);
+  f.tw0 = f.pw0 + c.ng;
+  f.n = f.br0 + (brmask ? 4 * c.ng : 0);
   return f;
 }
 
@@ -129,15 +134,19 @@ __device__ __forceinline__ int bisect2(const float2* g, int lo, int hi, float x)
   return lo;
 }
 
+// The third probe g[h+2] is read even where h + 2 = n (the next row's first
+// entry, or the one-entry pad after the last row) and then ignored.
 template <int C>
 __device__ __forceinline__ Bracket2 hunt2(const float2* g, int n, float x, int h) {
   h = min(max(h, 0), n - 2);
-  const int h2 = min(h + 2, n - 1);
-  const float2 A = __ldg(g + h), B = __ldg(g + h + 1), D = __ldg(g + h2);
+  const float2 A = __ldg(g + h), B = __ldg(g + h + 1), D = __ldg(g + h + 2);
   const float a = comp<C>(A), b = comp<C>(B), c = comp<C>(D);
-  // bracket h or h + 1 (at the right end of the row, x == g[n-1] keeps n-2)
-  if (a <= x && (x < c || h2 == n - 1)) {
-    const bool up = x >= b && h + 1 <= n - 2;
+  // bracket h or h + 1: every x >= a when the probes reach the row's end
+  // (h >= n - 3; x at or above g[n-1] keeps n - 2, and h + 1 <= n - 2 is the
+  // last bracket there), else x < g[h+2]
+  const bool tail = h + 2 >= n - 1;
+  if (a <= x && (x < c || tail)) {
+    const bool up = x >= b && h + 2 < n;
     return up ? Bracket2{h + 1, B, D} : Bracket2{h, A, B};
   }
   const int i = a <= x ? bisect2<C>(g, h + 2, n - 1, x) : bisect2<C>(g, 0, h, x);
@@ -257,10 +266,11 @@ __global__ void k_pack_tiles(CtlDev c, TblDev T, LosDev L, MixedPlan P, long lon
       out[(F.cgt0 + g) * 32] = (float)L.cgt[g * L.cap + q];
       out[(F.cgu0 + g) * 32] = (float)L.cgu[g * L.cap + q];
     }
-  // p-T brackets on the grids of channel 0 (identical for every channel)
+  // p-T brackets and interpolation weights on the grids of channel 0
+  // (identical for every channel)
   for (int g = 0; P.brmask && g < c.ng; g++) {
     unsigned wd = kNoBracket;  // no table (np < 30)
-    float pw = 0.f;
+    float pw = 0.f, wa = 0.f, wb = 0.f;
     const int np = __ldg(T.np + g);
     if (((P.brmask >> g) & 1u) && np >= 30) {
       const float pq = c.formod == 0 ? (float)L.cgp[g * L.cap + q] : (float)L.p[q];
@@ -273,19 +283,24 @@ __global__ void k_pack_tiles(CtlDev c, TblDev T, LosDev L, MixedPlan P, long lon
         const float* t0g = T.tf + ((long long)g * T.tp + ipr) * T.tt;
         const int it0 = bracket_regf(t0g, nt0, tq);
         const int it1 = bracket_regf(t0g + T.tt, nt1, tq);
-        wd = (unsigned)ipr | ((unsigned)it0 << 10) | ((unsigned)it1 << 20);
-        if (c.formod == 0) {  // pressure weight of intpol_tbl_cga (log-linear)
-          const float* pg = T.pf + (long long)g * T.tp;
-          const float pa = pg[ipr], pb = pg[ipr + 1];
-          if (pq / pa > 0.f && pb / pa > 0.f)
-            pw = __logf(pq / pa) / __logf(pb / pa);
-          else
-            pw = (pq - pa) / (pb - pa);
-        }
+        wd = (unsigned)(ipr * T.tt + it0) | ((unsigned)((ipr + 1) * T.tt + it1) << 16);
+        // temperature weights at both pressures (LIN in T of
+        // intpol_tbl_ega / intpol_tbl_cga)
+        wa = (tq - t0g[it0]) / (t0g[it0 + 1] - t0g[it0]);
+        wb = (tq - t0g[T.tt + it1]) / (t0g[T.tt + it1 + 1] - t0g[T.tt + it1]);
+        // pressure weight: linear in EGA, log-linear in CGA
+        const float* pg = T.pf + (long long)g * T.tp;
+        const float pa = pg[ipr], pb = pg[ipr + 1];
+        if (c.formod == 0 && pq / pa > 0.f && pb / pa > 0.f)
+          pw = __logf(pq / pa) / __logf(pb / pa);
+        else
+          pw = (pq - pa) / (pb - pa);
       }
     }
     out[(F.br0 + g) * 32] = __uint_as_float(wd);
-    if (c.formod == 0) out[(F.pw0 + g) * 32] = pw;
+    out[(F.pw0 + g) * 32] = pw;
+    out[(F.tw0 + 2 * g) * 32] = wa;
+    out[(F.tw0 + 2 * g + 1) * 32] = wb;
   }
 }
 
@@ -308,6 +323,7 @@ constexpr int kStateWords = 5;  // t, e, ipr, 2 words of 16-bit corner hints
 constexpr float kTauStop = 1e-12f;  // path transmittance below which the walk stops
 constexpr int kChanConsts = 16;  // constants of a warp's channel
 constexpr int kThreadFloats = 2;  // per-thread values kept in shared memory
+constexpr int kPathThreads = 128;  // threads of a path block: 4 warps = 4 channels
 
 // Per (channel, emitter) state carried along the path: transmittance t and
 // emissivity e of the extended path (each accurate where it is small), the
@@ -322,12 +338,13 @@ struct GasState {
 // jurassic.c:3710-3891).  Returns the segment emissivity; *sat is set where
 // the reference's segment transmittance becomes zero.
 // brw: packed bracket precomputed for the LOS point (grids shared by all
-// channels), or kNoBracket | 1 to search here; wpre: in CGA the pressure
-// weight precomputed with it.
+// channels), or kNoBracket | 1 to search here; wpre, wta, wtb: the pressure
+// and temperature interpolation weights precomputed with it.
 template <bool CGA>
 __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, float pq,
                                            float tq, float du, float ucg, unsigned brw,
-                                           float wpre, GasState& s, bool& sat) {
+                                           float wpre, float wta, float wtb, GasState& s,
+                                           bool& sat) {
   constexpr bool cga = CGA;
   const bool pre = brw != (kNoBracket | 1u);
   if (pre && brw == kNoBracket) return 0.f;   // np < 30
@@ -343,34 +360,28 @@ __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, float 
     sat = true;
     return 1.f;
   }
-  int ipr, it0, it1;
-  float pa, pb;
+  unsigned ra, rc;
+  float pa = 0.f, pb = 0.f;
   if (pre) {
     if (brw & kNoBracket) return 0.f;         // nt < 2 at this pressure
-    ipr = (int)(brw & 1023u);
-    it0 = (int)((brw >> 10) & 1023u);
-    it1 = (int)((brw >> 20) & 1023u);
-    if (cga) {
-      pa = pb = 0.f;
-    } else {
-      pa = __ldg(pg + ipr);
-      pb = __ldg(pg + ipr + 1);
-    }
+    const unsigned rb = (unsigned)dg * (unsigned)(T.tp * T.tt);
+    ra = rb + (brw & 0xffffu);
+    rc = rb + (brw >> 16);
   } else {
     const int* ntg = T.nt + dg * T.tp;
     const Bracket pb_ = pbracket_f(pg, np, pq, s.ipr);
-    ipr = pb_.i;
+    const int ipr = pb_.i;
     s.ipr = ipr;
     pa = pb_.a;
     pb = pb_.b;
     const int nt0 = __ldg(ntg + ipr), nt1 = __ldg(ntg + ipr + 1);
     if (nt0 < 2 || nt1 < 2) return 0.f;
-    it0 = bracket_regf(T.tf + (dg * T.tp + ipr) * T.tt, nt0, tq);
-    it1 = bracket_regf(T.tf + (dg * T.tp + ipr + 1) * T.tt, nt1, tq);
+    const int it0 = bracket_regf(T.tf + (dg * T.tp + ipr) * T.tt, nt0, tq);
+    const int it1 = bracket_regf(T.tf + (dg * T.tp + ipr + 1) * T.tt, nt1, tq);
+    const unsigned rp = (unsigned)dg * (unsigned)T.tp + (unsigned)ipr;
+    ra = rp * (unsigned)T.tt + (unsigned)it0;
+    rc = (rp + 1u) * (unsigned)T.tt + (unsigned)it1;
   }
-  const unsigned rp = (unsigned)dg * (unsigned)T.tp + (unsigned)ipr;
-  const unsigned ra = rp * (unsigned)T.tt + (unsigned)it0;
-  const unsigned rc = (rp + 1u) * (unsigned)T.tt + (unsigned)it1;
   const RowF r00 = rowf_at<CGA>(T, ra), r01 = rowf_at<CGA>(T, ra + 1u);
   const RowF r10 = rowf_at<CGA>(T, rc), r11 = rowf_at<CGA>(T, rc + 1u);
   if (r00.n < 2 || r01.n < 2 || r10.n < 2 || r11.n < 2) return 0.f;
@@ -378,16 +389,20 @@ __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, float 
   const float e01 = corner_eps<CGA>(T, r01, s.e, du, ucg, s.h[1]);
   const float e10 = corner_eps<CGA>(T, r10, s.e, du, ucg, s.h[2]);
   const float e11 = corner_eps<CGA>(T, r11, s.e, du, ucg, s.h[3]);
-  const float ta = r00.t, tb = r01.t, tc = r10.t, td = r11.t;
-  const float ea = e00 + (e01 - e00) / (tb - ta) * (tq - ta);
-  const float eb = e10 + (e11 - e10) / (td - tc) * (tq - tc);
-  float w;
-  if (cga && pre)
+  float ea, eb, w;
+  if (pre) {
+    ea = e00 + (e01 - e00) * wta;
+    eb = e10 + (e11 - e10) * wtb;
     w = wpre;
-  else if (cga && pq / pa > 0.f && pb / pa > 0.f)
-    w = __logf(pq / pa) / __logf(pb / pa);
-  else
-    w = (pq - pa) / (pb - pa);
+  } else {
+    const float ta = r00.t, tb = r01.t, tc = r10.t, td = r11.t;
+    ea = e00 + (e01 - e00) / (tb - ta) * (tq - ta);
+    eb = e10 + (e11 - e10) / (td - tc) * (tq - tc);
+    if (cga && pq / pa > 0.f && pb / pa > 0.f)
+      w = __logf(pq / pa) / __logf(pb / pa);
+    else
+      w = (pq - pa) / (pb - pa);
+  }
   float e = ea + (eb - ea) * w;
   e = fminf(fmaxf(e, 0.f), 1.f);
   const float te = 1.f - e;  // exact for e >= 0.5
@@ -412,7 +427,7 @@ __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, float 
 // other rays (finite-difference perturbations that leave a path prefix
 // unchanged); the arithmetic of every point is the same.
 template <int MINB, bool CGA, bool SPLIT = false, bool RESUME = false>
-__global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, ChanDev ch,
+__global__ void __launch_bounds__(kPathThreads, MINB) k_path_mixed(CtlDev c, TblDev T, ChanDev ch,
                                                           BatchDev b, LosDev L, MixedPlan P,
                                                           float* refl) {
   const int ng = c.ng;
@@ -457,9 +472,10 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
   const float st0 = (float)kTMIN, sdt = (float)((kTMAX - kTMIN) / (kNS - 1.0));
 
   // per-emitter path state in shared memory, word-major per thread:
-  // sh[(g * kStateWords + w) * blockDim.x + threadIdx.x]
+  // sh[(g * kStateWords + w) * kPathThreads + threadIdx.x]
   extern __shared__ unsigned sh_state[];
-  const int nth = blockDim.x, tid = threadIdx.x;
+  constexpr int nth = kPathThreads;
+  const int tid = threadIdx.x;
   // behind the state: the channel's constants (kChanConsts words per warp:
   // continuum coefficients, [11] channel index, [12] window index) and
   // kThreadFloats per thread (cloud extinction, surface emissivity), read
@@ -582,10 +598,12 @@ __global__ void __launch_bounds__(128, MINB) k_path_mixed(CtlDev c, TblDev T, Ch
         const float ucg = cga ? f[(F.cgu0 + g) * 32] : 0.f;
         const bool brg = (P.brmask >> g) & 1u;
         const unsigned brw = brg ? __float_as_uint(f[(F.br0 + g) * 32]) : (kNoBracket | 1u);
-        const float wpre = cga && brg ? f[(F.pw0 + g) * 32] : 0.f;
+        const float wpre = brg ? f[(F.pw0 + g) * 32] : 0.f;
+        const float wta = brg ? f[(F.tw0 + 2 * g) * 32] : 0.f;
+        const float wtb = brg ? f[(F.tw0 + 2 * g + 1) * 32] : 0.f;
         GasState st = sload(g);
         const long long dg = dg0 + g;  // (channel, emitter)
-        eg = gas_eps_f<CGA>(T, dg, pq, tq, du, ucg, brw, wpre, st, sat);
+        eg = gas_eps_f<CGA>(T, dg, pq, tq, du, ucg, brw, wpre, wta, wtb, st, sat);
         sstore(g, st);
       }
       E = E + (1.f - E) * eg;
@@ -755,9 +773,11 @@ __global__ void __launch_bounds__(128) k_path_gas(CtlDev c, TblDev T, BatchDev b
     const float tq = cga ? f[(F.cgt0 + g) * 32] : f[F.t * 32];
     const float ucg = cga ? f[(F.cgu0 + g) * 32] : 0.f;
     const unsigned brw = brbit ? __float_as_uint(f[(F.br0 + g) * 32]) : (kNoBracket | 1u);
-    const float wpre = cga && brbit ? f[(F.pw0 + g) * 32] : 0.f;
+    const float wpre = brbit ? f[(F.pw0 + g) * 32] : 0.f;
+    const float wta = brbit ? f[(F.tw0 + 2 * g) * 32] : 0.f;
+    const float wtb = brbit ? f[(F.tw0 + 2 * g + 1) * 32] : 0.f;
     bool sat = false;
-    const float eg = gas_eps_f<CGA>(T, dg, pq, tq, du, ucg, brw, wpre, st, sat);
+    const float eg = gas_eps_f<CGA>(T, dg, pq, tq, du, ucg, brw, wpre, wta, wtb, st, sat);
     const long long o = seg0 + ip * segstride;
     P.seg_eps[o] = eg;
     P.seg_sat[o] = sat ? 1 : 0;
@@ -835,13 +855,13 @@ void launch_variant(const CtlDev& c, const TblDev& T, const ChanDev& ch, const B
     cudaFuncSetAttribute(k_path_mixed<12, CGA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   }
   switch (variant) {
-    case 1: k_path_mixed<5, CGA><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl); break;
-    case 2: k_path_mixed<6, CGA><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl); break;
-    case 3: k_path_mixed<4, CGA><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl); break;
-    case 4: k_path_mixed<8, CGA><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl); break;
-    case 5: k_path_mixed<10, CGA><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl); break;
-    case 6: k_path_mixed<12, CGA><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl); break;
-    default: k_path_mixed<1, CGA><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl); break;
+    case 1: k_path_mixed<5, CGA><<<nblk, kPathThreads, smem, s>>>(c, T, ch, b, L, P, refl); break;
+    case 2: k_path_mixed<6, CGA><<<nblk, kPathThreads, smem, s>>>(c, T, ch, b, L, P, refl); break;
+    case 3: k_path_mixed<4, CGA><<<nblk, kPathThreads, smem, s>>>(c, T, ch, b, L, P, refl); break;
+    case 4: k_path_mixed<8, CGA><<<nblk, kPathThreads, smem, s>>>(c, T, ch, b, L, P, refl); break;
+    case 5: k_path_mixed<10, CGA><<<nblk, kPathThreads, smem, s>>>(c, T, ch, b, L, P, refl); break;
+    case 6: k_path_mixed<12, CGA><<<nblk, kPathThreads, smem, s>>>(c, T, ch, b, L, P, refl); break;
+    default: k_path_mixed<1, CGA><<<nblk, kPathThreads, smem, s>>>(c, T, ch, b, L, P, refl); break;
   }
 }
 
@@ -852,8 +872,8 @@ void launch_path_mixed(const CtlDev& c, const TblDev& T, const ChanDev& ch, cons
   const unsigned nblk = (unsigned)((long long)P.ntile * nchb);
   // state, then kChanConsts per warp and kThreadFloats per thread (128
   // threads, 4 warps per block)
-  const size_t smem = sizeof(unsigned) * kStateWords * 128 * (size_t)(c.ng > 0 ? c.ng : 1) +
-                      sizeof(float) * (4 * kChanConsts + kThreadFloats * 128);
+  const size_t smem = sizeof(unsigned) * kStateWords * kPathThreads * (size_t)(c.ng > 0 ? c.ng : 1) +
+                      sizeof(float) * (4 * kChanConsts + kThreadFloats * kPathThreads);
   if (c.formod == 0)
     launch_variant<true>(c, T, ch, b, L, P, refl_scratch, variant, nblk, smem, s);
   else
@@ -869,13 +889,13 @@ void launch_split(const CtlDev& c, const TblDev& T, const ChanDev& ch, const Bat
     cudaFuncSetAttribute(k_path_mixed<1, CGA, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
   const unsigned nblk = (unsigned)((long long)P.ntile * ((c.nd + 3) / 4));
-  k_path_mixed<1, CGA, true><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, refl);
+  k_path_mixed<1, CGA, true><<<nblk, kPathThreads, smem, s>>>(c, T, ch, b, L, P, refl);
 }
 
 void launch_path_split(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
                        const LosDev& L, const MixedPlan& P, float* refl_scratch, cudaStream_t s) {
-  const size_t smem = sizeof(unsigned) * kStateWords * 128 * (size_t)(c.ng > 0 ? c.ng : 1) +
-                      sizeof(float) * (4 * kChanConsts + kThreadFloats * 128);
+  const size_t smem = sizeof(unsigned) * kStateWords * kPathThreads * (size_t)(c.ng > 0 ? c.ng : 1) +
+                      sizeof(float) * (4 * kChanConsts + kThreadFloats * kPathThreads);
   if (c.formod == 0)
     launch_split<true>(c, T, ch, b, L, P, refl_scratch, smem, s);
   else
@@ -889,18 +909,18 @@ void launch_path_resume(const CtlDev& c, const TblDev& T, const ChanDev& ch, con
   const int nchb = (c.nd + 3) / 4;
   const unsigned nblk = (unsigned)((long long)(P.tile1 - P.tile0) * nchb);
   if (nblk == 0) return;
-  const size_t smem = sizeof(unsigned) * kStateWords * 128 * (size_t)(c.ng > 0 ? c.ng : 1) +
-                      sizeof(float) * (4 * kChanConsts + kThreadFloats * 128);
+  const size_t smem = sizeof(unsigned) * kStateWords * kPathThreads * (size_t)(c.ng > 0 ? c.ng : 1) +
+                      sizeof(float) * (4 * kChanConsts + kThreadFloats * kPathThreads);
   if (c.formod == 0) {
     if (smem > 48 * 1024)
       cudaFuncSetAttribute(k_path_mixed<8, true, false, true>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_path_mixed<8, true, false, true><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, nullptr);
+    k_path_mixed<8, true, false, true><<<nblk, kPathThreads, smem, s>>>(c, T, ch, b, L, P, nullptr);
   } else {
     if (smem > 48 * 1024)
       cudaFuncSetAttribute(k_path_mixed<8, false, false, true>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_path_mixed<8, false, false, true><<<nblk, 128, smem, s>>>(c, T, ch, b, L, P, nullptr);
+    k_path_mixed<8, false, false, true><<<nblk, kPathThreads, smem, s>>>(c, T, ch, b, L, P, nullptr);
   }
 }
 
