@@ -20,20 +20,29 @@
 
 namespace jgb {
 
-// Field indices of a tile plane.  For emitters whose p-T grids are shared by
-// all channels, the channel-independent part of the table interpolation is
-// done once per LOS point here: br0..br0+ng-1 hold the rows of the point's
-// p-T cell within a (channel, emitter) table, ipr * tt + it0 | ((ipr + 1)
-// * tt + it1) << 16 (kNoBracket: no table, kNoBracket | 2: no temperature
-// rows at that pressure; tp * tt < 2^15), pw0..pw0+ng-1 the
-// pressure interpolation weight in that bracket (linear in EGA, log-linear
-// in CGA), and tw0 + 2g, tw0 + 2g + 1 the temperature weights at the lower
-// and upper pressure of the bracket.
+// Field indices of a tile plane: the point's p, t, ds, q_H2O and cloud
+// factor, the extinction per window, then one block of kEmitterFields(CGA)
+// fields per emitter, emitter g's at g0 + g * es + k (k constant, so that a
+// warp addresses them from one base):
+//   EGA: u, br, pw, wa, wb;  CGA: u, cgp, cgt, cgu, br, pw, wa, wb.
+// For emitters whose p-T grids are shared by all channels, the
+// channel-independent part of the table interpolation is done once per LOS
+// point: br holds the rows of the point's p-T cell within a (channel,
+// emitter) table, ipr * tt + it0 | ((ipr + 1) * tt + it1) << 16
+// (kNoBracket: no table, kNoBracket | 2: no temperature rows at that
+// pressure; tp * tt < 2^15), pw the pressure interpolation weight in that
+// bracket (linear in EGA, log-linear in CGA), wa and wb the temperature
+// weights at the lower and upper pressure of the bracket.
 struct Fields {
-  int p, t, ds, qh2o, aux, kw0, u0, cgp0, cgt0, cgu0, br0, pw0, tw0, n;
+  int p, t, ds, qh2o, aux, kw0, g0, es, n;
 };
+constexpr int kFU = 0;  // column of the segment (EGA) / of the path (continua)
+constexpr int kFCgp = 1, kFCgt = 2, kFCgu = 3;  // CGA means
+__host__ __device__ constexpr int kEmitterFields(bool cga) { return cga ? 8 : 5; }
+__host__ __device__ constexpr int kFBr(bool cga) { return cga ? 4 : 1; }  // then pw, wa, wb
 
 __host__ __device__ inline Fields fields_of(const CtlDev& c, unsigned brmask) {
+  (void)brmask;
   Fields f;
   f.p = 0;
   f.t = 1;
@@ -41,14 +50,9 @@ __host__ __device__ inline Fields fields_of(const CtlDev& c, unsigned brmask) {
   f.qh2o = 3;
   f.aux = 4;
   f.kw0 = 5;
-  f.u0 = 5 + c.nw;
-  f.cgp0 = f.u0 + c.ng;
-  f.cgt0 = f.cgp0 + c.ng;
-  f.cgu0 = f.cgt0 + c.ng;
-  f.br0 = c.formod == 0 ? f.cgu0 + c.ng : f.u0 + c.ng;
-  f.pw0 = f.br0 + c.ng;
-  f.tw0 = f.pw0 + c.ng;
-  f.n = f.br0 + (brmask ? 4 * c.ng : 0);
+  f.g0 = 5 + c.nw;
+  f.es = kEmitterFields(c.formod == 0);
+  f.n = f.g0 + c.ng * f.es;
   return f;
 }
 
@@ -259,13 +263,17 @@ __global__ void k_pack_tiles(CtlDev c, TblDev T, LosDev L, MixedPlan P, long lon
   out[F.qh2o * 32] = c.ig_h2o >= 0 ? (float)L.qh2o[q] : 0.f;
   out[F.aux * 32] = (float)L.aux[q];
   for (int w = 0; w < c.nw; w++) out[(F.kw0 + w) * 32] = (float)L.kw[w * L.cap + q];
-  for (int g = 0; g < c.ng; g++) out[(F.u0 + g) * 32] = (float)L.u[g * L.cap + q];
-  if (c.formod == 0)
-    for (int g = 0; g < c.ng; g++) {
-      out[(F.cgp0 + g) * 32] = (float)L.cgp[g * L.cap + q];
-      out[(F.cgt0 + g) * 32] = (float)L.cgt[g * L.cap + q];
-      out[(F.cgu0 + g) * 32] = (float)L.cgu[g * L.cap + q];
+  const bool cgaf = c.formod == 0;
+  for (int g = 0; g < c.ng; g++) {
+    float* og = out + (F.g0 + g * F.es) * 32;
+    og[kFU * 32] = (float)L.u[g * L.cap + q];
+    if (cgaf) {
+      og[kFCgp * 32] = (float)L.cgp[g * L.cap + q];
+      og[kFCgt * 32] = (float)L.cgt[g * L.cap + q];
+      og[kFCgu * 32] = (float)L.cgu[g * L.cap + q];
     }
+    for (int k = 0; k < 4; k++) og[(kFBr(cgaf) + k) * 32] = 0.f;
+  }
   // p-T brackets and interpolation weights on the grids of channel 0
   // (identical for every channel)
   for (int g = 0; P.brmask && g < c.ng; g++) {
@@ -297,10 +305,11 @@ __global__ void k_pack_tiles(CtlDev c, TblDev T, LosDev L, MixedPlan P, long lon
           pw = (pq - pa) / (pb - pa);
       }
     }
-    out[(F.br0 + g) * 32] = __uint_as_float(wd);
-    out[(F.pw0 + g) * 32] = pw;
-    out[(F.tw0 + 2 * g) * 32] = wa;
-    out[(F.tw0 + 2 * g + 1) * 32] = wb;
+    float* og = out + (F.g0 + g * F.es + kFBr(cgaf)) * 32;
+    og[0] = __uint_as_float(wd);
+    og[32] = pw;
+    og[64] = wa;
+    og[96] = wb;
   }
 }
 
@@ -502,12 +511,14 @@ __global__ void __launch_bounds__(kPathThreads, MINB) k_path_mixed(CtlDev c, Tbl
   kthr[0] = cloud;
   kthr[nth] = sfeps;
   __syncwarp();
-  auto sload = [&](int g) {
+  // the pressure-bracket word is only used where the bracket is searched
+  // here (pre = false); with a precomputed bracket it keeps its initial -1
+  auto sload = [&](int g, bool pre = false) {
     const unsigned* q = sh_state + (g * kStateWords) * nth + tid;
     GasState st;
     st.t = __uint_as_float(q[0]);
     st.e = __uint_as_float(q[nth]);
-    st.ipr = (int)q[2 * nth];
+    st.ipr = pre ? -1 : (int)q[2 * nth];
 #pragma unroll
     for (int k = 0; k < 2; k++) {
       const unsigned hw = q[(3 + k) * nth];
@@ -516,11 +527,11 @@ __global__ void __launch_bounds__(kPathThreads, MINB) k_path_mixed(CtlDev c, Tbl
     }
     return st;
   };
-  auto sstore = [&](int g, const GasState& st) {
+  auto sstore = [&](int g, const GasState& st, bool pre = false) {
     unsigned* q = sh_state + (g * kStateWords) * nth + tid;
     q[0] = __float_as_uint(st.t);
     q[nth] = __float_as_uint(st.e);
-    q[2 * nth] = (unsigned)st.ipr;
+    if (!pre) q[2 * nth] = (unsigned)st.ipr;
 #pragma unroll
     for (int k = 0; k < 2; k++)
       q[(3 + k) * nth] = (unsigned)st.h[2 * k] | ((unsigned)st.h[2 * k + 1] << 16);
@@ -592,19 +603,21 @@ __global__ void __launch_bounds__(kPathThreads, MINB) k_path_mixed(CtlDev c, Tbl
         eg = P.seg_eps[o];
         if (P.seg_sat[o]) sat = true;
       } else {
-        const float du = cga ? 0.f : f[(F.u0 + g) * 32];
-        const float pq = cga ? f[(F.cgp0 + g) * 32] : p;
-        const float tq = cga ? f[(F.cgt0 + g) * 32] : t;
-        const float ucg = cga ? f[(F.cgu0 + g) * 32] : 0.f;
+        constexpr int es = kEmitterFields(CGA), kb = kFBr(CGA);
+        const float* fg = f + (F.g0 + g * es) * 32;
+        const float du = cga ? 0.f : fg[kFU * 32];
+        const float pq = cga ? fg[kFCgp * 32] : p;
+        const float tq = cga ? fg[kFCgt * 32] : t;
+        const float ucg = cga ? fg[kFCgu * 32] : 0.f;
         const bool brg = (P.brmask >> g) & 1u;
-        const unsigned brw = brg ? __float_as_uint(f[(F.br0 + g) * 32]) : (kNoBracket | 1u);
-        const float wpre = brg ? f[(F.pw0 + g) * 32] : 0.f;
-        const float wta = brg ? f[(F.tw0 + 2 * g) * 32] : 0.f;
-        const float wtb = brg ? f[(F.tw0 + 2 * g + 1) * 32] : 0.f;
-        GasState st = sload(g);
+        const unsigned brw = brg ? __float_as_uint(fg[kb * 32]) : (kNoBracket | 1u);
+        const float wpre = brg ? fg[(kb + 1) * 32] : 0.f;
+        const float wta = brg ? fg[(kb + 2) * 32] : 0.f;
+        const float wtb = brg ? fg[(kb + 3) * 32] : 0.f;
+        GasState st = sload(g, brg);
         const long long dg = dg0 + g;  // (channel, emitter)
         eg = gas_eps_f<CGA>(T, dg, pq, tq, du, ucg, brw, wpre, wta, wtb, st, sat);
-        sstore(g, st);
+        sstore(g, st, brg);
       }
       E = E + (1.f - E) * eg;
     }
@@ -617,12 +630,12 @@ __global__ void __launch_bounds__(kPathThreads, MINB) k_path_mixed(CtlDev c, Tbl
       const float d230 = t - 230.f, d260 = t - 260.f, d296 = t - 296.f;
       const float ctw = d260 * 5.050505e-4f * d296 * co2_230 - d230 * 9.259259e-4f * d296 * co2_260 +
                         d230 * 4.208754e-4f * d260 * co2_296;
-      const float uco2 = f[(F.u0 + c.ig_co2) * 32];
+      const float uco2 = f[(F.g0 + c.ig_co2 * F.es + kFU) * 32];
       beta += (uco2 / ds) * (float)(1.0 / (kNA * 1000.0)) * pr * ctw;
     }
     if (h2o_on) {
       const float q = f[F.qh2o * 32];
-      const float uh = f[(F.u0 + c.ig_h2o) * 32];
+      const float uh = f[(F.g0 + c.ig_h2o * F.es + kFU) * 32];
       const float nu = kc[0], h2o_s296 = kc[4], h2o_lr = kc[5], h2o_frn = kc[6];
       const float self = h2o_s296 * __expf(h2o_lr * (296.f - t) * (1.f / 36.f));
       const float a1 = nu * ((uh / ds) * 1e-20f) * tanhf(.7193876f / t * nu);
@@ -768,14 +781,16 @@ __global__ void __launch_bounds__(128) k_path_gas(CtlDev c, TblDev T, BatchDev b
   const unsigned brbit = (P.brmask >> g) & 1u;
   for (int ip = 0; ip < n; ip++) {
     const float* f = base + (long long)ip * F.n * 32;
-    const float du = cga ? 0.f : f[(F.u0 + g) * 32];
-    const float pq = cga ? f[(F.cgp0 + g) * 32] : f[F.p * 32];
-    const float tq = cga ? f[(F.cgt0 + g) * 32] : f[F.t * 32];
-    const float ucg = cga ? f[(F.cgu0 + g) * 32] : 0.f;
-    const unsigned brw = brbit ? __float_as_uint(f[(F.br0 + g) * 32]) : (kNoBracket | 1u);
-    const float wpre = brbit ? f[(F.pw0 + g) * 32] : 0.f;
-    const float wta = brbit ? f[(F.tw0 + 2 * g) * 32] : 0.f;
-    const float wtb = brbit ? f[(F.tw0 + 2 * g + 1) * 32] : 0.f;
+    constexpr int es = kEmitterFields(CGA), kb = kFBr(CGA);
+    const float* fg = f + (F.g0 + g * es) * 32;
+    const float du = cga ? 0.f : fg[kFU * 32];
+    const float pq = cga ? fg[kFCgp * 32] : f[F.p * 32];
+    const float tq = cga ? fg[kFCgt * 32] : f[F.t * 32];
+    const float ucg = cga ? fg[kFCgu * 32] : 0.f;
+    const unsigned brw = brbit ? __float_as_uint(fg[kb * 32]) : (kNoBracket | 1u);
+    const float wpre = brbit ? fg[(kb + 1) * 32] : 0.f;
+    const float wta = brbit ? fg[(kb + 2) * 32] : 0.f;
+    const float wtb = brbit ? fg[(kb + 3) * 32] : 0.f;
     bool sat = false;
     const float eg = gas_eps_f<CGA>(T, dg, pq, tq, du, ucg, brw, wpre, wta, wtb, st, sat);
     const long long o = seg0 + ip * segstride;
