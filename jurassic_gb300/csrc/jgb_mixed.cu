@@ -85,7 +85,9 @@ struct RowF {
 // below the rows and saturates above them).  CGA records are 16 bytes,
 // {n, t, u[0], eps[0]}: a column above a row brackets at n-2, and the
 // search brings the row's last entries.
-template <bool CGA>
+// With the temperature weights precomputed (PRE) a row's temperature is not
+// needed: EGA then reads only the count n of the second half of the record.
+template <bool CGA, bool PRE = false>
 __device__ __forceinline__ RowF rowf_at(const TblDev& T, unsigned r) {
   RowF w;
   w.off = r * (unsigned)T.tu;
@@ -97,9 +99,15 @@ __device__ __forceinline__ RowF rowf_at(const TblDev& T, unsigned r) {
     w.e0 = m.w;
     w.un = w.en = 0.f;
   } else {
-    const float4 m = __ldg(T.rowmeta + 2 * r), m2 = __ldg(T.rowmeta + 2 * r + 1);
-    w.n = __float_as_int(m2.x);
-    w.t = m2.y;
+    const float4 m = __ldg(T.rowmeta + 2 * r);
+    if (PRE) {
+      w.n = __ldg(reinterpret_cast<const int*>(T.rowmeta + 2 * r + 1));
+      w.t = 0.f;
+    } else {
+      const float4 m2 = __ldg(T.rowmeta + 2 * r + 1);
+      w.n = __float_as_int(m2.x);
+      w.t = m2.y;
+    }
     w.u0 = m.x;
     w.un = m.y;
     w.e0 = m.z;
@@ -391,19 +399,26 @@ __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, float 
     ra = rp * (unsigned)T.tt + (unsigned)it0;
     rc = (rp + 1u) * (unsigned)T.tt + (unsigned)it1;
   }
-  const RowF r00 = rowf_at<CGA>(T, ra), r01 = rowf_at<CGA>(T, ra + 1u);
-  const RowF r10 = rowf_at<CGA>(T, rc), r11 = rowf_at<CGA>(T, rc + 1u);
-  if (r00.n < 2 || r01.n < 2 || r10.n < 2 || r11.n < 2) return 0.f;
-  const float e00 = corner_eps<CGA>(T, r00, s.e, du, ucg, s.h[0]);
-  const float e01 = corner_eps<CGA>(T, r01, s.e, du, ucg, s.h[1]);
-  const float e10 = corner_eps<CGA>(T, r10, s.e, du, ucg, s.h[2]);
-  const float e11 = corner_eps<CGA>(T, r11, s.e, du, ucg, s.h[3]);
   float ea, eb, w;
   if (pre) {
+    const RowF r00 = rowf_at<CGA, true>(T, ra), r01 = rowf_at<CGA, true>(T, ra + 1u);
+    const RowF r10 = rowf_at<CGA, true>(T, rc), r11 = rowf_at<CGA, true>(T, rc + 1u);
+    if (r00.n < 2 || r01.n < 2 || r10.n < 2 || r11.n < 2) return 0.f;
+    const float e00 = corner_eps<CGA>(T, r00, s.e, du, ucg, s.h[0]);
+    const float e01 = corner_eps<CGA>(T, r01, s.e, du, ucg, s.h[1]);
+    const float e10 = corner_eps<CGA>(T, r10, s.e, du, ucg, s.h[2]);
+    const float e11 = corner_eps<CGA>(T, r11, s.e, du, ucg, s.h[3]);
     ea = e00 + (e01 - e00) * wta;
     eb = e10 + (e11 - e10) * wtb;
     w = wpre;
   } else {
+    const RowF r00 = rowf_at<CGA>(T, ra), r01 = rowf_at<CGA>(T, ra + 1u);
+    const RowF r10 = rowf_at<CGA>(T, rc), r11 = rowf_at<CGA>(T, rc + 1u);
+    if (r00.n < 2 || r01.n < 2 || r10.n < 2 || r11.n < 2) return 0.f;
+    const float e00 = corner_eps<CGA>(T, r00, s.e, du, ucg, s.h[0]);
+    const float e01 = corner_eps<CGA>(T, r01, s.e, du, ucg, s.h[1]);
+    const float e10 = corner_eps<CGA>(T, r10, s.e, du, ucg, s.h[2]);
+    const float e11 = corner_eps<CGA>(T, r11, s.e, du, ucg, s.h[3]);
     const float ta = r00.t, tb = r01.t, tc = r10.t, td = r11.t;
     ea = e00 + (e01 - e00) / (tb - ta) * (tq - ta);
     eb = e10 + (e11 - e10) / (td - tc) * (tq - tc);
