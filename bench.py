@@ -165,11 +165,10 @@ def sm_count(device=0):
 
 def path_fields(ctl):
     """Float fields per LOS point of the path kernel's tile planes: p, t, ds,
-    q_H2O, cloud factor, extinction per window, column per emitter (EGA) or
-    CG pressure, temperature and column per emitter (CGA, plus the column),
-    and the per-point p-T bracket (+ pressure weight in CGA) per emitter."""
-    ng, nw = ctl.ng, ctl.nw
-    return 5 + nw + ng + (3 * ng if ctl.formod == 0 else 0) + (2 * ng if ctl.formod == 0 else ng)
+    q_H2O, cloud factor, extinction per window, and per emitter its column
+    (plus the CG pressure, temperature and column in CGA), the p-T cell's
+    rows and the pressure and two temperature interpolation weights."""
+    return 5 + ctl.nw + ctl.ng * (8 if ctl.formod == 0 else 5)
 
 
 def compulsory_bytes(ctl, tables, los_points, nray):
@@ -784,11 +783,13 @@ def main():
                            "parallelism": "replicas" if world > 1 else "single GPU"},
                 "stage_ms": {k: stats[k] for k in ("hydro_ms", "trace_ms", "pack_ms", "path_ms")},
                 "trace_passes": stats["trace_passes"],
-                "autotune": {"path_variant": stats["path_variant"], "variant_ms": stats["tune_ms"][:7],
-                             "variants": ["no register cap", "5 blocks/SM (<=102 regs)",
-                                          "6 blocks/SM (<=85 regs)", "4 blocks/SM (<=128 regs)",
-                                          "8 blocks/SM (<=64 regs)", "10 blocks/SM (<=51 regs)",
-                                          "12 blocks/SM (<=42 regs)"]},
+                "autotune": {"path_variant": stats["path_variant"], "variant_ms": stats["tune_ms"][:14],
+                             "caps": ["no register cap", "5 blocks/SM (<=102 regs)",
+                                      "6 blocks/SM (<=85 regs)", "4 blocks/SM (<=128 regs)",
+                                      "8 blocks/SM (<=64 regs)", "10 blocks/SM (<=51 regs)",
+                                      "12 blocks/SM (<=42 regs)"],
+                             "note": "variant v: register cap v % 7; block = 4 channels x 1 tile "
+                                     "(v < 7) or 1 channel x 4 tiles (v >= 7)"},
                 "wall_s_timed": wall,
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h), "ms_per_step": statistics.mean(e2e_ms),

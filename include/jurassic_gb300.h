@@ -95,8 +95,11 @@ typedef struct {
   double h2d_ms, hydro_ms, trace_ms, pack_ms, path_ms, d2h_ms, total_ms;
   long long los_points;          /* LOS points of the batch */
   int path_launches;             /* kernels launched by the last call */
-  int path_variant;              /* mixed path kernel variant chosen by the autotuner */
-  float tune_ms[8];              /* autotuner timings of the variants [ms] */
+  int path_variant;              /* mixed path kernel variant chosen by the autotuner:
+                                    register cap (path_variant % 7) and block shape
+                                    (path_variant / 7: 0 = 4 channels of one tile,
+                                    1 = one channel of 4 tiles) */
+  float tune_ms[16];             /* autotuner timings of the variants [ms] */
   int trace_passes;              /* ray-tracing passes over the batch: 1 = one
                                     pass, 2 = count + fill, 3 = a capacity
                                     bound was exceeded and the rays were

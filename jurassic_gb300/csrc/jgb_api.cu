@@ -668,14 +668,15 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
       launch_path_split(c, T, ch, bo, L, Pm, refl, s);
       launches += 7;
     } else if (x->path_variant < 0 && !rs) {
-      // autotune: time every variant on this batch (results are identical)
+      // autotune: time every register cap with both block shapes on this
+      // batch (results are identical)
       const char* force = getenv("JGB_PATH_VARIANT");
       if (force) {
         x->path_variant = atoi(force) % path_mixed_variants();
       } else {
         float best = 1e30f;
         x->tune_ms.clear();
-        for (int v = 0; v < path_mixed_variants(); v++) {
+        auto trial = [&](int v) -> int {
           CK(cudaEventRecord(x->ev[4], s));
           launch_path_mixed(c, T, ch, bo, L, Pm, refl, v, s);
           CK(cudaEventRecord(x->ev[5], s));
@@ -686,6 +687,11 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
             best = ms;
             x->path_variant = v;
           }
+          return JGB_OK;
+        };
+        for (int v = 0; v < path_mixed_variants(); v++) {
+          const int rc = trial(v);
+          if (rc) return rc;
         }
       }
     }
@@ -709,7 +715,7 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
   x->stats.trace_passes = passes;
   x->stats.path_launches = launches;
   x->stats.path_variant = x->path_variant;
-  for (int v = 0; v < 8; v++) x->stats.tune_ms[v] = v < (int)x->tune_ms.size() ? x->tune_ms[v] : 0.f;
+  for (int v = 0; v < 16; v++) x->stats.tune_ms[v] = v < (int)x->tune_ms.size() ? x->tune_ms[v] : 0.f;
   return JGB_OK;
 }
 

@@ -54,6 +54,11 @@ struct MixedPlan {
   unsigned char* seg_sat;
   // tiles [tile0, tile1) of this launch
   int tile0, tile1;
+  // block shape of the path kernel: 0 = the 4 warps of a block take 4
+  // channels of one tile (they share the tile's LOS data), 1 = one channel
+  // of 4 consecutive tiles (they share the table rows: similar rays at
+  // similar p-T)
+  int tile_major;
   // resumed forward models (finite-difference perturbations): start[r] is
   // the LOS point ray r starts at (its state read from snap, slot r); ray r
   // saves the path state for the rays snap_ray[k] before its point
@@ -67,6 +72,9 @@ struct MixedPlan {
 int mixed_nfield(const CtlDev& c, unsigned brmask);
 void launch_pack_tiles_n(const CtlDev& c, const TblDev& T, const LosDev& L, const MixedPlan& P,
                          long long total_tile_points, cudaStream_t s);
+// register-cap variants of the path kernel (each with both block shapes:
+// variant v = cap + path_mixed_caps() * shape)
+int path_mixed_caps();
 int path_mixed_variants();
 // the path split over emitters: one warp per (tile, channel, emitter) for the
 // emitter path states, then the combination and radiance per (tile, channel)

@@ -457,9 +457,15 @@ __global__ void __launch_bounds__(kPathThreads, MINB) k_path_mixed(CtlDev c, Tbl
   const int ng = c.ng;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
-  const int nchb = (c.nd + 3) / 4;
-  const int tile = P.tile0 + blockIdx.x / nchb;
-  const int id = (blockIdx.x % nchb) * 4 + warp;
+  int tile, id;
+  if (P.tile_major) {  // one channel of 4 consecutive tiles
+    tile = P.tile0 + (int)(blockIdx.x / c.nd) * 4 + warp;
+    id = (int)(blockIdx.x % c.nd);
+  } else {             // 4 channels of one tile
+    const int nchb = (c.nd + 3) / 4;
+    tile = P.tile0 + blockIdx.x / nchb;
+    id = (blockIdx.x % nchb) * 4 + warp;
+  }
   if (tile >= P.tile1 || id >= c.nd) return;
   int r = P.perm[tile * 32 + lane];
   if (r >= 0 && b.obs_skip && b.obs_skip[b.ray_obs[r]]) r = -1;  // lane idle, outputs untouched
@@ -868,13 +874,16 @@ void launch_pack_tiles_n(const CtlDev& c, const TblDev& T, const LosDev& L, cons
   k_pack_tiles<<<(unsigned)((nth + bs - 1) / bs), bs, 0, s>>>(c, T, L, P, total_tile_points);
 }
 
-// register caps of the autotuner's variants (minimum resident blocks per SM)
-int path_mixed_variants() { return 7; }
+// register caps of the autotuner's variants (minimum resident blocks per SM),
+// each with both block shapes
+int path_mixed_caps() { return 7; }
+int path_mixed_variants() { return 2 * path_mixed_caps(); }
 
 template <bool CGA>
 void launch_variant(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
                     const LosDev& L, const MixedPlan& P, float* refl, int variant, unsigned nblk,
                     size_t smem, cudaStream_t s) {
+  variant %= path_mixed_caps();
   if (smem > 48 * 1024) {  // many emitters: opt in to the larger shared memory
     cudaFuncSetAttribute(k_path_mixed<1, CGA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_path_mixed<5, CGA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -898,16 +907,19 @@ void launch_variant(const CtlDev& c, const TblDev& T, const ChanDev& ch, const B
 void launch_path_mixed(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
                        const LosDev& L, const MixedPlan& P, float* refl_scratch, int variant,
                        cudaStream_t s) {
+  MixedPlan Pv = P;
+  Pv.tile_major = variant >= path_mixed_caps() ? 1 : 0;
   const int nchb = (c.nd + 3) / 4;
-  const unsigned nblk = (unsigned)((long long)P.ntile * nchb);
+  const unsigned nblk = Pv.tile_major ? (unsigned)((long long)((P.ntile + 3) / 4) * c.nd)
+                                      : (unsigned)((long long)P.ntile * nchb);
   // state, then kChanConsts per warp and kThreadFloats per thread (128
   // threads, 4 warps per block)
   const size_t smem = sizeof(unsigned) * kStateWords * kPathThreads * (size_t)(c.ng > 0 ? c.ng : 1) +
                       sizeof(float) * (4 * kChanConsts + kThreadFloats * kPathThreads);
   if (c.formod == 0)
-    launch_variant<true>(c, T, ch, b, L, P, refl_scratch, variant, nblk, smem, s);
+    launch_variant<true>(c, T, ch, b, L, Pv, refl_scratch, variant, nblk, smem, s);
   else
-    launch_variant<false>(c, T, ch, b, L, P, refl_scratch, variant, nblk, smem, s);
+    launch_variant<false>(c, T, ch, b, L, Pv, refl_scratch, variant, nblk, smem, s);
 }
 
 template <bool CGA>
@@ -935,9 +947,12 @@ void launch_path_split(const CtlDev& c, const TblDev& T, const ChanDev& ch, cons
 int path_state_words(const CtlDev& c) { return kStateWords * c.ng + 3; }
 
 void launch_path_resume(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
-                        const LosDev& L, const MixedPlan& P, cudaStream_t s) {
-  const int nchb = (c.nd + 3) / 4;
-  const unsigned nblk = (unsigned)((long long)(P.tile1 - P.tile0) * nchb);
+                        const LosDev& L, const MixedPlan& P0, cudaStream_t s) {
+  // block = one channel of 4 consecutive tiles (the perturbations of one
+  // observation share table rows)
+  MixedPlan P = P0;
+  P.tile_major = 1;
+  const unsigned nblk = (unsigned)((long long)((P.tile1 - P.tile0 + 3) / 4) * c.nd);
   if (nblk == 0) return;
   const size_t smem = sizeof(unsigned) * kStateWords * kPathThreads * (size_t)(c.ng > 0 ? c.ng : 1) +
                       sizeof(float) * (4 * kChanConsts + kThreadFloats * kPathThreads);

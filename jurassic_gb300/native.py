@@ -74,7 +74,7 @@ class Stats(C.Structure):
                 ("pack_ms", C.c_double), ("path_ms", C.c_double), ("d2h_ms", C.c_double),
                 ("total_ms", C.c_double), ("los_points", C.c_longlong),
                 ("path_launches", C.c_int), ("path_variant", C.c_int),
-                ("tune_ms", C.c_float * 8), ("trace_passes", C.c_int),
+                ("tune_ms", C.c_float * 16), ("trace_passes", C.c_int),
                 ("resume_skip", C.c_double)]
 
     def as_dict(self):
