@@ -144,13 +144,13 @@ def peaks():
 # channels, 5 emitters), from one capture of the 4000-observation launch
 # with the same channels, emitters and tables (the nadir observations are
 # alike, so the counters scale with the LOS points):
-#   ncu --set full --clock-control none -k regex:k_path_mixed -s 7 -c 1 -o path \
+#   ncu --set full --clock-control none -k regex:k_path_mixed -s 14 -c 1 -o path \
 #       python bench.py --nobs 4000 --steps 2 --warmup 1 --fp64-steps 0 --no-cpu \
 #       --serve-requests 0 --no-extra
-#   smsp__inst_executed.sum 3.6857e10, dram__bytes_read.sum + write.sum 359.8 MB,
+#   smsp__inst_executed.sum 3.2978e10, dram__bytes_read.sum + write.sum 769.9 MB,
 #   4,004,179 LOS points in the launch.
-PATH_NCU_NADIR = {"warp_inst_per_los_point": 36856860952 / 4004179,
-                  "dram_bytes_per_los_point": 359.773440e6 / 4004179}
+PATH_NCU_NADIR = {"warp_inst_per_los_point": 32978257734 / 4004179,
+                  "dram_bytes_per_los_point": 769.919232e6 / 4004179}
 
 
 def sm_count(device=0):
