@@ -105,3 +105,40 @@ def stream_requests(ctl, forward, n, seed=55):
     nch = rng.integers(50, 301, n)
     return synth.retrieval_requests(ctl, forward, n, seed, nlev=(41, 101), ztop=100.0, nch=nch,
                                     limb_rays=5)
+
+
+def main(argv=None):
+    """Closed-loop run of the serving stream: ``python -m
+    jurassic_gb300.serving --requests N [--precision mixed|fp64]
+    [--marker]``.  Serves N requests after a 4-request warm-up and prints
+    one JSON line (wall time, steps, retrievals/s, engine phase times).
+    --marker launches a short measurement kernel (jgb_measure_l2_read)
+    just before the timed run, so that a profiler's launch list can be cut
+    there."""
+    import argparse
+    import ctypes
+    import json
+
+    from . import native
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--requests", type=int, default=64)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--marker", action="store_true")
+    a = ap.parse_args(argv)
+    prec = native.MIXED if a.precision == "mixed" else native.FP64
+    ctl, ret, tables, filters = stream_workload()
+    ctx = native.Context(ctl, tables, filters)
+    reqs = stream_requests(ctl, lambda b: ctx.formod_batch(b.fresh_outputs(), native.FP64),
+                           a.requests)
+    serve(ctx.engine(ret, prec), ctl, reqs[:4], np.inf)   # warm-up (autotuner, allocations)
+    eng = ctx.engine(ret, prec)
+    if a.marker:
+        g = ctypes.c_double(0.0)
+        native.load().jgb_measure_l2_read(1 << 20, 1, ctypes.byref(g))
+    r = serve(eng, ctl, reqs, np.inf)
+    print(json.dumps({k: v for k, v in r.items() if k != "results"}))
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()
