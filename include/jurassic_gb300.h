@@ -175,6 +175,11 @@ int jgb_set_path_split(jgb_ctx *ctx, int mode);
    bases run first and the lanes of a warp walk the union of their ranges,
    so it pays on large batches: mode 1 (default) resumes a Jacobian chunk
    when the estimated schedule of its tiles is shorter, 2 always, 0 never.
+   A perturbation of one emitter's mixing ratio (or of an extinction) also
+   leaves the other emitters' path states equal to the base's: resumed
+   chunks then take those emitters' segment emissivities from the base's
+   walk and compute only the perturbed one, where at least 30 % of the
+   perturbed lookups can be shared (mode 3: always resume and always share).
    The results do not depend on it. */
 int jgb_set_fd_resume(jgb_ctx *ctx, int mode);
 

@@ -239,12 +239,17 @@ __global__ void k_resume_points(int nray, BatchDev b, LosDev L, int nbase, const
 }
 
 // Sort key of a resumed batch: bases first (their tiles run first and save
-// the states), then by measured channels, by the LOS points left to do in
-// 64-point buckets (longest first, so that no long warp is left for the
-// end) and by start point in 16-point buckets (so that the lanes of a warp
-// walk nearly the same range of points).
+// the states), then by measured channels, by perturbation class (below), by
+// the LOS points left to do in 64-point buckets (longest first, so that no
+// long warp is left for the end) and by start point in 16-point buckets (so
+// that the lanes of a warp walk nearly the same range of points).
+// The perturbation class follows the channels: the perturbations of one
+// emitter's mixing ratio (class 1 + emitter) and of extinctions (class 0)
+// compute only that emitter (none) and take the others from their base, so
+// a warp whose lanes share the class skips the others' work altogether.
 __global__ void k_resume_keys(int nray, int nbase_rays, int nd, const unsigned char* mask,
-                              int skip_masked, const int* count, const int* start, int* key) {
+                              int skip_masked, const int* count, const int* start,
+                              const int4* pert, const int* ray_obs, int* key) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nray) return;
   int m = nd;
@@ -253,8 +258,13 @@ __global__ void k_resume_keys(int nray, int nbase_rays, int nd, const unsigned c
     for (int id = 0; id < nd; id++) m += mask[(long long)id * nray + r] ? 0 : 1;
   }
   const int left = count[r] - start[r];
-  key[r] = ((r < nbase_rays ? 1 : 0) << 30) | (min(m, 511) << 21) | (min(left >> 6, 127) << 14) |
-           (min(start[r] >> 4, 255) << 6);
+  int cls = 0;
+  if (pert) {  // emitters shared with the base
+    const int4 pr = pert[ray_obs[r]];
+    cls = pr.x == 2 ? 1 + min(pr.y, 13) : pr.x == 3 ? 0 : 15;
+  }
+  key[r] = ((r < nbase_rays ? 1 : 0) << 30) | (min(m, 511) << 21) | (cls << 17) |
+           (min(left >> 6, 127) << 10) | (min(start[r] >> 4, 255) << 2);
 }
 
 // Sort key of a batch whose masked pairs are skipped: rays with the same
@@ -468,8 +478,27 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
     double resume_skip = 0.0;
     int* rstart = nullptr;
     int *snap_off = nullptr, *snap_ip = nullptr, *snap_ray = nullptr;
+    // emitters shared between a perturbed ray and its base (see MixedPlan)
+    float* seg_base = nullptr;
+    unsigned *seg_satm = nullptr, *seg_final = nullptr;
+    int* seg_nvalid = nullptr;
+    const int2* seg_reuse = nullptr;
+    bool share_emitters = false;
     if (rs) {
       nbase_rays = rs->h_ray_off[rs->nbase];
+      // sharing emitters with the base pays where most of the perturbed
+      // lookups can be taken from it (several emitters, mostly mixing-ratio
+      // perturbations); elsewhere its bookkeeping and the registers of the
+      // sharing kernel cost more than it saves
+      double shr = 0, tot = 0;
+      for (int e = rs->nbase; e < b.nobs; e++) {
+        const double wr = rs->h_ray_off[e + 1] - rs->h_ray_off[e];
+        const int4 pr = rs->h_pert[e];
+        tot += wr;
+        if (pr.x == 2 && c.ng > 1) shr += wr * (c.ng - 1.0) / c.ng;
+        else if (pr.x == 3) shr += wr;
+      }
+      share_emitters = x->fd_resume == 3 || (tot > 0 && shr / tot >= 0.3);
       CK(x->rs_start.reserve(sizeof(int) * (size_t)nray));
       rstart = x->rs_start.as<int>();
       k_resume_points<<<(nray + 127) / 128, 128, 0, s>>>(nray, b, L, rs->nbase, rs->pert,
@@ -478,7 +507,9 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
       CK(cudaGetLastError());
       CK(x->tiles_keys.reserve(sizeof(int) * (size_t)nray));
       k_resume_keys<<<(nray + 255) / 256, 256, 0, s>>>(nray, nbase_rays, c.nd, b.mask, b.skip_masked,
-                                                        L.count, rstart, x->tiles_keys.as<int>());
+                                                        L.count, rstart,
+                                                        share_emitters ? rs->pert : nullptr,
+                                                        b.ray_obs, x->tiles_keys.as<int>());
       std::vector<int> hs(nray), ray_obs(nray), hc(nray), hk(nray);
       CK(cudaMemcpyAsync(hs.data(), rstart, sizeof(int) * nray, cudaMemcpyDeviceToHost, s));
       CK(cudaMemcpyAsync(hc.data(), L.count, sizeof(int) * nray, cudaMemcpyDeviceToHost, s));
@@ -573,6 +604,42 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
         CK(cudaMemcpyAsync(snap_ray, sray.data(), sizeof(int) * nsnap, cudaMemcpyHostToDevice, s));
       }
       CK(x->rs_snap.reserve(sizeof(float) * (size_t)nray * c.nd * path_state_words(c)));
+      // a perturbation of one emitter's mixing ratio (array 2) or of an
+      // extinction (array 3) leaves the LOS (refraction needs p and T only)
+      // and the other emitters' inputs and states equal to the base's: those
+      // emitters' segment emissivities are taken from the base's walk
+      std::vector<int2> reuse(nray, make_int2(-1, -1));
+      bool any_reuse = false;
+      for (int r = nbase_rays; r < nray && share_emitters; r++) {
+        const int e = ray_obs[r];
+        const int4 pr = rs->h_pert[e];
+        if (pr.x == 2 || pr.x == 3) {
+          const int eb = rs->h_base_obs[e];
+          reuse[r] = make_int2(rs->h_ray_off[eb] + (r - rs->h_ray_off[e]), pr.x == 2 ? pr.y : -1);
+          any_reuse = true;
+        }
+      }
+      if (any_reuse) {
+        long long bpts = 0;
+        CK(cudaMemcpyAsync(&bpts, L.off + nbase_rays, sizeof(long long), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        const size_t nseg = (size_t)std::max(bpts, 1LL) * c.nd;
+        const size_t nst = (size_t)nbase_rays * c.nd;
+        const size_t sw = (size_t)path_state_words(c) - 3;
+        auto a16 = [](size_t b) { return (b + 15) & ~size_t(15); };
+        const size_t b_eps = a16(sizeof(float) * nseg * c.ng), b_satm = a16(sizeof(unsigned) * nseg);
+        const size_t b_nv = a16(sizeof(int) * nst), b_fin = a16(sizeof(unsigned) * nst * sw);
+        const size_t b_ru = a16(sizeof(int2) * (size_t)nray);
+        CK(x->rs_seg.reserve(b_eps + b_satm + b_nv + b_fin + b_ru));
+        char* sp = x->rs_seg.as<char>();
+        seg_base = reinterpret_cast<float*>(sp);
+        seg_satm = reinterpret_cast<unsigned*>(sp + b_eps);
+        seg_nvalid = reinterpret_cast<int*>(sp + b_eps + b_satm);
+        seg_final = reinterpret_cast<unsigned*>(sp + b_eps + b_satm + b_nv);
+        int2* d_reuse = reinterpret_cast<int2*>(sp + b_eps + b_satm + b_nv + b_fin);
+        CK(cudaMemcpyAsync(d_reuse, reuse.data(), sizeof(int2) * (size_t)nray, cudaMemcpyHostToDevice, s));
+        seg_reuse = d_reuse;
+      }
       CK(cudaStreamSynchronize(s));  // the host lists go out of scope
       tfirst = (nbase_rays + 31) / 32;
     }
@@ -592,7 +659,9 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
     const int* keys = L.count;
     if (rs) {
       k_resume_keys<<<(nray + 255) / 256, 256, 0, s>>>(nray, nbase_rays, c.nd, b.mask, b.skip_masked,
-                                                        L.count, rstart, x->tiles_keys.as<int>());
+                                                        L.count, rstart,
+                                                        share_emitters ? rs->pert : nullptr,
+                                                        b.ray_obs, x->tiles_keys.as<int>());
       keys = x->tiles_keys.as<int>();
     } else if (b.skip_masked) {
       k_mask_keys<<<(nray + 255) / 256, 256, 0, s>>>(nray, c.nd, b.mask, L.count,
@@ -650,12 +719,18 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
       Pm.snap_ip = snap_ip;
       Pm.snap_ray = snap_ray;
       Pm.snap = x->rs_snap.as<float>();
+      Pm.seg_base = seg_base;
+      Pm.seg_satm = seg_satm;
+      Pm.seg_nvalid = seg_nvalid;
+      Pm.seg_final = seg_final;
       CK(cudaEventRecord(x->ev[4], s));
       Pm.tile0 = 0;
       Pm.tile1 = tfirst;
+      Pm.reuse = nullptr;       // the bases write their emitters' values
       launch_path_resume(c, T, ch, bo, L, Pm, s);
       Pm.tile0 = tfirst;
       Pm.tile1 = ntile;
+      Pm.reuse = seg_reuse;     // the perturbations read them
       launch_path_resume(c, T, ch, bo, L, Pm, s);
       launches += 9;
       x->stats.resume_skip = resume_skip;
@@ -1052,6 +1127,7 @@ int fd_core(jgb_ctx* x, const FdLayout& H, const FdInput& in, const std::vector<
       rsp.ray_off = x->kx_rayoff.as<int>();
       rsp.h_ray_off = eoff_r.data();
       rsp.h_base_obs = ebase.data();
+      rsp.h_pert = pert.data();
       x->resume = &rsp;
     }
     int rc = run_core(x, b, precision, false);
@@ -1367,7 +1443,7 @@ int jgb_set_table(jgb_ctx* x, int id, int ig, int np, const double* p, const int
 
 int jgb_set_fd_resume(jgb_ctx* x, int mode) {
   jgb::CtxLock lock(x);
-  if (!x || mode < 0 || mode > 2) return fail(x, JGB_ERR_ARG, "bad resume setting");
+  if (!x || mode < 0 || mode > 3) return fail(x, JGB_ERR_ARG, "bad resume setting");
   x->fd_resume = mode;
   return JGB_OK;
 }

@@ -48,6 +48,7 @@ struct ResumeSpec {
   const int* ray_off;    // device, ray offsets of the batch
   const int* h_ray_off;  // host copies
   const int* h_base_obs;
+  const int4* h_pert;
 };
 
 struct jgb_ctx {
@@ -97,7 +98,7 @@ struct jgb_ctx {
   int fd_resume = 1;      // resume perturbed paths from their base's state: 0 never,
                           // 1 when the estimated schedule is shorter, 2 always
   const ResumeSpec* resume = nullptr;  // set by fd_core for the run_core call it makes
-  jgb::DevBuf rs_start, rs_lists, rs_snap, rs_base;
+  jgb::DevBuf rs_start, rs_lists, rs_snap, rs_base, rs_seg, rs_reuse;
   int sms = 152;          // multiprocessors of the device
   jgb::DevBuf seg;        // segment emissivities and flags of the split path
   std::vector<float> tune_ms;

@@ -68,6 +68,22 @@ struct MixedPlan {
   const int* snap_ip;
   const int* snap_ray;
   float* snap;          // [nray][nd][kStateWords * ng + 3]
+  // resumed launches, emitters shared with the base ray: a perturbation of
+  // one emitter's mixing ratio (or of an extinction) leaves the other
+  // emitters' inputs and path states equal to the base's.  The base launch
+  // (reuse == nullptr) writes every emitter's segment emissivity at
+  // seg_base[((L.off[rb] + ip) * nd + id) * ng + g] and the emitters'
+  // saturation flags as bits of seg_satm[(L.off[rb] + ip) * nd + id], the
+  // points it walked in seg_nvalid[rb * nd + id] and its final emitter states
+  // at seg_final[(rb * nd + id) * kStateWords * ng]; a perturbed ray r with
+  // reuse[r] = {rb, pg}, rb >= 0, takes every emitter but pg (pg < 0: all)
+  // from there while ip < nvalid and continues from the base's final states
+  // after that.  nullptr seg_base: nothing shared.
+  float* seg_base;
+  unsigned* seg_satm;
+  int* seg_nvalid;
+  unsigned* seg_final;
+  const int2* reuse;
 };
 int mixed_nfield(const CtlDev& c, unsigned brmask);
 void launch_pack_tiles_n(const CtlDev& c, const TblDev& T, const LosDev& L, const MixedPlan& P,

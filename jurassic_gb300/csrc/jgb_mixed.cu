@@ -450,7 +450,7 @@ __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, float 
 // RESUME: rays start at P.start[r] from a saved state and save states for
 // other rays (finite-difference perturbations that leave a path prefix
 // unchanged); the arithmetic of every point is the same.
-template <int MINB, bool CGA, bool SPLIT = false, bool RESUME = false>
+template <int MINB, bool CGA, bool SPLIT = false, bool RESUME = false, bool SHARE = false>
 __global__ void __launch_bounds__(kPathThreads, MINB) k_path_mixed(CtlDev c, TblDev T, ChanDev ch,
                                                           BatchDev b, LosDev L, MixedPlan P,
                                                           float* refl) {
@@ -597,6 +597,20 @@ __global__ void __launch_bounds__(kPathThreads, MINB) k_path_mixed(CtlDev c, Tbl
     se = P.snap_off[r + 1];
   }
 
+  // emitters shared with the base ray (see MixedPlan): rb >= 0 takes every
+  // emitter but pg from the base while ip < nvalid; a base lane writes them
+  const bool seg_write = SHARE && P.reuse == nullptr && r >= 0 && n > 0;
+  int rb = -1, pg = -1, nvalid = 0;
+  if (SHARE && P.reuse != nullptr && r >= 0 && n > 0) {
+    const int2 ru = P.reuse[r];
+    rb = ru.x;
+    pg = ru.y;
+    if (rb >= 0) nvalid = P.seg_nvalid[(long long)rb * c.nd + id];
+  }
+  int walked = n;  // points this lane walked (a base lane records it)
+  // LOS offset of the base ray whose entries this lane writes or reads
+  const long long soff = !SHARE ? 0 : rb >= 0 ? L.off[rb] : seg_write ? L.off[r] : 0;
+
   // resumed lanes join the warp's walk at their own start point: every
   // iteration reads one point of the tile for all lanes (coalesced)
   int ip0 = start;
@@ -609,9 +623,24 @@ __global__ void __launch_bounds__(kPathThreads, MINB) k_path_mixed(CtlDev c, Tbl
     // opaque from here on: the rest of the path adds at most max(src) tau,
     // below 1e-10 of the radiance (not with surface reflection, whose sum
     // needs every point)
-    if (tau < kTauStop && !do_refl) break;
+    if (tau < kTauStop && !do_refl) {
+      walked = ip;
+      break;
+    }
     if (RESUME)
       for (; sn < se && P.snap_ip[sn] == ip; sn++) snap_write(P.snap_ray[sn]);
+    // the base stopped here: the shared emitters continue from its final states
+    if (SHARE && rb >= 0 && ip == nvalid) {
+      const unsigned* q = P.seg_final + ((long long)rb * c.nd + id) * sw;
+      for (int g2 = 0; g2 < ng; g2++)
+        if (g2 != pg)
+          for (int k = 0; k < kStateWords; k++)
+            sh_state[(g2 * kStateWords + k) * nth + tid] = q[g2 * kStateWords + k];
+    }
+    const bool shared = SHARE && rb >= 0 && ip < nvalid;
+    const long long sbase = SHARE ? (soff + ip) * c.nd + id : 0;
+    const unsigned satm_in = shared ? P.seg_satm[sbase] : 0u;
+    unsigned satm_out = 0u;
     const float* f = base + (long long)ip * F.n * 32;
     const float p = f[F.p * 32], t = f[F.t * 32], ds = f[F.ds * 32];
     float E = 0.f;
@@ -623,6 +652,9 @@ __global__ void __launch_bounds__(kPathThreads, MINB) k_path_mixed(CtlDev c, Tbl
         const long long o = seg0 + ip * segstride + g * 32;
         eg = P.seg_eps[o];
         if (P.seg_sat[o]) sat = true;
+      } else if (SHARE && shared && g != pg) {
+        eg = P.seg_base[sbase * ng + g];
+        if ((satm_in >> g) & 1u) sat = true;
       } else {
         constexpr int es = kEmitterFields(CGA), kb = kFBr(CGA);
         const float* fg = f + (F.g0 + g * es) * 32;
@@ -637,11 +669,18 @@ __global__ void __launch_bounds__(kPathThreads, MINB) k_path_mixed(CtlDev c, Tbl
         const float wtb = brg ? fg[(kb + 3) * 32] : 0.f;
         GasState st = sload(g, brg);
         const long long dg = dg0 + g;  // (channel, emitter)
-        eg = gas_eps_f<CGA>(T, dg, pq, tq, du, ucg, brw, wpre, wta, wtb, st, sat);
+        bool sg = false;
+        eg = gas_eps_f<CGA>(T, dg, pq, tq, du, ucg, brw, wpre, wta, wtb, st, sg);
         sstore(g, st, brg);
+        if (sg) sat = true;
+        if (SHARE && seg_write) {
+          P.seg_base[sbase * ng + g] = eg;
+          if (sg) satm_out |= 1u << g;
+        }
       }
       E = E + (1.f - E) * eg;
     }
+    if (SHARE && seg_write) P.seg_satm[sbase] = satm_out;
     // extinction and continua
     float beta = c.nw > 0 ? f[(F.kw0 + w) * 32] : 0.f;
     if (has_cloud) beta += f[F.aux * 32] * kthr[0];
@@ -699,6 +738,11 @@ __global__ void __launch_bounds__(kPathThreads, MINB) k_path_mixed(CtlDev c, Tbl
   // opaque earlier hands its final state on, so the resumed rays stop too)
   if (RESUME)
     for (; sn < se; sn++) snap_write(P.snap_ray[sn]);
+  if (SHARE && seg_write) {  // what a perturbed ray needs past this walk
+    P.seg_nvalid[(long long)r * c.nd + id] = walked;
+    unsigned* q = P.seg_final + ((long long)r * c.nd + id) * sw;
+    for (int k = 0; k < sw; k++) q[k] = sh_state[k * nth + tid];
+  }
   if (r < 0) return;
 
   const double nud2 = ch.nu[id];
@@ -956,16 +1000,18 @@ void launch_path_resume(const CtlDev& c, const TblDev& T, const ChanDev& ch, con
   if (nblk == 0) return;
   const size_t smem = sizeof(unsigned) * kStateWords * kPathThreads * (size_t)(c.ng > 0 ? c.ng : 1) +
                       sizeof(float) * (4 * kChanConsts + kThreadFloats * kPathThreads);
+  auto go = [&](auto kern) {
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<nblk, kPathThreads, smem, s>>>(c, T, ch, b, L, P, nullptr);
+  };
+  const bool share = P.seg_base != nullptr;
   if (c.formod == 0) {
-    if (smem > 48 * 1024)
-      cudaFuncSetAttribute(k_path_mixed<8, true, false, true>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_path_mixed<8, true, false, true><<<nblk, kPathThreads, smem, s>>>(c, T, ch, b, L, P, nullptr);
+    if (share) go(k_path_mixed<8, true, false, true, true>);
+    else go(k_path_mixed<8, true, false, true, false>);
   } else {
-    if (smem > 48 * 1024)
-      cudaFuncSetAttribute(k_path_mixed<8, false, false, true>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_path_mixed<8, false, false, true><<<nblk, kPathThreads, smem, s>>>(c, T, ch, b, L, P, nullptr);
+    if (share) go(k_path_mixed<8, false, false, true, true>);
+    else go(k_path_mixed<8, false, false, true, false>);
   }
 }
 

@@ -248,7 +248,8 @@ class Context:
     def set_fd_resume(self, mode: int):
         """Resume perturbed paths of mixed Jacobians from their base's saved
         state: 1 when the estimated schedule is shorter (default), 2 always,
-        0 never (the results do not depend on it)."""
+        0 never; 3 always, with the emitters a perturbation leaves unchanged
+        always taken from the base (the results do not depend on it)."""
         self._check(load().jgb_set_fd_resume(self.h, int(mode)))
 
     def _check(self, rc):

@@ -4,9 +4,13 @@ GPU.
 A perturbation of a level value changes the atmosphere only on the two
 intervals next to the level, so the perturbed ray's LOS points and path
 state equal its unperturbed base's until the ray comes near those levels;
-the perturbed path restarts there from the base's saved state.  The
-Jacobians (and a whole retrieval) are bit-identical with and without it:
-nadir with masked channels, refracted limb EGA, limb CGA.
+the perturbed path restarts there from the base's saved state.  A
+perturbation of one emitter's mixing ratio also leaves the other emitters'
+states equal to the base's all along the path, so their segment
+emissivities can be taken from the base's walk.  The Jacobians (and a whole
+retrieval) are bit-identical in every mode -- resumed with emitters always
+shared (mode 3), resumed (2, sharing where it pays), plain (0), automatic
+(1): nadir with masked channels, refracted limb EGA, limb CGA.
 """
 import copy
 
@@ -23,7 +27,7 @@ def _both(ctx, batch):
     """Jacobians resumed (forced) and plain; the resumed call must have
     skipped LOS points."""
     out = []
-    for mode in (2, 0, 1):
+    for mode in (3, 2, 0, 1):
         ctx.set_fd_resume(mode)
         Ks, fm = ctx.kernel_batch(batch.fresh_outputs(), native.MIXED)
         out.append(Ks)
@@ -34,12 +38,12 @@ def _both(ctx, batch):
 
 
 def _same(res):
-    (Ka, Kb, Kc), skip = res
+    (Kd, Ka, Kb, Kc), skip = res
     assert skip > 0.05
-    assert len(Ka) == len(Kb) == len(Kc)
-    for a, b, c in zip(Ka, Kb, Kc):
+    assert len(Ka) == len(Kb) == len(Kc) == len(Kd)
+    for a, b, c, d in zip(Ka, Kb, Kc, Kd):
         assert a.shape == b.shape
-        assert np.array_equal(a, b) and np.array_equal(a, c)
+        assert np.array_equal(a, b) and np.array_equal(a, c) and np.array_equal(a, d)
         assert np.all(np.isfinite(a))
 
 
@@ -88,10 +92,11 @@ def test_resume_retrieval_identical(built_lib, built_oracle):
               err_q_ch=np.array([-999.0, 500.0]))
     ctx = native.Context(ctl, w.tables, w.filters)
     res = []
-    for mode in (2, 0):
+    for mode in (3, 2, 0):
         ctx.set_fd_resume(mode)
         res.append(ctx.engine(ret, native.MIXED).run(synth.pack(ctl, items)))
-    for a, b in zip(*res):
+    for a, b, c in zip(*res):
         for k in ("x", "costs", "rad", "tau", "cov", "avk"):
             assert np.array_equal(np.asarray(a[k]), np.asarray(b[k]), equal_nan=True), k
-        assert a["iters"] == b["iters"] and a["status"] == b["status"] == 0
+            assert np.array_equal(np.asarray(a[k]), np.asarray(c[k]), equal_nan=True), k
+        assert a["iters"] == b["iters"] == c["iters"] and a["status"] == b["status"] == 0
