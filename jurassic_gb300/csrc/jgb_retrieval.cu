@@ -44,6 +44,12 @@ struct RetDesc {
   long long xo, yo, so, ko;   // offsets: state vectors, measurement vectors, n*n, m*n
 };
 
+// sum over the 32 lanes of a warp (butterfly: every lane gets the same sum)
+__device__ __forceinline__ double warp_sum_d(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 // ---------------------------------------------------------------------------
 // state <-> atmosphere (atm2x / x2atm, jurassic.c:29-104, 5896-5958)
 
@@ -140,25 +146,43 @@ __global__ void k_residuals(int nret, const RetDesc* d, const int* active, const
   for (int r = threadIdx.x; r < d[i].m; r += blockDim.x) dy[d[i].yo + r] = ym[d[i].yo + r] - yv[d[i].yo + r];
 }
 
-// chi^2/m (cost_function, retrieval.c:340-369): serial sums in the
-// reference's order, one thread per retrieval.
+// chi^2/m (cost_function, retrieval.c:340-369), one block per retrieval:
+// chi_m = sum_k (w_k dy_k)^2 and chi_a = sum_a dx_a (S_a^-1 dx)_a, a warp per
+// row of S_a^-1 (lanes along the row) and per stretch of dy, the partial
+// sums combined in a fixed order (deterministic).
 __global__ void k_cost(int nret, const RetDesc* d, const int* active, const double* dx,
                        const double* dy, const double* sainv, const double* w, double* chisq) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.x;
   if (i >= nret || !active[i]) return;
   const RetDesc r = d[i];
-  double chim = 0, chia = 0;
-  for (int k = 0; k < r.m; k++) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  __shared__ double part_m[32], part_a[32];
+  double pm = 0, pa = 0;
+  for (int k = threadIdx.x; k < r.m; k += blockDim.x) {
     const double v = dy[r.yo + k] * w[r.yo + k];
-    chim += v * v;
+    pm += v * v;
   }
+  pm = warp_sum_d(pm);
   const double* S = sainv + r.so;
-  for (int a = 0; a < r.n; a++) {
+  for (int a = warp; a < r.n; a += nwarp) {
     double s = 0;
-    for (int b = 0; b < r.n; b++) s += S[(long long)a * r.n + b] * dx[r.xo + b];
-    chia += dx[r.xo + a] * s;
+    for (int b = lane; b < r.n; b += 32) s += S[(long long)a * r.n + b] * dx[r.xo + b];
+    s = warp_sum_d(s);
+    pa += dx[r.xo + a] * s;
   }
-  chisq[i] = (chim + chia) / (double)r.m;
+  if (lane == 0) {
+    part_m[warp] = pm;
+    part_a[warp] = pa;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double chim = 0, chia = 0;
+    for (int k = 0; k < nwarp; k++) {
+      chim += part_m[k];
+      chia += part_a[k];
+    }
+    chisq[i] = (chim + chia) / (double)r.m;
+  }
 }
 
 // b = -S_a^-1 dx + K^T W dy (retrieval.c:573-577)
@@ -187,32 +211,46 @@ __global__ void k_lm_matrix(int nret, const RetDesc* d, const int* active, const
     A[r.so + e] = sainv[r.so + e] * (1 + lmpar[i]) + cov[r.so + e];
 }
 
-// In-place Cholesky factor (lower triangle, mirrored into the upper one),
-// one block per retrieval; dot products are serial per entry so the result
-// is the textbook column algorithm's.  status[i] = 1 if not positive definite.
+// In-place Cholesky factor (lower triangle, mirrored into the upper one;
+// gsl_linalg_cholesky_decomp of matrix_invert / the LM step, retrieval.c:
+// 373-399, 588-589), one block per retrieval.  Column j: warp 0 forms the
+// diagonal L_jj = sqrt(A_jj - sum_k L_jk^2), then every warp takes rows
+// r > j in turn, L_rj = (A_rj - sum_k L_rk L_jk) / L_jj, the 32 lanes of a
+// warp summing over k < j along the two rows (coalesced) and reducing by
+// shuffles.  status[i] = 1 if not positive definite.
 __global__ void k_chol_factor(int nret, const RetDesc* d, const int* active, double* Aall,
                               int* status) {
   const int i = blockIdx.x;
   if (i >= nret || !active[i]) return;
   const int n = d[i].n;
   double* A = Aall + d[i].so;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   __shared__ double ljj;
   __shared__ int bad;
   if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
   for (int j = 0; j < n; j++) {
-    if (threadIdx.x == 0) {
-      double s = A[(long long)j * n + j];
-      for (int k = 0; k < j; k++) s -= A[(long long)j * n + k] * A[(long long)j * n + k];
-      if (!(s > 0)) bad = 1;
-      ljj = sqrt(s);
-      A[(long long)j * n + j] = ljj;
+    const double* Aj = A + (long long)j * n;
+    if (warp == 0) {
+      double s = 0;
+      for (int k = lane; k < j; k += 32) s += Aj[k] * Aj[k];
+      s = warp_sum_d(s);
+      if (lane == 0) {
+        const double dj = Aj[j] - s;
+        if (!(dj > 0)) bad = 1;
+        ljj = sqrt(dj);
+        A[(long long)j * n + j] = ljj;
+      }
     }
     __syncthreads();
     if (bad) break;
-    for (int r = j + 1 + threadIdx.x; r < n; r += blockDim.x) {
-      double s = A[(long long)r * n + j];
-      for (int k = 0; k < j; k++) s -= A[(long long)r * n + k] * A[(long long)j * n + k];
-      A[(long long)r * n + j] = s / ljj;
+    const double lj = ljj;
+    for (int r = j + 1 + warp; r < n; r += nwarp) {
+      const double* Ar = A + (long long)r * n;
+      double s = 0;
+      for (int k = lane; k < j; k += 32) s += Ar[k] * Aj[k];
+      s = warp_sum_d(s);
+      if (lane == 0) A[(long long)r * n + j] = (Ar[j] - s) / lj;
     }
     __syncthreads();
   }
@@ -241,12 +279,40 @@ __device__ void chol_solve_serial(const double* L, int n, const double* b, doubl
   }
 }
 
-// step = A^-1 b from the factor (retrieval.c:589), one thread per retrieval
+// step = A^-1 b from the factor (gsl_linalg_cholesky_solve, retrieval.c:
+// 589), one block per retrieval, the vector in shared memory (n doubles).
+// Forward L y = b by column sweeps: once y_r is final, every thread
+// subtracts L_kr y_r from its rows k > r, so each row sees its subtractions
+// in the serial order.  Backward L^T x = y the same way from the last row.
+// L's upper triangle holds L^T (k_chol_factor mirrors it), so both sweeps
+// read rows of the matrix, coalesced.
 __global__ void k_chol_solve(int nret, const RetDesc* d, const int* active, const double* L,
                              const double* b, double* step) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.x;
   if (i >= nret || !active[i]) return;
-  chol_solve_serial(L + d[i].so, d[i].n, b + d[i].xo, step + d[i].xo, 1);
+  const int n = d[i].n;
+  const double* Li = L + d[i].so;
+  extern __shared__ double xs[];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int r = tid; r < n; r += nt) xs[r] = b[d[i].xo + r];
+  __syncthreads();
+  for (int r = 0; r < n; r++) {
+    const double* row = Li + (long long)r * n;   // row r: L_rk for k < r, L_kr for k > r
+    const double yr = xs[r] / row[r];
+    for (int k = r + 1 + tid; k < n; k += nt) xs[k] -= row[k] * yr;
+    __syncthreads();
+    if (tid == 0) xs[r] = yr;
+    __syncthreads();
+  }
+  for (int r = n - 1; r >= 0; r--) {
+    const double* row = Li + (long long)r * n;
+    const double xr = xs[r] / row[r];
+    for (int k = tid; k < r; k += nt) xs[k] -= row[k] * xr;
+    __syncthreads();
+    if (tid == 0) xs[r] = xr;
+    __syncthreads();
+  }
+  for (int r = tid; r < n; r += nt) step[d[i].xo + r] = xs[r];
 }
 
 // Inverse from the factor: column solves of L L^T X = I, symmetrised
@@ -1021,7 +1087,7 @@ int init_requests(jgb_engine* E, WorkSet& w, const std::vector<int>& F) {
   rc = put_flags(E, w, F);
   if (rc) return rc;
   k_residuals<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, w.xi, w.xa, w.ym, w.yi, w.dx, w.dy);
-  k_cost<<<(nret + 63) / 64, 64, 0, s>>>(nret, w.desc_d, w.active, w.dx, w.dy, w.sainv, w.w, w.chisq);
+  k_cost<<<nret, 256, 0, s>>>(nret, w.desc_d, w.active, w.dx, w.dy, w.sainv, w.w, w.chisq);
   std::vector<double> chisq(nret);
   std::vector<int> st(nret);
   ECK(cudaMemcpyAsync(chisq.data(), w.chisq, sizeof(double) * nret, cudaMemcpyDeviceToHost, s));
@@ -1115,7 +1181,13 @@ int trial_round(jgb_engine* E, WorkSet& w, std::vector<int>& trying, std::vector
   ECK(cudaMemcpyAsync(cw.lmpar, lam.data(), sizeof(double) * nc, cudaMemcpyHostToDevice, s));
   k_lm_matrix<<<dim3(64, nc), 256, 0, s>>>(nc, cw.desc_d, cw.active, cw.lmpar, cw.sainv, cw.cov, cw.Amat);
   k_chol_factor<<<nc, 256, 0, s>>>(nc, cw.desc_d, cw.active, cw.Amat, cw.status);
-  k_chol_solve<<<(nc + 63) / 64, 64, 0, s>>>(nc, cw.desc_d, cw.active, cw.Amat, cw.bvec, cw.step);
+  int nmax = 1;
+  for (int k = 0; k < nc; k++) nmax = std::max(nmax, cw.desc[k].n);
+  const size_t solve_smem = sizeof(double) * (size_t)nmax;
+  if (solve_smem > 48 * 1024)
+    ECK(cudaFuncSetAttribute(k_chol_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)solve_smem));
+  k_chol_solve<<<nc, 128, solve_smem, s>>>(nc, cw.desc_d, cw.active, cw.Amat, cw.bvec, cw.step);
   std::vector<int> fc(2 * (size_t)nq);
   for (int r = 0; r < nq; r++) {
     fc[r] = first[r];
@@ -1141,7 +1213,7 @@ int trial_round(jgb_engine* E, WorkSet& w, std::vector<int>& trying, std::vector
     E->st.trial_path_ms += b;
   }
   k_residuals<<<nc, 128, 0, s>>>(nc, cw.desc_d, cw.active, cw.xi, cw.xa, cw.ym, cw.yi, cw.dx, cw.dy);
-  k_cost<<<(nc + 63) / 64, 64, 0, s>>>(nc, cw.desc_d, cw.active, cw.dx, cw.dy, cw.sainv, cw.w, cw.chisq);
+  k_cost<<<nc, 256, 0, s>>>(nc, cw.desc_d, cw.active, cw.dx, cw.dy, cw.sainv, cw.w, cw.chisq);
   std::vector<double> cnew(nc);
   std::vector<int> st(nc);
   ECK(cudaMemcpyAsync(cnew.data(), cw.chisq, sizeof(double) * nc, cudaMemcpyDeviceToHost, s));
