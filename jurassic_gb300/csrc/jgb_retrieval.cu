@@ -316,20 +316,31 @@ __global__ void k_chol_solve(int nret, const RetDesc* d, const int* active, cons
 }
 
 // Inverse from the factor: column solves of L L^T X = I, symmetrised
-// (matrix_invert, retrieval.c:373-399, non-diagonal branch).
-__global__ void k_chol_inverse(int nret, const RetDesc* d, const int* active, const double* L,
-                               double* work, double* out) {
-  const int i = blockIdx.x;
+// (matrix_invert, retrieval.c:373-399, non-diagonal branch).  The column
+// solves are independent: thread c of the block (blockIdx.x, i) solves for
+// column blockIdx.x * blockDim.x + c (its loads of X run along rows across
+// the threads, L is read by all threads alike), so a retrieval's columns
+// spread over several blocks; k_sym_half then forms (X + X^T) / 2.
+__global__ void k_chol_inverse_cols(int nret, const RetDesc* d, const int* active,
+                                    const double* L, double* work) {
+  const int i = blockIdx.y;
   if (i >= nret || !active[i]) return;
   const int n = d[i].n;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
   double* W = work + d[i].so;
-  for (int c = threadIdx.x; c < n; c += blockDim.x) {
-    // solve for unit vector e_c, stored in column c of W (stride n)
-    for (int r = 0; r < n; r++) W[(long long)r * n + c] = (r == c) ? 1.0 : 0.0;
-    chol_solve_serial(L + d[i].so, n, W + c, W + c, n);
-  }
-  __syncthreads();
-  for (long long e = threadIdx.x; e < (long long)n * n; e += blockDim.x) {
+  for (int r = 0; r < n; r++) W[(long long)r * n + c] = (r == c) ? 1.0 : 0.0;
+  chol_solve_serial(L + d[i].so, n, W + c, W + c, n);
+}
+
+__global__ void k_sym_half(int nret, const RetDesc* d, const int* active, const double* work,
+                           double* out) {
+  const int i = blockIdx.y;
+  if (i >= nret || !active[i]) return;
+  const int n = d[i].n;
+  const double* W = work + d[i].so;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < (long long)n * n;
+       e += (long long)gridDim.x * blockDim.x) {
     const int r = (int)(e / n), c = (int)(e % n);
     out[d[i].so + e] = 0.5 * (W[(long long)r * n + c] + W[(long long)c * n + r]);
   }
@@ -983,6 +994,17 @@ int build_workset(jgb_engine* E, WorkSet& w, WorkSet* old, const std::vector<Req
   return JGB_OK;
 }
 
+// Inverse of every flagged retrieval's matrix from its Cholesky factor L
+// (matrix_invert): the column solves spread over blocks of 64 columns, then
+// the symmetrised result in out.
+void chol_inverse(int nret, const WorkSet& w, const double* L, double* work, double* out,
+                  cudaStream_t s) {
+  int nmax = 1;
+  for (int i = 0; i < nret; i++) nmax = std::max(nmax, w.desc[i].n);
+  k_chol_inverse_cols<<<dim3((nmax + 63) / 64, nret), 64, 0, s>>>(nret, w.desc_d, w.active, L, work);
+  k_sym_half<<<dim3(16, nret), 256, 0, s>>>(nret, w.desc_d, w.active, work, out);
+}
+
 int put_flags(jgb_engine* E, WorkSet& w, const std::vector<int>& f) {
   ECK(cudaMemcpyAsync(w.active, f.data(), sizeof(int) * w.nret, cudaMemcpyHostToDevice, E->x->stream));
   return JGB_OK;
@@ -1081,8 +1103,8 @@ int init_requests(jgb_engine* E, WorkSet& w, const std::vector<int>& F) {
     rc = put_flags(E, w, nondiag);
     if (rc) return rc;
     k_select_nn<<<dim3(16, nret), 256, 0, s>>>(nret, w.desc_d, w.active, w.sainv, w.work);
-    k_chol_factor<<<nret, 256, 0, s>>>(nret, w.desc_d, w.active, w.work, w.status);
-    k_chol_inverse<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, w.work, w.Amat, w.sainv);
+    k_chol_factor<<<nret, 1024, 0, s>>>(nret, w.desc_d, w.active, w.work, w.status);
+    chol_inverse(nret, w, w.work, w.Amat, w.sainv, s);
   }
   rc = put_flags(E, w, F);
   if (rc) return rc;
@@ -1180,7 +1202,7 @@ int trial_round(jgb_engine* E, WorkSet& w, std::vector<int>& trying, std::vector
   if (rc) return rc;
   ECK(cudaMemcpyAsync(cw.lmpar, lam.data(), sizeof(double) * nc, cudaMemcpyHostToDevice, s));
   k_lm_matrix<<<dim3(64, nc), 256, 0, s>>>(nc, cw.desc_d, cw.active, cw.lmpar, cw.sainv, cw.cov, cw.Amat);
-  k_chol_factor<<<nc, 256, 0, s>>>(nc, cw.desc_d, cw.active, cw.Amat, cw.status);
+  k_chol_factor<<<nc, 1024, 0, s>>>(nc, cw.desc_d, cw.active, cw.Amat, cw.status);
   int nmax = 1;
   for (int k = 0; k < nc; k++) nmax = std::max(nmax, cw.desc[k].n);
   const size_t solve_smem = sizeof(double) * (size_t)nmax;
@@ -1398,8 +1420,8 @@ int finish_requests(jgb_engine* E, WorkSet& w) {
     if (rc) return rc;
     ECK(cudaMemsetAsync(w.status, 0, sizeof(int) * nret, s));
     k_add_nn<<<dim3(16, nret), 256, 0, s>>>(nret, w.desc_d, w.active, w.sainv, w.covn);
-    k_chol_factor<<<nret, 256, 0, s>>>(nret, w.desc_d, w.active, w.covn, w.status);
-    k_chol_inverse<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, w.covn, w.work, w.Amat);
+    k_chol_factor<<<nret, 1024, 0, s>>>(nret, w.desc_d, w.active, w.covn, w.status);
+    chol_inverse(nret, w, w.covn, w.work, w.Amat, s);
     k_gain<<<dim3(64, nret), 256, 0, s>>>(nret, w.desc_d, w.active, w.Amat, w.Kd, w.w, w.G);
     k_sqrt_diag<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, w.Amat, w.e_tot);
     k_err_diag<<<nret, 128, 0, s>>>(nret, w.desc_d, w.active, w.G, w.sn, w.e_noise);
