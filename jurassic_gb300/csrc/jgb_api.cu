@@ -180,14 +180,26 @@ __global__ void k_iota(int n, int* v) {
 }
 
 // tile plan from the rays in sort order (descending key): the first nfirst
-// rays fill tiles [0, tfirst), the others start a new tile (two groups that
-// never share a tile; nfirst = nray, tfirst = ntile: one group)
-__global__ void k_tiles(int nray, int ntile, int nfirst, int tfirst, const int* count,
-                        const int* sorted_ray, int* perm, int* tlen, long long* tpts) {
+// rays fill tiles [0, tfirst), the next nsecond - nfirst tiles [tfirst,
+// tsecond), the others start a new tile again (three groups that never share
+// a tile; nsecond = nfirst, tsecond = tfirst: two; nfirst = nray, tfirst =
+// ntile: one)
+__global__ void k_tiles(int nray, int ntile, int nfirst, int tfirst, int nsecond, int tsecond,
+                        const int* count, const int* sorted_ray, int* perm, int* tlen,
+                        long long* tpts) {
   const int tile = blockIdx.x * blockDim.x + threadIdx.x;
   if (tile >= ntile) return;
-  const int k0 = tile < tfirst ? tile * 32 : nfirst + (tile - tfirst) * 32;
-  const int k1 = tile < tfirst ? min(k0 + 32, nfirst) : min(k0 + 32, nray);
+  int k0, k1;
+  if (tile < tfirst) {
+    k0 = tile * 32;
+    k1 = min(k0 + 32, nfirst);
+  } else if (tile < tsecond) {
+    k0 = nfirst + (tile - tfirst) * 32;
+    k1 = min(k0 + 32, nsecond);
+  } else {
+    k0 = nsecond + (tile - tsecond) * 32;
+    k1 = min(k0 + 32, nray);
+  }
   int mx = 0;
   for (int l = 0; l < 32; l++) {
     const int k = k0 + l;
@@ -239,10 +251,12 @@ __global__ void k_resume_points(int nray, BatchDev b, LosDev L, int nbase, const
 }
 
 // Sort key of a resumed batch: bases first (their tiles run first and save
-// the states), then by measured channels, by perturbation class (below), by
-// the LOS points left to do in 64-point buckets (longest first, so that no
-// long warp is left for the end) and by start point in 16-point buckets (so
-// that the lanes of a warp walk nearly the same range of points).
+// the states), then by perturbation class (below: the perturbations that
+// cannot share emitters, class 15, before those that can, so that the two
+// form separate tile ranges), by measured channels, by the LOS points left
+// to do in 64-point buckets (longest first, so that no long warp is left for
+// the end) and by start point in 16-point buckets (so that the lanes of a
+// warp walk nearly the same range of points).
 // The perturbation class follows the channels: the perturbations of one
 // emitter's mixing ratio (class 1 + emitter) and of extinctions (class 0)
 // compute only that emitter (none) and take the others from their base, so
@@ -263,7 +277,7 @@ __global__ void k_resume_keys(int nray, int nbase_rays, int nd, const unsigned c
     const int4 pr = pert[ray_obs[r]];
     cls = pr.x == 2 ? 1 + min(pr.y, 13) : pr.x == 3 ? 0 : 15;
   }
-  key[r] = ((r < nbase_rays ? 1 : 0) << 30) | (min(m, 511) << 21) | (cls << 17) |
+  key[r] = ((r < nbase_rays ? 1 : 0) << 30) | (cls << 26) | (min(m, 511) << 17) |
            (min(left >> 6, 127) << 10) | (min(start[r] >> 4, 255) << 2);
 }
 
@@ -475,6 +489,7 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
     const ResumeSpec* rs = x->resume;
     const int nchb = (c.nd + 3) / 4;
     int nbase_rays = nray, tfirst = 0;
+    int nplain_end = nray, tsecond = 0;  // resumed: end of the rays that share no emitter
     double resume_skip = 0.0;
     int* rstart = nullptr;
     int *snap_off = nullptr, *snap_ip = nullptr, *snap_ray = nullptr;
@@ -546,9 +561,9 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
       for (int r = 0; r < nray; r++) ord[r] = r;
       std::stable_sort(ord.begin(), ord.end(), [&](int a, int b2) { return hk[a] > hk[b2]; });
       const double t_res = group_time(ord, 0, nbase_rays, false) + group_time(ord, nbase_rays, nray, true);
-      // the plain plan: measured channels (key bits 21-29), then LOS length
+      // the plain plan: measured channels (key bits 17-25), then LOS length
       std::stable_sort(ord.begin(), ord.end(), [&](int a, int b2) {
-        const int ma = (hk[a] >> 21) & 511, mb = (hk[b2] >> 21) & 511;
+        const int ma = (hk[a] >> 17) & 511, mb = (hk[b2] >> 17) & 511;
         return ma != mb ? ma > mb : hc[a] > hc[b2];
       });
       const double t_plain = group_time(ord, 0, nray, false);
@@ -642,11 +657,20 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
       }
       CK(cudaStreamSynchronize(s));  // the host lists go out of scope
       tfirst = (nbase_rays + 31) / 32;
+      // the perturbations that share no emitter sort before those that do
+      int nplain = 0;
+      for (int r = nbase_rays; r < nray; r++) nplain += reuse[r].x < 0 ? 1 : 0;
+      nplain_end = nbase_rays + nplain;
+      tsecond = tfirst + (nplain + 31) / 32;
     }
     // tile plan: rays sorted by LOS length, 32 per tile (resumed batches:
-    // base tiles first)
-    const int ntile = rs ? tfirst + (nray - nbase_rays + 31) / 32 : (nray + 31) / 32;
-    if (!rs) tfirst = ntile;
+    // base tiles first, then the perturbations that share no emitter with
+    // their base, then those that do)
+    const int ntile = rs ? tsecond + (nray - nplain_end + 31) / 32 : (nray + 31) / 32;
+    if (!rs) {
+      tfirst = tsecond = ntile;
+      nplain_end = nray;
+    }
     CK(x->tiles_keys.reserve(sizeof(int) * (size_t)nray));
     CK(x->tiles_keys2.reserve(sizeof(int) * (size_t)nray));
     CK(x->tiles_vals.reserve(sizeof(int) * 2 * (size_t)nray));
@@ -684,8 +708,9 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
     Pm.toff = toff;
     Pm.tile0 = 0;
     Pm.tile1 = ntile;
-    k_tiles<<<(ntile + 127) / 128, 128, 0, s>>>(nray, ntile, rs ? nbase_rays : nray, tfirst, L.count,
-                                                 vals_out, Pm.perm, Pm.tlen, tpts);
+    k_tiles<<<(ntile + 127) / 128, 128, 0, s>>>(nray, ntile, rs ? nbase_rays : nray, tfirst,
+                                                 nplain_end, tsecond, L.count, vals_out, Pm.perm,
+                                                 Pm.tlen, tpts);
     CK(cudaMemsetAsync(toff, 0, sizeof(long long), s));
     size_t sb2 = 0;
     cub::DeviceScan::InclusiveSum(nullptr, sb2, tpts, toff + 1, ntile, s);
@@ -728,11 +753,16 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
       Pm.tile1 = tfirst;
       Pm.reuse = nullptr;       // the bases write their emitters' values
       launch_path_resume(c, T, ch, bo, L, Pm, s);
-      Pm.tile0 = tfirst;
+      MixedPlan Pp = Pm;        // perturbations that share no emitter
+      Pp.tile0 = tfirst;
+      Pp.tile1 = tsecond;
+      Pp.seg_base = nullptr;
+      launch_path_resume(c, T, ch, bo, L, Pp, s);
+      Pm.tile0 = tsecond;
       Pm.tile1 = ntile;
-      Pm.reuse = seg_reuse;     // the perturbations read them
+      Pm.reuse = seg_reuse;     // the perturbations that do read them
       launch_path_resume(c, T, ch, bo, L, Pm, s);
-      launches += 9;
+      launches += 10;
       x->stats.resume_skip = resume_skip;
     } else if (split) {
       const size_t nseg = (size_t)std::max(tile_points, 1LL) * c.nd * c.ng * 32;
