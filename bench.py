@@ -783,13 +783,15 @@ def main():
                            "parallelism": "replicas" if world > 1 else "single GPU"},
                 "stage_ms": {k: stats[k] for k in ("hydro_ms", "trace_ms", "pack_ms", "path_ms")},
                 "trace_passes": stats["trace_passes"],
-                "autotune": {"path_variant": stats["path_variant"], "variant_ms": stats["tune_ms"][:14],
+                "autotune": {"path_variant": stats["path_variant"], "variant_ms": stats["tune_ms"][:16],
                              "caps": ["no register cap", "5 blocks/SM (<=102 regs)",
                                       "6 blocks/SM (<=85 regs)", "4 blocks/SM (<=128 regs)",
                                       "8 blocks/SM (<=64 regs)", "10 blocks/SM (<=51 regs)",
                                       "12 blocks/SM (<=42 regs)"],
-                             "note": "variant v: register cap v % 7; block = 4 channels x 1 tile "
-                                     "(v < 7) or 1 channel x 4 tiles (v >= 7)"},
+                             "note": "variant v < 14: register cap v % 7; block = 4 channels x 1 "
+                                     "tile (v < 7) or 1 channel x 4 tiles (7 <= v < 14); v = 14, "
+                                     "15: block = 1 channel x 8 tiles (256 threads), <= 64 or "
+                                     "<= 51 registers"},
                 "wall_s_timed": wall,
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h), "ms_per_step": statistics.mean(e2e_ms),

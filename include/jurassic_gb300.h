@@ -96,9 +96,11 @@ typedef struct {
   long long los_points;          /* LOS points of the batch */
   int path_launches;             /* kernels launched by the last call */
   int path_variant;              /* mixed path kernel variant chosen by the autotuner:
-                                    register cap (path_variant % 7) and block shape
-                                    (path_variant / 7: 0 = 4 channels of one tile,
-                                    1 = one channel of 4 tiles) */
+                                    0-13: register cap (path_variant % 7) and block
+                                    shape (path_variant / 7: 0 = 4 channels of one
+                                    tile, 1 = one channel of 4 tiles); 14, 15: one
+                                    channel of 8 tiles (256 threads), at most 64 or
+                                    51 registers */
   float tune_ms[16];             /* autotuner timings of the variants [ms] */
   int trace_passes;              /* ray-tracing passes over the batch: 1 = one
                                     pass, 2 = count + fill, 3 = a capacity

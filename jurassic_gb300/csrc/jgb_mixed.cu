@@ -450,21 +450,23 @@ __device__ __forceinline__ float gas_eps_f(const TblDev& T, long long dg, float 
 // RESUME: rays start at P.start[r] from a saved state and save states for
 // other rays (finite-difference perturbations that leave a path prefix
 // unchanged); the arithmetic of every point is the same.
-template <int MINB, bool CGA, bool SPLIT = false, bool RESUME = false, bool SHARE = false>
-__global__ void __launch_bounds__(kPathThreads, MINB) k_path_mixed(CtlDev c, TblDev T, ChanDev ch,
+template <int MINB, bool CGA, bool SPLIT = false, bool RESUME = false, bool SHARE = false,
+          int NT = kPathThreads>
+__global__ void __launch_bounds__(NT, MINB) k_path_mixed(CtlDev c, TblDev T, ChanDev ch,
                                                           BatchDev b, LosDev L, MixedPlan P,
                                                           float* refl) {
   const int ng = c.ng;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
+  constexpr int W = NT / 32;  // warps of a block
   int tile, id;
-  if (P.tile_major) {  // one channel of 4 consecutive tiles
-    tile = P.tile0 + (int)(blockIdx.x / c.nd) * 4 + warp;
+  if (P.tile_major) {  // one channel of W consecutive tiles
+    tile = P.tile0 + (int)(blockIdx.x / c.nd) * W + warp;
     id = (int)(blockIdx.x % c.nd);
-  } else {             // 4 channels of one tile
-    const int nchb = (c.nd + 3) / 4;
+  } else {             // W channels of one tile
+    const int nchb = (c.nd + W - 1) / W;
     tile = P.tile0 + blockIdx.x / nchb;
-    id = (blockIdx.x % nchb) * 4 + warp;
+    id = (blockIdx.x % nchb) * W + warp;
   }
   if (tile >= P.tile1 || id >= c.nd) return;
   int r = P.perm[tile * 32 + lane];
@@ -502,9 +504,9 @@ __global__ void __launch_bounds__(kPathThreads, MINB) k_path_mixed(CtlDev c, Tbl
   const float st0 = (float)kTMIN, sdt = (float)((kTMAX - kTMIN) / (kNS - 1.0));
 
   // per-emitter path state in shared memory, word-major per thread:
-  // sh[(g * kStateWords + w) * kPathThreads + threadIdx.x]
+  // sh[(g * kStateWords + w) * NT + threadIdx.x]
   extern __shared__ unsigned sh_state[];
-  constexpr int nth = kPathThreads;
+  constexpr int nth = NT;
   const int tid = threadIdx.x;
   // behind the state: the channel's constants (kChanConsts words per warp:
   // continuum coefficients, [11] channel index, [12] window index) and
@@ -919,51 +921,64 @@ void launch_pack_tiles_n(const CtlDev& c, const TblDev& T, const LosDev& L, cons
 }
 
 // register caps of the autotuner's variants (minimum resident blocks per SM),
-// each with both block shapes
+// each with both 128-thread block shapes, and the tile-major shape with
+// 256-thread blocks (one channel of 8 consecutive tiles) at two caps
 int path_mixed_caps() { return 7; }
-int path_mixed_variants() { return 2 * path_mixed_caps(); }
+int path_mixed_variants() { return 2 * path_mixed_caps() + 2; }
+
+size_t path_smem(const CtlDev& c, int nt) {
+  return sizeof(unsigned) * kStateWords * nt * (size_t)(c.ng > 0 ? c.ng : 1) +
+         sizeof(float) * ((nt / 32) * kChanConsts + kThreadFloats * nt);
+}
+
+template <typename K>
+void launch_k(K kern, unsigned nblk, int nt, size_t smem, cudaStream_t s, const CtlDev& c,
+              const TblDev& T, const ChanDev& ch, const BatchDev& b, const LosDev& L,
+              const MixedPlan& P, float* refl) {
+  if (smem > 48 * 1024)  // many emitters: opt in to the larger shared memory
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  kern<<<nblk, nt, smem, s>>>(c, T, ch, b, L, P, refl);
+}
 
 template <bool CGA>
 void launch_variant(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
-                    const LosDev& L, const MixedPlan& P, float* refl, int variant, unsigned nblk,
-                    size_t smem, cudaStream_t s) {
-  variant %= path_mixed_caps();
-  if (smem > 48 * 1024) {  // many emitters: opt in to the larger shared memory
-    cudaFuncSetAttribute(k_path_mixed<1, CGA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_path_mixed<5, CGA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_path_mixed<6, CGA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_path_mixed<4, CGA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_path_mixed<8, CGA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_path_mixed<10, CGA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_path_mixed<12, CGA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                    const LosDev& L, const MixedPlan& P, float* refl, int variant,
+                    cudaStream_t s) {
+  MixedPlan Pv = P;
+  if (variant >= 2 * path_mixed_caps()) {  // 256 threads, one channel of 8 tiles
+    Pv.tile_major = 1;
+    const unsigned nblk = (unsigned)((long long)((P.ntile + 7) / 8) * c.nd);
+    const size_t smem = path_smem(c, 256);
+    if (variant == 2 * path_mixed_caps())
+      launch_k(k_path_mixed<4, CGA, false, false, false, 256>, nblk, 256, smem, s, c, T, ch, b, L, Pv, refl);
+    else
+      launch_k(k_path_mixed<5, CGA, false, false, false, 256>, nblk, 256, smem, s, c, T, ch, b, L, Pv, refl);
+    return;
   }
-  switch (variant) {
-    case 1: k_path_mixed<5, CGA><<<nblk, kPathThreads, smem, s>>>(c, T, ch, b, L, P, refl); break;
-    case 2: k_path_mixed<6, CGA><<<nblk, kPathThreads, smem, s>>>(c, T, ch, b, L, P, refl); break;
-    case 3: k_path_mixed<4, CGA><<<nblk, kPathThreads, smem, s>>>(c, T, ch, b, L, P, refl); break;
-    case 4: k_path_mixed<8, CGA><<<nblk, kPathThreads, smem, s>>>(c, T, ch, b, L, P, refl); break;
-    case 5: k_path_mixed<10, CGA><<<nblk, kPathThreads, smem, s>>>(c, T, ch, b, L, P, refl); break;
-    case 6: k_path_mixed<12, CGA><<<nblk, kPathThreads, smem, s>>>(c, T, ch, b, L, P, refl); break;
-    default: k_path_mixed<1, CGA><<<nblk, kPathThreads, smem, s>>>(c, T, ch, b, L, P, refl); break;
+  Pv.tile_major = variant >= path_mixed_caps() ? 1 : 0;
+  const int nchb = (c.nd + 3) / 4;
+  const unsigned nblk = Pv.tile_major ? (unsigned)((long long)((P.ntile + 3) / 4) * c.nd)
+                                      : (unsigned)((long long)P.ntile * nchb);
+  // state, then kChanConsts per warp and kThreadFloats per thread
+  const size_t smem = path_smem(c, kPathThreads);
+  switch (variant % path_mixed_caps()) {
+    case 1: launch_k(k_path_mixed<5, CGA>, nblk, kPathThreads, smem, s, c, T, ch, b, L, Pv, refl); break;
+    case 2: launch_k(k_path_mixed<6, CGA>, nblk, kPathThreads, smem, s, c, T, ch, b, L, Pv, refl); break;
+    case 3: launch_k(k_path_mixed<4, CGA>, nblk, kPathThreads, smem, s, c, T, ch, b, L, Pv, refl); break;
+    case 4: launch_k(k_path_mixed<8, CGA>, nblk, kPathThreads, smem, s, c, T, ch, b, L, Pv, refl); break;
+    case 5: launch_k(k_path_mixed<10, CGA>, nblk, kPathThreads, smem, s, c, T, ch, b, L, Pv, refl); break;
+    case 6: launch_k(k_path_mixed<12, CGA>, nblk, kPathThreads, smem, s, c, T, ch, b, L, Pv, refl); break;
+    default: launch_k(k_path_mixed<1, CGA>, nblk, kPathThreads, smem, s, c, T, ch, b, L, Pv, refl); break;
   }
 }
 
 void launch_path_mixed(const CtlDev& c, const TblDev& T, const ChanDev& ch, const BatchDev& b,
                        const LosDev& L, const MixedPlan& P, float* refl_scratch, int variant,
                        cudaStream_t s) {
-  MixedPlan Pv = P;
-  Pv.tile_major = variant >= path_mixed_caps() ? 1 : 0;
-  const int nchb = (c.nd + 3) / 4;
-  const unsigned nblk = Pv.tile_major ? (unsigned)((long long)((P.ntile + 3) / 4) * c.nd)
-                                      : (unsigned)((long long)P.ntile * nchb);
-  // state, then kChanConsts per warp and kThreadFloats per thread (128
-  // threads, 4 warps per block)
-  const size_t smem = sizeof(unsigned) * kStateWords * kPathThreads * (size_t)(c.ng > 0 ? c.ng : 1) +
-                      sizeof(float) * (4 * kChanConsts + kThreadFloats * kPathThreads);
   if (c.formod == 0)
-    launch_variant<true>(c, T, ch, b, L, Pv, refl_scratch, variant, nblk, smem, s);
+    launch_variant<true>(c, T, ch, b, L, P, refl_scratch, variant, s);
   else
-    launch_variant<false>(c, T, ch, b, L, Pv, refl_scratch, variant, nblk, smem, s);
+    launch_variant<false>(c, T, ch, b, L, P, refl_scratch, variant, s);
 }
 
 template <bool CGA>
