@@ -114,6 +114,9 @@ typedef struct {
 /* Context: replaces the process-global table state initialised by the first
    formod_pencil call (jurassic.c:3202-3217). */
 int jgb_create(const jgb_ctl *ctl, int device, jgb_ctx **out);
+/* Frees the context's device memory, and that of the engines made from it
+   and still open: their handles then accept only jgb_engine_destroy (every
+   other engine call returns JGB_ERR_STATE). */
 void jgb_destroy(jgb_ctx *ctx);
 const char *jgb_last_error(const jgb_ctx *ctx);
 
@@ -330,6 +333,7 @@ typedef struct {
 int jgb_engine_create(jgb_ctx *ctx, const jgb_ret *ret, int precision,
                       unsigned long long mem_budget, int max_active, int keep_gain,
                       jgb_engine **out);
+/* Frees an engine (before or after its context). */
 void jgb_engine_destroy(jgb_engine *e);
 /* Queue every observation of a host batch (a-priori atmosphere, geometry and
    measurement in b->rad, NaN = not used) as one request; ids[nobs] out.

@@ -174,9 +174,9 @@ __global__ void k_slab_offsets(int nray, long long slab, long long* off, int* co
   if (r < nray) count[r] = (int)slab;
 }
 
-__global__ void k_iota(int n, int* v) {
+__global__ void k_iota(int n, int* v, int from = 0) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) v[i] = i;
+  if (i < n) v[i] = from + i;
 }
 
 // tile plan from the rays in sort order (descending key): the first nfirst
@@ -221,6 +221,21 @@ __global__ void k_tiles(int nray, int ntile, int nfirst, int tfirst, int nsecond
 // ray's, and the path state before the first segment that comes closer is
 // the base's (one point earlier is taken as a safety margin).  Bases, and
 // perturbations of other than level values, start at 0.
+// First segment [zb[p], zb[p + 1]] of n LOS points (the last point alone)
+// that comes within [z_lo, z_hi] of perturbation pr of observation e, each
+// side widened by margin; n if none does.
+__device__ int first_near(const BatchDev& b, int e, int4 pr, double margin, const double* zb,
+                          int n) {
+  const int l0 = b.lev_off[e], nl = b.lev_off[e + 1] - l0;
+  const double z1 = b.z[l0 + max(pr.z - 1, 0)], z2 = b.z[l0 + min(pr.z + 1, nl - 1)];
+  const double lo = fmin(z1, z2) - margin, hi = fmax(z1, z2) + margin;
+  for (int p = 0; p < n; p++) {
+    const double za = zb[p], zc = p + 1 < n ? zb[p + 1] : za;
+    if (fmin(za, zc) <= hi && fmax(za, zc) >= lo) return p;
+  }
+  return n;
+}
+
 __global__ void k_resume_points(int nray, BatchDev b, LosDev L, int nbase, const int4* pert,
                                 const int* base_obs, const int* ray_off, double margin,
                                 int* start) {
@@ -234,20 +249,47 @@ __global__ void k_resume_points(int nray, BatchDev b, LosDev L, int nbase, const
   }
   const int eb = base_obs[e];
   const int rb = ray_off[eb] + (r - ray_off[e]);
-  const int l0 = b.lev_off[e], nl = b.lev_off[e + 1] - l0;
-  const double z1 = b.z[l0 + max(pr.z - 1, 0)], z2 = b.z[l0 + min(pr.z + 1, nl - 1)];
-  const double lo = fmin(z1, z2) - margin, hi = fmax(z1, z2) + margin;
   const int n = min(L.count[rb], L.count[r]);
-  const double* zb = L.z + L.off[rb];
-  int p0 = n;
-  for (int p = 0; p < n; p++) {
-    const double za = zb[p], zc = p + 1 < n ? zb[p + 1] : za;
-    if (fmin(za, zc) <= hi && fmax(za, zc) >= lo) {
-      p0 = p;
-      break;
+  const int p0 = first_near(b, e, pr, margin, L.z + L.off[rb], n);
+  start[r] = max(p0 - 1, 0);
+}
+
+// Trace plan of the perturbed rays [nbase_rays, nray) of a resumed batch
+// (TraceResume; the base rays are traced).  A perturbed mixing ratio
+// (array 2) or extinction (array 3) leaves the walk alone: the step rule,
+// refraction and the clipping at the ground and the top see z, p and T
+// only, so the ray takes its base's geometry (mode 2).  A perturbed
+// temperature (array 1) changes the walk only from the first segment that
+// comes within margin of the perturbed levels' intervals, p0: before p0 the
+// points, their data and the walk's state equal the base's, so the ray walks
+// on from the base's state one point before p0 (mode 1, which needs that
+// point unclipped: m < n_b - 1), or takes the base's geometry when no
+// segment comes near (mode 2).  Everything else walks from the start
+// (mode 0).  key: the points left to walk, for ordering the threads.
+__global__ void k_trace_plan(int nray, int nbase_rays, BatchDev b, LosDev L, const int4* pert,
+                             const int* base_obs, const int* ray_off, double margin, int4* plan,
+                             int* key) {
+  const int r = nbase_rays + blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nray) return;
+  const int e = b.ray_obs[r];
+  const int4 pr = pert[e];
+  int4 pl = make_int4(-1, 0, 0, 0);
+  if (pr.x >= 1 && pr.x <= 3) {
+    const int eb = base_obs[e];
+    const int rb = ray_off[eb] + (r - ray_off[e]);
+    const int nb = L.count[rb];
+    if (nb > 0) {
+      if (pr.x >= 2) {
+        pl = make_int4(rb, 0, 2, 0);
+      } else {
+        const int p0 = first_near(b, e, pr, margin, L.z + L.off[rb], nb);
+        if (p0 >= nb) pl = make_int4(rb, 0, 2, 0);
+        else if (p0 - 1 >= 1) pl = make_int4(rb, p0 - 1, 1, 0);
+      }
     }
   }
-  start[r] = max(p0 - 1, 0);
+  plan[r] = pl;
+  key[r - nbase_rays] = pl.z == 2 ? 0 : max(L.count[r] - pl.y, 0);
 }
 
 // Sort key of a resumed batch: bases first (their tiles run first and save
@@ -322,6 +364,18 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
   // geometric bound of every ray's LOS points; if a ray outgrows its bound,
   // or in FP64, the rays are counted first (count, scan, fill).
   const long long slab = c.nlos_max;
+  // resumed perturbations (EGA; the Curtis-Godson sums run from the first
+  // point) are traced from their base rays' walks (TraceResume).  The base
+  // rays are then traced before the others, which adds a whole walk to the
+  // critical path: in the automatic mode this pays only where the perturbed
+  // rays take several waves of the fill kernel (a batch within one wave
+  // takes as long as its longest walk).
+  bool tres = x->resume && precision == JGB_MIXED && c.formod != 0;
+  if (tres && x->fd_resume == 1) {
+    const int nbr = x->resume->h_ray_off[x->resume->nbase];
+    tres = (long long)(nray - nbr) >= 4LL * trace_fill_resident(x->sms);
+  }
+  int trace_launches = 0;  // kernels of the resumed tracing beyond one fill
   enum { kSlab, kBound, kCount } mode =
       precision != JGB_MIXED ? kCount
       : (long long)nray * slab <= kSinglePassPoints ? kSlab
@@ -388,7 +442,53 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
     L.cgp = L.kw + (long long)c.nw * cap;
     L.cgt = L.cgp + (long long)c.ng * cap;
     L.cgu = L.cgt + (long long)c.ng * cap;
-    if (precision == JGB_MIXED) {
+    if (tres) {
+      // resumed perturbations: the base rays first, keeping their walks;
+      // then the perturbed rays, by the points they have left to walk
+      const int nbr = x->resume->h_ray_off[x->resume->nbase], npr = nray - nbr;
+      long long bpts = (long long)nbr * slab;
+      if (mode != kSlab) {
+        CK(cudaMemcpyAsync(&bpts, L.off + nbr, sizeof(long long), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+      }
+      bpts = std::max(bpts, 1LL);
+      auto a16 = [](size_t v) { return (v + 15) & ~size_t(15); };
+      const size_t o_es = a16(sizeof(double) * 3 * (size_t)bpts);
+      const size_t o_ds = o_es + o_es, o_lev = o_ds + a16(sizeof(double) * (size_t)bpts);
+      const size_t o_plan = o_lev + a16(sizeof(int) * (size_t)bpts);
+      const size_t o_key = o_plan + a16(sizeof(int4) * (size_t)nray);
+      const size_t nk = (size_t)std::max(npr, 1);
+      CK(x->rs_trace.reserve(o_key + 4 * a16(sizeof(int) * nk)));
+      char* tb = x->rs_trace.as<char>();
+      TraceResume R{};
+      R.bpts = bpts;
+      R.xs = reinterpret_cast<double*>(tb);
+      R.es = reinterpret_cast<double*>(tb + o_es);
+      R.dsr = reinterpret_cast<double*>(tb + o_ds);
+      R.lev = reinterpret_cast<int*>(tb + o_lev);
+      int4* plan = reinterpret_cast<int4*>(tb + o_plan);
+      R.plan = plan;
+      int* key = reinterpret_cast<int*>(tb + o_key);
+      int* key2 = key + a16(sizeof(int) * nk) / sizeof(int);
+      int* vin = key2 + a16(sizeof(int) * nk) / sizeof(int);
+      int* vout = vin + a16(sizeof(int) * nk) / sizeof(int);
+      launch_trace_fill_resumed(c, b, L, nullptr, 0, nbr, R, 1, d_err, s);
+      if (npr > 0) {
+        const ResumeSpec* rs = x->resume;
+        k_trace_plan<<<(npr + 127) / 128, 128, 0, s>>>(nray, nbr, b, L, rs->pert, rs->base_obs,
+                                                        rs->ray_off, 0.05, plan, key);
+        k_iota<<<(npr + 255) / 256, 256, 0, s>>>(npr, vin, nbr);
+        int bits = 1;
+        while (bits < 31 && (1LL << bits) <= (long long)c.nlos_max) bits++;
+        size_t sb = 0;
+        cub::DeviceRadixSort::SortPairsDescending(nullptr, sb, key, key2, vin, vout, npr, 0, bits, s);
+        CK(x->scan_tmp.reserve(sb + 16));
+        cub::DeviceRadixSort::SortPairsDescending(x->scan_tmp.p, sb, key, key2, vin, vout, npr, 0,
+                                                  bits, s);
+        launch_trace_fill_resumed(c, b, L, vout, 0, npr, R, 2, d_err, s);
+        trace_launches += 6;  // plan, iota, the sort's three passes, the fill
+      }
+    } else if (precision == JGB_MIXED) {
       // rays ordered by capacity (longest first) when the capacities are
       // bounds of the real lengths: a warp's rays then walk similar lengths
       const int* order = nullptr;
@@ -445,7 +545,7 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
   // reflection needs per-point source and emissivity per channel
   const bool need_refl = c.sftype >= 2 && c.nsf > 0;
   TblDev T = tbl_view(x);
-  int launches = 4 + (c.hydz >= 0);
+  int launches = 4 + (c.hydz >= 0) + trace_launches;
   if (precision == JGB_FP64) {
     double* refl = nullptr;
     if (need_refl) {
@@ -1348,9 +1448,14 @@ int jgb_create(const jgb_ctl* ctl, int device, jgb_ctx** out) {
 
 void jgb_destroy(jgb_ctx* x) {
   if (!x) return;
-  { jgb::CtxLock lock(x); }  // calls still running on other threads end first
-  cudaSetDevice(x->device);
-  if (x->stream) cudaStreamSynchronize(x->stream);
+  {
+    jgb::CtxLock lock(x);  // calls still running on other threads end first
+    cudaSetDevice(x->device);
+    if (x->stream) cudaStreamSynchronize(x->stream);
+    // engines still open lose their memory now and their context
+    for (jgb_engine* E : x->engines) engine_detach(E);
+    x->engines.clear();
+  }
   DevBuf* bufs[] = {&x->d_nu, &x->d_window, &x->d_clnu, &x->d_sfnu, &x->d_ctm, &x->t_np,
                     &x->t_p, &x->t_nt, &x->t_t, &x->t_nu, &x->t_u, &x->t_eps, &x->t_pf,
                     &x->t_tf, &x->t_meta, &x->t_ue, &x->s_st, &x->s_sr, &x->s_srf, &x->b_levoff, &x->b_rayoff,
@@ -1359,7 +1464,8 @@ void jgb_destroy(jgb_ctx* x) {
                     &x->los_sft, &x->los_ends, &x->los_planes, &x->scan_tmp, &x->err_word,
                     &x->tiles_perm, &x->tiles_keys, &x->tiles_keys2, &x->tiles_vals,
                     &x->tiles_off, &x->tiles_len, &x->tiles_data, &x->refl, &x->seg,
-                    &x->rs_start, &x->rs_lists, &x->rs_snap, &x->rs_base,
+                    &x->rs_start, &x->rs_lists, &x->rs_snap, &x->rs_base, &x->rs_seg, &x->rs_trace,
+                    &x->d_fov, &x->fov_raw,
                     &x->kx_levoff, &x->kx_rayoff, &x->kx_rayobs, &x->kx_src, &x->kx_lev,
                     &x->kx_scal, &x->kx_geo, &x->kx_rad, &x->kx_tau, &x->kx_tp, &x->kx_mask,
                     &x->kx_pert, &x->kx_h, &x->kx_ymap, &x->kx_K, &x->kx_base_rayoff,

@@ -17,6 +17,10 @@ namespace jgb {
 struct DevBuf {
   void* p = nullptr;
   size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }  // a context's buffers go with it
   cudaError_t reserve(size_t bytes) {
     if (bytes <= n) return cudaSuccess;
     if (p) cudaFree(p);
@@ -96,9 +100,14 @@ struct jgb_ctx {
   double los_bound_scale = 1.0;  // factor on the per-ray LOS bound (0: count first)
   int path_split = -1;    // path split over emitters: -1 when latency-bound, 0 never, 1 always
   int fd_resume = 1;      // resume perturbed paths from their base's state: 0 never,
-                          // 1 when the estimated schedule is shorter, 2 always
+                          // 1 when the estimated schedule is shorter, 2 always,
+                          // 3 always and with the emitters shared with the base
   const ResumeSpec* resume = nullptr;  // set by fd_core for the run_core call it makes
-  jgb::DevBuf rs_start, rs_lists, rs_snap, rs_base, rs_seg, rs_reuse;
+  jgb::DevBuf rs_start, rs_lists, rs_snap, rs_base, rs_seg;
+  // resumed tracing: the base rays' walks and the perturbed rays' plan
+  jgb::DevBuf rs_trace;
+  // retrieval engines made from this context (detached by jgb_destroy)
+  std::vector<jgb_engine*> engines;
   int sms = 152;          // multiprocessors of the device
   jgb::DevBuf seg;        // segment emissivities and flags of the split path
   std::vector<float> tune_ms;

@@ -6,6 +6,7 @@
 #include "jgb_common.cuh"
 
 struct jgb_ctx;
+struct jgb_engine;
 
 namespace jgb {
 
@@ -21,6 +22,33 @@ void launch_trace_count_mixed(const CtlDev& c, const BatchDev& b, const LosDev& 
                               cudaStream_t s);
 void launch_trace_fill_mixed(const CtlDev& c, const BatchDev& b, const LosDev& L, const int* order,
                              unsigned* err, cudaStream_t s);
+// Resumed tracing of finite-difference perturbations (EGA).  The fill of the
+// base rays (the first nbase rays of the batch) keeps, per LOS point (indexed
+// like the LOS planes, bpts points), the walk's FP64 position and direction,
+// its raw segment length and its level interval.  A perturbed ray r then
+// follows plan[r] = {base ray, m, mode}: mode 2 takes the base's geometry
+// whole and recomputes the point values from its own profile (a perturbed
+// mixing ratio or extinction: the step rule and refraction see z, p and T
+// only; or a perturbed temperature whose levels the ray never comes near);
+// mode 1 copies the base's points before m and walks on from the base's
+// state at point m (a perturbed temperature, m before the first segment that
+// comes near the perturbed levels); mode 0 walks from the start.  Every
+// perturbed ray's LOS equals, bit for bit, what a walk from the start writes.
+struct TraceResume {
+  long long bpts;
+  double* xs;        // [3][bpts] positions
+  double* es;        // [3][bpts] directions
+  double* dsr;       // [bpts] raw segment lengths
+  int* lev;          // [bpts] level intervals
+  const int4* plan;  // [nray] (perturbed rays)
+};
+// rays the fill kernel of the perturbed rays holds on the device at once
+int trace_fill_resident(int sms);
+// rays [r0, r0 + nr) (or order[0, nr)); role 1: the base rays (keep their
+// walks in R), role 2: the perturbed rays (follow R.plan)
+void launch_trace_fill_resumed(const CtlDev& c, const BatchDev& b, const LosDev& L,
+                               const int* order, int r0, int nr, const TraceResume& R, int role,
+                               unsigned* err, cudaStream_t s);
 void launch_los_bound_mixed(const CtlDev& c, const BatchDev& b, double scale, int* cap,
                             cudaStream_t s);
 void launch_trace_fill(const CtlDev& c, const ChanDev& ch, const BatchDev& b, const LosDev& L,
@@ -108,6 +136,11 @@ void launch_src_to_float(int nd, const double* sr, float* srf, cudaStream_t s);
 void launch_tables_to_float(long long n, const double* src, float* dst, cudaStream_t s);
 void launch_rowmeta(long long nrow, int tu, const int* nu, const float* u, const float* e,
                     const float* tf, int cga, float4* meta, float2* ue, cudaStream_t s);
+
+// jgb_retrieval.cu: frees an engine's device and pinned memory and unties
+// it from its context (which is being destroyed); the handle then accepts
+// only jgb_engine_destroy, every other call returns JGB_ERR_STATE
+void engine_detach(jgb_engine* E);
 
 // jgb_api.cu: read-only view of a context for entry points defined in other
 // translation units.  Returns JGB_OK, or an error code with the context's

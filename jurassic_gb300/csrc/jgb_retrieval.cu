@@ -1590,6 +1590,7 @@ extern "C" int jgb_engine_create(jgb_ctx* x, const jgb_ret* ret, int precision,
   const CtlDev& c = x->c;
   jgb_engine* E = new jgb_engine();
   E->x = x;
+  x->engines.push_back(E);
   E->precision = precision;
   E->budget = mem_budget ? mem_budget : ~0ULL;
   E->max_active = max_active > 0 ? std::min(max_active, 65535) : 65535;
@@ -1614,17 +1615,37 @@ extern "C" int jgb_engine_create(jgb_ctx* x, const jgb_ret* ret, int precision,
   return JGB_OK;
 }
 
+void jgb::engine_detach(jgb_engine* E) {
+  for (jgb::WorkSet& w : E->ws) w.mem.release();
+  E->cw.mem.release();
+  E->chainbuf.release();
+  E->segbuf.release();
+  E->stage.release();
+  if (E->pinned) cudaFreeHost(E->pinned);
+  E->pinned = nullptr;
+  E->pinned_n = 0;
+  E->have_ws = false;
+  E->x = nullptr;
+}
+
 extern "C" void jgb_engine_destroy(jgb_engine* E) {
-  jgb::CtxLock lock(E ? E->x : nullptr);
   if (!E) return;
-  cudaSetDevice(E->x->device);
-  cudaStreamSynchronize(E->x->stream);
+  jgb_ctx* x = E->x;
+  if (!x) {  // detached by jgb_destroy: its memory is gone already
+    delete E;
+    return;
+  }
+  jgb::CtxLock lock(x);
+  cudaSetDevice(x->device);
+  cudaStreamSynchronize(x->stream);
+  x->engines.erase(std::remove(x->engines.begin(), x->engines.end(), E), x->engines.end());
   delete E;
 }
 
 extern "C" int jgb_engine_submit(jgb_engine* E, const jgb_batch* hb, unsigned long long* ids) {
   jgb::CtxLock lock(E ? E->x : nullptr);
   if (!E || !hb || hb->nobs <= 0) return ctx_error(E ? E->x : nullptr, JGB_ERR_ARG, "bad arguments");
+  if (!E->x) return JGB_ERR_STATE;  // context destroyed
   jgb_ctx* x = E->x;
   const CtlDev& c = x->c;
   const int nobs = hb->nobs;
@@ -1675,6 +1696,7 @@ extern "C" int jgb_engine_submit(jgb_engine* E, const jgb_batch* hb, unsigned lo
 extern "C" int jgb_engine_step(jgb_engine* E, int* n_active, int* n_queued, int* n_done) {
   jgb::CtxLock lock(E ? E->x : nullptr);
   if (!E) return JGB_ERR_ARG;
+  if (!E->x) return JGB_ERR_STATE;  // context destroyed
   const int rc = engine_step(E);
   if (n_active) *n_active = (int)E->active.size();
   if (n_queued) *n_queued = (int)E->queue.size();
@@ -1685,6 +1707,7 @@ extern "C" int jgb_engine_step(jgb_engine* E, int* n_active, int* n_queued, int*
 extern "C" int jgb_engine_finished(jgb_engine* E, unsigned long long* ids, int max, int* count) {
   jgb::CtxLock lock(E ? E->x : nullptr);
   if (!E || !count) return JGB_ERR_ARG;
+  if (!E->x) return JGB_ERR_STATE;  // context destroyed
   int k = 0;
   for (auto it = E->done.begin(); it != E->done.end() && k < max; ++it) ids[k++] = it->first;
   *count = k;
@@ -1694,6 +1717,7 @@ extern "C" int jgb_engine_finished(jgb_engine* E, unsigned long long* ids, int m
 extern "C" int jgb_engine_sizes(jgb_engine* E, unsigned long long id, int* n, int* m, int* np, int* nr) {
   jgb::CtxLock lock(E ? E->x : nullptr);
   if (!E) return JGB_ERR_ARG;
+  if (!E->x) return JGB_ERR_STATE;  // context destroyed
   auto it = E->done.find(id);
   if (it == E->done.end()) return ctx_error(E->x, JGB_ERR_ARG, "unknown or unfinished request");
   const Request* q = it->second;
@@ -1707,6 +1731,7 @@ extern "C" int jgb_engine_sizes(jgb_engine* E, unsigned long long id, int* n, in
 extern "C" int jgb_engine_result(jgb_engine* E, unsigned long long id, jgb_ret_out* o) {
   jgb::CtxLock lock(E ? E->x : nullptr);
   if (!E || !o) return JGB_ERR_ARG;
+  if (!E->x) return JGB_ERR_STATE;  // context destroyed
   auto it = E->done.find(id);
   if (it == E->done.end()) return ctx_error(E->x, JGB_ERR_ARG, "unknown or unfinished request");
   Request* q = it->second;
@@ -1738,6 +1763,7 @@ extern "C" int jgb_engine_result(jgb_engine* E, unsigned long long id, jgb_ret_o
 extern "C" int jgb_engine_get_stats(const jgb_engine* E, jgb_engine_stats* out) {
   jgb::CtxLock lock(E ? E->x : nullptr);
   if (!E || !out) return JGB_ERR_ARG;
+  if (!E->x) return JGB_ERR_STATE;  // context destroyed
   *out = E->st;
   out->active = (int)E->active.size();
   out->queued = (int)E->queue.size();

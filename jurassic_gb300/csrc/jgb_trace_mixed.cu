@@ -92,11 +92,25 @@ __device__ inline bool lev_holds(const Lev& L, float dl) {
   return L.i >= 0 && L.dz > 0.f && (dl >= 0.f || L.first) && (dl < L.dz || L.last);
 }
 
-// Interval of z with the cached interval as hint; returns dl = z - z_i.
+// Interval of z with the cached interval as hint, then its neighbour towards
+// z (a ray or a refraction sub-point mostly crosses one level at a time:
+// one round of independent loads instead of a bisection's chain); returns
+// dl = z - z_i.  An interval that holds z is the one the bisection finds,
+// so the hints change no result.
 __device__ inline float lev_find(const AtmM& a, double z, Lev& L) {
   if (L.i >= 0) {
     const float dl = (float)(z - L.z0);
     if (lev_holds(L, dl)) return dl;
+    const int j = dl < 0.f ? L.i - 1 : L.i + 1;
+    if (j >= 0 && j <= a.np - 2) {
+      Lev M;
+      lev_load(a, j, M);
+      const float dm = (float)(z - M.z0);
+      if (lev_holds(M, dm)) {
+        L = M;
+        return dm;
+      }
+    }
   }
   lev_load(a, bracket_irr(a.z, a.np, z), L);
   return (float)(z - L.z0);
@@ -141,16 +155,42 @@ struct GeoKeep {
   bool want_p1;
 };
 
+// The walk's state at LOS point n, for walking on from there: position,
+// direction and altitude at the point, the previous point's position and
+// altitude, and the previous point's level interval (the search hint).
+struct WalkFrom {
+  int n;
+  double x[3], e[3], z;
+  double x_last[3], z_last;
+  int lev_last;
+};
+
+// Mixing ratio or extinction at offset dl in a level interval, from the
+// level value v0 and the slope (v1 - v0) / dz, rounded after the product
+// and after the sum (shared by the walk and the copies of a base's
+// geometry, so both give the same bits).
+__device__ __forceinline__ float qk_at(float v0, float slope, float dl) {
+  return __fadd_rn(v0, __fmul_rn(slope, dl));
+}
+
+// Column density of a segment, 10 / k_B q p / T ds (p in hPa, ds in km).
+__device__ __forceinline__ float col_density(float q, float p, float t, float ds) {
+  return (float)(10.0 / kKB) * q * p / t * ds;
+}
+
 // Threads per block of the trace kernels (the fill pass keeps per-thread
 // level caches in shared memory with this stride).
 constexpr int kTraceThreads = 64;
 
 // qc: the fill pass's cache of the current level's emitter and window values
 // and slopes (qc[k * kTraceThreads], qc[(ng + nw + k) * kTraceThreads]).
-template <bool STORE>
+// ROLE 1 keeps every point's position, direction and level interval in sv;
+// ROLE 2 with wf walks on from the state wf (a base ray's walk).
+template <bool STORE, int ROLE = 0>
 __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long nray, int r,
                       const LosDev& L, long long base, int cap, double* sft_out, GeoKeep* gk,
-                      float* qc, unsigned* err) {
+                      float* qc, unsigned* err, const WalkFrom* wf = nullptr,
+                      const TraceResume* sv = nullptr) {
   const float h = 0.02f;
   const double zrefrac = 60;
   *sft_out = -999;
@@ -175,36 +215,47 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
   }
   if (vpz > zmax) return 0;
 
-  double x[3], xobs[3], xvp[3];
-  to_cart(obsz, obslon, obslat, xobs);
-  to_cart(vpz, vplon, vplat, xvp);
   // the direction stays FP64: renormalising an FP32 unit vector every step
   // would random-walk it by ~1e-7 rad per step (metres over a limb path)
-  double ex0[3];
-  for (int i = 0; i < 3; i++) ex0[i] = xvp[i] - xobs[i];
-  const double norm = sqrt(ex0[0] * ex0[0] + ex0[1] * ex0[1] + ex0[2] * ex0[2]);
-  for (int i = 0; i < 3; i++) {
-    ex0[i] /= norm;
-    x[i] = xobs[i];
-  }
-  double z = obsz;
-  if (obsz > zmax) {  // entry into the atmosphere: bisection on the line of sight (FP64, once)
-    double dmax = norm, dmin = 0;
-    for (int guard = 0; fabs(dmin - dmax) > 0.001 && guard < 200; guard++) {
-      const double d = (dmax + dmin) / 2;
-      for (int i = 0; i < 3; i++) x[i] = xobs[i] + d * ex0[i];
-      z = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]) - kRE;
-      if (z <= zmax && z > zmax - 0.001) break;
-      if (z < zmax - 0.0005) dmax = d; else dmin = d;
-    }
-  }
-  z = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]) - kRE;
-
+  double x[3], ex0[3], z;
+  double last_z = 0, x_last[3] = {0, 0, 0};
   Lev lv;
   lv.i = -1;
   int n = 0, stop = 0, qc_level = -1;
+  if (ROLE == 2 && wf) {  // on from a base's walk
+    for (int i = 0; i < 3; i++) {
+      x[i] = wf->x[i];
+      ex0[i] = wf->e[i];
+      x_last[i] = wf->x_last[i];
+    }
+    z = wf->z;
+    last_z = wf->z_last;
+    n = wf->n;
+    lev_load(a, wf->lev_last, lv);
+  } else {
+    double xobs[3], xvp[3];
+    to_cart(obsz, obslon, obslat, xobs);
+    to_cart(vpz, vplon, vplat, xvp);
+    for (int i = 0; i < 3; i++) ex0[i] = xvp[i] - xobs[i];
+    const double norm = sqrt(ex0[0] * ex0[0] + ex0[1] * ex0[1] + ex0[2] * ex0[2]);
+    for (int i = 0; i < 3; i++) {
+      ex0[i] /= norm;
+      x[i] = xobs[i];
+    }
+    z = obsz;
+    if (obsz > zmax) {  // entry into the atmosphere: bisection on the line of sight (FP64, once)
+      double dmax = norm, dmin = 0;
+      for (int guard = 0; fabs(dmin - dmax) > 0.001 && guard < 200; guard++) {
+        const double d = (dmax + dmin) / 2;
+        for (int i = 0; i < 3; i++) x[i] = xobs[i] + d * ex0[i];
+        z = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]) - kRE;
+        if (z <= zmax && z > zmax - 0.001) break;
+        if (z < zmax - 0.0005) dmax = d; else dmin = d;
+      }
+    }
+    z = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]) - kRE;
+  }
   const int nqk = c.ng + c.nw;
-  double last_z = 0, x_last[3] = {0, 0, 0};
   const float rayds = (float)c.rayds, raydz = (float)c.raydz;
   for (;;) {
     // radial unit vector and radius at x
@@ -258,12 +309,22 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
           qc[(nqk + k) * kTraceThreads] = (v1 - v0) / lv.dz;
         }
       }
-      for (int ig = 0; ig < c.ng; ig++)
-        L.u[ig * L.cap + s] = qc[ig * kTraceThreads] + qc[(nqk + ig) * kTraceThreads] * dl;
-      if (c.ig_h2o >= 0) L.qh2o[s] = L.u[c.ig_h2o * L.cap + s];
+      for (int ig = 0; ig < c.ng; ig++) {
+        const float v = qk_at(qc[ig * kTraceThreads], qc[(nqk + ig) * kTraceThreads], dl);
+        L.u[ig * L.cap + s] = v;
+        if (ig == c.ig_h2o) L.qh2o[s] = v;
+      }
       for (int iw = 0; iw < c.nw; iw++)
-        L.kw[iw * L.cap + s] = qc[(c.ng + iw) * kTraceThreads] +
-                               qc[(nqk + c.ng + iw) * kTraceThreads] * dl;
+        L.kw[iw * L.cap + s] = qk_at(qc[(c.ng + iw) * kTraceThreads],
+                                     qc[(nqk + c.ng + iw) * kTraceThreads], dl);
+      if (ROLE == 1) {
+        const long long bp = sv->bpts;
+        for (int i2 = 0; i2 < 3; i2++) {
+          sv->xs[i2 * bp + s] = x[i2];
+          sv->es[i2 * bp + s] = ex0[i2];
+        }
+        sv->lev[s] = i;
+      }
       if (c.ncl > 0 && a.cldz > 0) {
         const float v = (float)((z - a.clz) / a.cldz);
         L.aux[s] = expf(-0.5f * v * v);
@@ -443,13 +504,72 @@ __global__ void k_los_bound_m(CtlDev c, BatchDev b, double scale, int* cap) {
   cap[r] = bound >= (double)c.nlos_max ? c.nlos_max : (int)bound;
 }
 
-// order (optional): thread t traces ray order[t], so that a warp's rays have
-// similar LOS capacities and finish together; each ray's outputs go to its
-// own slots, so the order does not change any result.
-__global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, const int* order, unsigned* err) {
+// Resumed perturbation of mode 2 (TraceResume): ray r takes base ray rb's
+// LOS geometry, p, T, cloud weights, segment lengths, tangent point and
+// ends, and evaluates its own mixing ratios and extinctions on the base's
+// level intervals, as its own walk would.
+__device__ void copy_base_geometry(const CtlDev& c, const BatchDev& b, const LosDev& L,
+                                   const AtmM& a, int r, int rb, int cap, const TraceResume& R,
+                                   float* qc, unsigned* err) {
+  const long long base = L.off[r], ob = L.off[rb];
+  const int n = L.count[rb];
+  if (n > cap) {
+    atomicOr(err, cap < c.nlos_max ? kErrSlabOverflow : kErrLosOverflow);
+    return;
+  }
+  const long long nr = b.nray;
+  for (int k = 0; k < 3; k++) b.tp[k * nr + r] = b.tp[k * nr + rb];
+  for (int k = 0; k < 6; k++) L.ends[6LL * r + k] = L.ends[6LL * rb + k];
+  L.sft[r] = L.sft[rb];
+  L.count[r] = n;
+  const int nqk = c.ng + c.nw;
+  int qc_level = -1;
+  double z0 = 0;
+  for (int ip = 0; ip < n; ip++) {
+    const long long q = ob + ip, s = base + ip;
+    const double z = L.z[q], p = L.p[q], t = L.t[q], ds = L.ds[q];
+    L.z[s] = z;
+    L.p[s] = p;
+    L.t[s] = t;
+    L.ds[s] = ds;
+    L.aux[s] = L.aux[q];
+    const int i = R.lev[q];
+    if (i != qc_level) {  // the walk's level values and slopes
+      qc_level = i;
+      z0 = a.z[i];
+      const float dz = (float)(a.z[i + 1] - a.z[i]);
+      for (int k = 0; k < nqk; k++) {
+        const double* src = k < c.ng ? a.q + k * a.stride : a.k + (k - c.ng) * a.stride;
+        const float v0 = (float)src[i], v1 = (float)src[i + 1];
+        qc[k * kTraceThreads] = v0;
+        qc[(nqk + k) * kTraceThreads] = (v1 - v0) / dz;
+      }
+    }
+    const float dl = (float)(z - z0);
+    const float pf = (float)p, tf = (float)t, dsf = (float)ds;
+    for (int ig = 0; ig < c.ng; ig++) {
+      const float v = qk_at(qc[ig * kTraceThreads], qc[(nqk + ig) * kTraceThreads], dl);
+      if (ig == c.ig_h2o) L.qh2o[s] = v;
+      L.u[ig * L.cap + s] = col_density(v, pf, tf, dsf);
+    }
+    for (int iw = 0; iw < c.nw; iw++)
+      L.kw[iw * L.cap + s] = qk_at(qc[(c.ng + iw) * kTraceThreads],
+                                   qc[(nqk + c.ng + iw) * kTraceThreads], dl);
+  }
+}
+
+// order (optional): thread t traces ray order[t], else ray r0 + t, so that a
+// warp's rays have similar LOS capacities and finish together; each ray's
+// outputs go to its own slots, so the order does not change any result.
+// ROLE 0: plain rays; 1: base rays of resumed perturbations (their walks are
+// kept in R); 2: the perturbations (R.plan; EGA only: the Curtis-Godson sums
+// run from the first point).
+template <int ROLE>
+__global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, const int* order, int r0, int nr_l,
+                               TraceResume R, unsigned* err) {
   const int th = blockIdx.x * blockDim.x + threadIdx.x;
-  if (th >= b.nray) return;
-  const int r = order ? order[th] : th;
+  if (th >= nr_l) return;
+  const int r = order ? order[th] : r0 + th;
   if (b.obs_skip && b.obs_skip[b.ray_obs[r]]) {
     L.count[r] = 0;
     return;
@@ -457,15 +577,72 @@ __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, const int* order,
   const AtmM a = atm_m(b, c, b.ray_obs[r]);
   const long long base = L.off[r];
   const int cap = L.count[r];
+  __shared__ float qcache[2 * (kMaxG + kMaxW) * kTraceThreads];
+  int4 pl = make_int4(-1, 0, 0, 0);
+  if (ROLE == 2) pl = R.plan[r];
+  if (ROLE == 2 && pl.z == 2) {
+    copy_base_geometry(c, b, L, a, r, pl.x, cap, R, qcache + threadIdx.x, err);
+    return;
+  }
   double sft;
   GeoKeep gk;
   gk.want_p1 = false;
   gk.imin = 0;
   gk.zmin_seen = 0;
   for (int i = 0; i < 3; i++) gk.x_m1[i] = gk.x_p1[i] = gk.x_first[i] = gk.x_last[i] = 0;
-  __shared__ float qcache[2 * (kMaxG + kMaxW) * kTraceThreads];
-  const int n = walk_m<true>(c, a, b.geo, b.nray, r, L, base, cap, &sft, &gk,
-                             qcache + threadIdx.x, err);
+  // mode 1: points [0, m) are the base's (final values); the walk goes on
+  // from the base's state at m, its lon/lat bookkeeping restated from the
+  // base's points before m
+  int m = 0;
+  long long ob = 0;
+  WalkFrom wf;
+  if (ROLE == 2 && pl.z == 1) {
+    m = pl.y;
+    ob = L.off[pl.x];
+    if (m > cap) {
+      atomicOr(err, cap < c.nlos_max ? kErrSlabOverflow : kErrLosOverflow);
+      return;
+    }
+    const long long bp = R.bpts;
+    for (int ip = 0; ip < m; ip++) {
+      const long long q = ob + ip, s = base + ip;
+      L.z[s] = L.z[q];
+      L.p[s] = L.p[q];
+      L.t[s] = L.t[q];
+      L.ds[s] = L.ds[q];
+      L.aux[s] = L.aux[q];
+      if (c.ig_h2o >= 0) L.qh2o[s] = L.qh2o[q];
+      for (int ig = 0; ig < c.ng; ig++) L.u[ig * L.cap + s] = L.u[ig * L.cap + q];
+      for (int iw = 0; iw < c.nw; iw++) L.kw[iw * L.cap + s] = L.kw[iw * L.cap + q];
+    }
+    wf.n = m;
+    for (int i = 0; i < 3; i++) {
+      wf.x[i] = R.xs[i * bp + ob + m];
+      wf.e[i] = R.es[i * bp + ob + m];
+      wf.x_last[i] = R.xs[i * bp + ob + m - 1];
+      gk.x_first[i] = R.xs[i * bp + ob];
+    }
+    wf.z = L.z[ob + m];
+    wf.z_last = L.z[ob + m - 1];
+    wf.lev_last = R.lev[ob + m - 1];
+    // the first lowest point so far and its neighbours
+    int imin = 0;
+    double zmin = L.z[ob];
+    for (int ip = 1; ip < m; ip++)
+      if (L.z[ob + ip] < zmin) {
+        zmin = L.z[ob + ip];
+        imin = ip;
+      }
+    gk.imin = imin;
+    gk.zmin_seen = zmin;
+    gk.want_p1 = imin == m - 1;
+    for (int i = 0; i < 3; i++) {
+      gk.x_m1[i] = imin > 0 ? R.xs[i * bp + ob + imin - 1] : 0.0;
+      gk.x_p1[i] = imin + 1 < m ? R.xs[i * bp + ob + imin + 1] : 0.0;
+    }
+  }
+  const int n = walk_m<true, ROLE>(c, a, b.geo, b.nray, r, L, base, cap, &sft, &gk,
+                                   qcache + threadIdx.x, err, m > 0 ? &wf : nullptr, &R);
   L.sft[r] = sft;
   if (n > 0) L.count[r] = n;
   const long long nr = b.nray;
@@ -480,6 +657,10 @@ __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, const int* order,
   }
   const double* z = L.z + base;
   double* ds = L.ds + base;
+  if (ROLE == 1)  // raw segment lengths, for the perturbations walking on
+    for (int ip = 0; ip < n; ip++) R.dsr[base + ip] = ds[ip];
+  // raw segment length of point ip (the base's before m)
+  auto ds_raw = [&](int ip) { return ip < m ? R.dsr[ob + ip] : ds[ip]; };
   double dummy, lon0, lat0, lonl, latl;
   to_geo(gk.x_first, &dummy, &lon0, &lat0);
   to_geo(gk.x_last, &dummy, &lonl, &latl);
@@ -491,8 +672,9 @@ __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, const int* order,
     tp[2 * nr + r] = latl;
   } else {
     const double y0 = z[imin - 1], y1 = z[imin], y2 = z[imin + 1];
-    const double x1 = sqrt(ds[imin] * ds[imin] - (y1 - y0) * (y1 - y0));
-    const double x2 = x1 + sqrt(ds[imin + 1] * ds[imin + 1] - (y2 - y1) * (y2 - y1));
+    const double d1 = ds_raw(imin), d2 = ds_raw(imin + 1);
+    const double x1 = sqrt(d1 * d1 - (y1 - y0) * (y1 - y0));
+    const double x2 = x1 + sqrt(d2 * d2 - (y2 - y1) * (y2 - y1));
     const double aa = 1 / (x1 - x2) * (-(y0 - y1) / x1 + (y0 - y2) / x2);
     const double bb = -(y0 - y1) / x1 - aa * x1;
     const double cc = y0;
@@ -511,10 +693,15 @@ __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, const int* order,
   e[3] = z[n - 1];
   e[4] = lonl;
   e[5] = latl;
-  // trapezoid segment lengths
-  float prev = (float)ds[0];
-  ds[0] = 0.5f * prev;
-  for (int ip = 1; ip < n; ip++) {
+  // trapezoid segment lengths (points before m hold the base's)
+  float prev;
+  if (m > 0) {
+    prev = (float)R.dsr[ob + m - 1];
+  } else {
+    prev = (float)ds[0];
+    ds[0] = 0.5f * prev;
+  }
+  for (int ip = m > 0 ? m : 1; ip < n; ip++) {
     const float cur = (float)ds[ip];
     ds[ip] = 0.5f * (prev + cur);
     prev = cur;
@@ -522,16 +709,15 @@ __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, const int* order,
   // column densities (q stored in the u plane) and Curtis-Godson means
   const double* p = L.p + base;
   const double* t = L.t + base;
-  const float c10kb = (float)(10.0 / kKB);
   for (int ig = 0; ig < c.ng; ig++) {
     double* u = L.u + ig * L.cap + base;
     double* cgu = L.cga ? L.cgu + ig * L.cap + base : nullptr;
     double* cgp = L.cga ? L.cgp + ig * L.cap + base : nullptr;
     double* cgt = L.cga ? L.cgt + ig * L.cap + base : nullptr;
     float su = 0.f, sp = 0.f, st = 0.f, cu = 0.f, cp = 0.f, ct = 0.f;
-    for (int ip = 0; ip < n; ip++) {
+    for (int ip = m; ip < n; ip++) {
       const float pf = (float)p[ip], tf = (float)t[ip];
-      const float uu = c10kb * (float)u[ip] * pf / tf * (float)ds[ip];
+      const float uu = col_density((float)u[ip], pf, tf, (float)ds[ip]);
       u[ip] = uu;
       if (cgu) {
         // compensated running sums
@@ -571,7 +757,32 @@ void launch_los_bound_mixed(const CtlDev& c, const BatchDev& b, double scale, in
 void launch_trace_fill_mixed(const CtlDev& c, const BatchDev& b, const LosDev& L, const int* order,
                              unsigned* err, cudaStream_t s) {
   const int bs = kTraceThreads;
-  k_trace_fill_m<<<(b.nray + bs - 1) / bs, bs, 0, s>>>(c, b, L, order, err);
+  k_trace_fill_m<0><<<(b.nray + bs - 1) / bs, bs, 0, s>>>(c, b, L, order, 0, b.nray,
+                                                           TraceResume{}, err);
+}
+
+int trace_fill_resident(int sms) {
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_trace_fill_m<2>, kTraceThreads, 0) !=
+            cudaSuccess ||
+        nb < 1)
+      nb = 1;
+    per_sm = nb * kTraceThreads;
+  }
+  return per_sm * sms;
+}
+
+void launch_trace_fill_resumed(const CtlDev& c, const BatchDev& b, const LosDev& L,
+                               const int* order, int r0, int nr, const TraceResume& R, int role,
+                               unsigned* err, cudaStream_t s) {
+  const int bs = kTraceThreads;
+  if (nr <= 0) return;
+  if (role == 1)
+    k_trace_fill_m<1><<<(nr + bs - 1) / bs, bs, 0, s>>>(c, b, L, order, r0, nr, R, err);
+  else
+    k_trace_fill_m<2><<<(nr + bs - 1) / bs, bs, 0, s>>>(c, b, L, order, r0, nr, R, err);
 }
 
 }  // namespace jgb

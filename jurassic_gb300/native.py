@@ -538,7 +538,7 @@ class Engine:
 
     def stats(self) -> dict:
         st = EngineStats()
-        load().jgb_engine_get_stats(self.h, C.byref(st))
+        self.ctx._check(load().jgb_engine_get_stats(self.h, C.byref(st)))
         return st.as_dict()
 
     def result(self, rid: int) -> dict:

@@ -136,7 +136,8 @@ def main(argv=None):
         g = ctypes.c_double(0.0)
         native.load().jgb_measure_l2_read(1 << 20, 1, ctypes.byref(g))
     r = serve(eng, ctl, reqs, np.inf)
-    print(json.dumps({k: v for k, v in r.items() if k != "results"}))
+    print(json.dumps({k: v for k, v in r.items() if k != "results"}), flush=True)
+    eng.close()
     ctx.close()
 
 

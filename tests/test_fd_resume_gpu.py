@@ -10,7 +10,10 @@ states equal to the base's all along the path, so their segment
 emissivities can be taken from the base's walk.  The Jacobians (and a whole
 retrieval) are bit-identical in every mode -- resumed with emitters always
 shared (mode 3), resumed (2, sharing where it pays), plain (0), automatic
-(1): nadir with masked channels, refracted limb EGA, limb CGA.
+(1): nadir with masked channels, refracted limb EGA, limb CGA, limb EGA with
+window extinctions and pressures.  In EGA the perturbed rays' tracing is
+resumed too: a perturbed mixing ratio or extinction takes the base ray's
+geometry, a perturbed temperature walks on from the base's walk.
 """
 import copy
 
@@ -70,6 +73,28 @@ def test_resume_limb(built_lib, formod):
     items = [w.batch.item(w.ctl, 0) for _ in range(3)]
     for i, (atm, obs) in enumerate(items):
         atm.t = atm.t + i                       # three different atmospheres
+    ctx = native.Context(ctl, w.tables, w.filters)
+    _same(_both(ctx, synth.pack(ctl, items)))
+
+
+def test_resume_limb_extinction_pressure(built_lib):
+    """Window extinctions (whose perturbed rays take their base's geometry)
+    and pressures (which walk from the start) next to temperatures and a
+    mixing ratio, on refracted limb rays that cross the perturbed levels and
+    rays that stay above them."""
+    w = synth.config_limb_ega(n_rays=8, formod=1)
+    ctl = copy.deepcopy(w.ctl)
+    ctl.window = np.array([0, 0, 0], dtype=np.int32)
+    ctl.rett_zmin, ctl.rett_zmax = 5.0, 45.0
+    ctl.retp_zmin, ctl.retp_zmax = 18.0, 26.0
+    ctl.retq_zmin = np.array([-999.0, 8.0])
+    ctl.retq_zmax = np.array([-999.0, 20.0])
+    ctl.retk_zmin = np.array([12.0])
+    ctl.retk_zmax = np.array([36.0])
+    items = [w.batch.item(w.ctl, 0) for _ in range(2)]
+    for i, (atm, obs) in enumerate(items):
+        atm.t = atm.t - 2 * i
+        atm.k = np.where((atm.z >= 10) & (atm.z <= 40), 1e-3 * (1 + i), 0.0)[None, :]
     ctx = native.Context(ctl, w.tables, w.filters)
     _same(_both(ctx, synth.pack(ctl, items)))
 
