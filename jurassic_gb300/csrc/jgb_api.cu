@@ -426,22 +426,40 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
     }
     cap = std::max(total, 1LL);
     const int nplanes = 8 + c.ng + c.nw + (c.formod == 0 ? 3 * c.ng : 0);
-    CK(x->los_planes.reserve(sizeof(double) * (size_t)cap * nplanes));
+    const int nfplanes = 5 + c.ng + c.nw + (c.formod == 0 ? 3 * c.ng : 0);
+    CK(x->los_planes.reserve(precision == JGB_MIXED
+                                 ? (sizeof(double) + sizeof(float) * nfplanes) * (size_t)cap
+                                 : sizeof(double) * (size_t)cap * nplanes));
     double* P = x->los_planes.as<double>();
+    if (precision == JGB_MIXED) {  // z in FP64, the point data in FP32 planes
+      float* F = reinterpret_cast<float*>(P + cap);
+      L.f.p = F + 0 * cap;
+      L.f.t = F + 1 * cap;
+      L.f.ds = F + 2 * cap;
+      L.f.aux = F + 3 * cap;
+      L.f.qh2o = F + 4 * cap;
+      L.f.u = F + 5 * cap;
+      L.f.kw = L.f.u + (long long)c.ng * cap;
+      L.f.cgp = L.f.kw + (long long)c.nw * cap;
+      L.f.cgt = L.f.cgp + (long long)c.ng * cap;
+      L.f.cgu = L.f.cgt + (long long)c.ng * cap;
+    }
     L.cap = cap;
     L.z = P + 0 * cap;
-    L.lon = P + 1 * cap;
-    L.lat = P + 2 * cap;
-    L.p = P + 3 * cap;
-    L.t = P + 4 * cap;
-    L.ds = P + 5 * cap;
-    L.aux = P + 6 * cap;
-    L.qh2o = P + 7 * cap;
-    L.u = P + 8 * cap;
-    L.kw = L.u + (long long)c.ng * cap;
-    L.cgp = L.kw + (long long)c.nw * cap;
-    L.cgt = L.cgp + (long long)c.ng * cap;
-    L.cgu = L.cgt + (long long)c.ng * cap;
+    if (precision != JGB_MIXED) {
+      L.lon = P + 1 * cap;
+      L.lat = P + 2 * cap;
+      L.p = P + 3 * cap;
+      L.t = P + 4 * cap;
+      L.ds = P + 5 * cap;
+      L.aux = P + 6 * cap;
+      L.qh2o = P + 7 * cap;
+      L.u = P + 8 * cap;
+      L.kw = L.u + (long long)c.ng * cap;
+      L.cgp = L.kw + (long long)c.nw * cap;
+      L.cgt = L.cgp + (long long)c.ng * cap;
+      L.cgu = L.cgt + (long long)c.ng * cap;
+    }
     if (tres) {
       // resumed perturbations: the base rays first, keeping their walks;
       // then the perturbed rays, by the points they have left to walk
@@ -464,7 +482,7 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
       R.bpts = bpts;
       R.xs = reinterpret_cast<double*>(tb);
       R.es = reinterpret_cast<double*>(tb + o_es);
-      R.dsr = reinterpret_cast<double*>(tb + o_ds);
+      R.dsr = reinterpret_cast<float*>(tb + o_ds);
       R.lev = reinterpret_cast<int*>(tb + o_lev);
       int4* plan = reinterpret_cast<int4*>(tb + o_plan);
       R.plan = plan;

@@ -188,6 +188,14 @@ struct LosDev {
   double* u;            // [ng][cap]
   double* kw;           // [nw][cap]
   double *cgp, *cgt, *cgu;  // [ng][cap] (CGA only)
+  // mixed precision: the point data as FP32 planes (the values are FP32
+  // numbers; z above stays FP64)
+  struct F32 {
+    float *p, *t, *ds, *aux, *qh2o;
+    float* u;             // [ng][cap]
+    float* kw;            // [nw][cap]
+    float *cgp, *cgt, *cgu;  // [ng][cap] (CGA only)
+  } f;
 };
 
 // Float LOS tiles for the mixed path: 32 rays per tile (rays sorted by

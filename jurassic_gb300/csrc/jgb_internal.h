@@ -38,7 +38,7 @@ struct TraceResume {
   long long bpts;
   double* xs;        // [3][bpts] positions
   double* es;        // [3][bpts] directions
-  double* dsr;       // [bpts] raw segment lengths
+  float* dsr;        // [bpts] raw segment lengths
   int* lev;          // [bpts] level intervals
   const int4* plan;  // [nray] (perturbed rays)
 };

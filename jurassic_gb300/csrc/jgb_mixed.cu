@@ -265,20 +265,21 @@ __global__ void k_pack_tiles(CtlDev c, TblDev T, LosDev L, MixedPlan P, long lon
     return;
   }
   const long long q = L.off[r] + ip;
-  out[F.p * 32] = (float)L.p[q];
-  out[F.t * 32] = (float)L.t[q];
-  out[F.ds * 32] = (float)L.ds[q];
-  out[F.qh2o * 32] = c.ig_h2o >= 0 ? (float)L.qh2o[q] : 0.f;
-  out[F.aux * 32] = (float)L.aux[q];
-  for (int w = 0; w < c.nw; w++) out[(F.kw0 + w) * 32] = (float)L.kw[w * L.cap + q];
+  const LosDev::F32& Lf = L.f;
+  out[F.p * 32] = Lf.p[q];
+  out[F.t * 32] = Lf.t[q];
+  out[F.ds * 32] = Lf.ds[q];
+  out[F.qh2o * 32] = c.ig_h2o >= 0 ? Lf.qh2o[q] : 0.f;
+  out[F.aux * 32] = Lf.aux[q];
+  for (int w = 0; w < c.nw; w++) out[(F.kw0 + w) * 32] = Lf.kw[w * L.cap + q];
   const bool cgaf = c.formod == 0;
   for (int g = 0; g < c.ng; g++) {
     float* og = out + (F.g0 + g * F.es) * 32;
-    og[kFU * 32] = (float)L.u[g * L.cap + q];
+    og[kFU * 32] = Lf.u[g * L.cap + q];
     if (cgaf) {
-      og[kFCgp * 32] = (float)L.cgp[g * L.cap + q];
-      og[kFCgt * 32] = (float)L.cgt[g * L.cap + q];
-      og[kFCgu * 32] = (float)L.cgu[g * L.cap + q];
+      og[kFCgp * 32] = Lf.cgp[g * L.cap + q];
+      og[kFCgt * 32] = Lf.cgt[g * L.cap + q];
+      og[kFCgu * 32] = Lf.cgu[g * L.cap + q];
     }
     for (int k = 0; k < 4; k++) og[(kFBr(cgaf) + k) * 32] = 0.f;
   }
@@ -289,8 +290,8 @@ __global__ void k_pack_tiles(CtlDev c, TblDev T, LosDev L, MixedPlan P, long lon
     float pw = 0.f, wa = 0.f, wb = 0.f;
     const int np = __ldg(T.np + g);
     if (((P.brmask >> g) & 1u) && np >= 30) {
-      const float pq = c.formod == 0 ? (float)L.cgp[g * L.cap + q] : (float)L.p[q];
-      const float tq = c.formod == 0 ? (float)L.cgt[g * L.cap + q] : (float)L.t[q];
+      const float pq = c.formod == 0 ? Lf.cgp[g * L.cap + q] : Lf.p[q];
+      const float tq = c.formod == 0 ? Lf.cgt[g * L.cap + q] : Lf.t[q];
       const int ipr = bracket_irrf(T.pf + (long long)g * T.tp, np, pq);
       const int nt0 = __ldg(T.nt + (long long)g * T.tp + ipr);
       const int nt1 = __ldg(T.nt + (long long)g * T.tp + ipr + 1);

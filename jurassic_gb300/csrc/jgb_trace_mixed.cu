@@ -151,6 +151,7 @@ __device__ inline float dz_of(const float* xh, float r, const float* d) {
 struct GeoKeep {
   double x_first[3], x_m1[3], x_p1[3], x_last[3];
   double zmin_seen;
+  double ds_clip;  // the clipped last segment (point n - 2) in FP64
   int imin;
   bool want_p1;
 };
@@ -257,12 +258,13 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
   }
   const int nqk = c.ng + c.nw;
   const float rayds = (float)c.rayds, raydz = (float)c.raydz;
+  // the direction in FP32 (carried from the previous step's conversion)
+  float ef[3] = {(float)ex0[0], (float)ex0[1], (float)ex0[2]};
   for (;;) {
     // radial unit vector and radius at x
     const double rr = z + kRE;
     const float rf = (float)rr, rinv = 1.f / rf;
     float xh[3] = {(float)x[0] * rinv, (float)x[1] * rinv, (float)x[2] * rinv};
-    const float ef[3] = {(float)ex0[0], (float)ex0[1], (float)ex0[2]};
     // step length from this point (jurassic.c:4278-4287)
     float step = rayds;
     if (raydz > 0) {
@@ -283,7 +285,9 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
       const double frac = ((z < zmin ? zmin : zmax) - last_z) / (z - last_z);
       for (int i = 0; i < 3; i++) x[i] = x_last[i] + frac * (x[i] - x_last[i]);
       z = last_z + frac * (z - last_z);
-      L.ds[base + n - 1] = (double)step * frac;
+      const double dsc = (double)step * frac;
+      L.f.ds[base + n - 1] = (float)dsc;
+      gk->ds_clip = dsc;
       step = 0.f;
     }
     if (n >= cap) {
@@ -296,9 +300,9 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
     if (STORE) {
       const long long s = base + n;
       L.z[s] = z;
-      L.p[s] = p;
-      L.t[s] = t;
-      L.ds[s] = step;
+      L.f.p[s] = p;
+      L.f.t[s] = t;
+      L.f.ds[s] = step;
       const int i = lv.i;
       if (i != qc_level) {  // a new level: its values and slopes q0 + (q1 - q0) / dz * dl
         qc_level = i;
@@ -311,12 +315,12 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
       }
       for (int ig = 0; ig < c.ng; ig++) {
         const float v = qk_at(qc[ig * kTraceThreads], qc[(nqk + ig) * kTraceThreads], dl);
-        L.u[ig * L.cap + s] = v;
-        if (ig == c.ig_h2o) L.qh2o[s] = v;
+        L.f.u[ig * L.cap + s] = v;
+        if (ig == c.ig_h2o) L.f.qh2o[s] = v;
       }
       for (int iw = 0; iw < c.nw; iw++)
-        L.kw[iw * L.cap + s] = qk_at(qc[(c.ng + iw) * kTraceThreads],
-                                     qc[(nqk + c.ng + iw) * kTraceThreads], dl);
+        L.f.kw[iw * L.cap + s] = qk_at(qc[(c.ng + iw) * kTraceThreads],
+                                       qc[(nqk + c.ng + iw) * kTraceThreads], dl);
       if (ROLE == 1) {
         const long long bp = sv->bpts;
         for (int i2 = 0; i2 < 3; i2++) {
@@ -327,9 +331,9 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
       }
       if (c.ncl > 0 && a.cldz > 0) {
         const float v = (float)((z - a.clz) / a.cldz);
-        L.aux[s] = expf(-0.5f * v * v);
+        L.f.aux[s] = expf(-0.5f * v * v);
       } else {
-        L.aux[s] = 0.0;
+        L.f.aux[s] = 0.f;
       }
       // geometry kept for lon/lat of the points that need them
       if (n == 0)
@@ -413,12 +417,16 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
         for (int k = 0; k < 3; k++) ex1[k] /= nn;
       }
     }
-    float D[3];
-    for (int k = 0; k < 3; k++) D[k] = 0.5f * step * (ef[k] + (float)ex1[k]);
+    float D[3], efn[3];
+    for (int k = 0; k < 3; k++) {
+      efn[k] = (float)ex1[k];
+      D[k] = 0.5f * step * (ef[k] + efn[k]);
+    }
     const float dzs = dz_of(xh, rf, D);
     for (int k = 0; k < 3; k++) {
       x[k] += (double)D[k];
       ex0[k] = ex1[k];
+      ef[k] = efn[k];
     }
     z += dzs;
   }
@@ -527,12 +535,13 @@ __device__ void copy_base_geometry(const CtlDev& c, const BatchDev& b, const Los
   double z0 = 0;
   for (int ip = 0; ip < n; ip++) {
     const long long q = ob + ip, s = base + ip;
-    const double z = L.z[q], p = L.p[q], t = L.t[q], ds = L.ds[q];
+    const double z = L.z[q];
+    const float pf = L.f.p[q], tf = L.f.t[q], dsf = L.f.ds[q];
     L.z[s] = z;
-    L.p[s] = p;
-    L.t[s] = t;
-    L.ds[s] = ds;
-    L.aux[s] = L.aux[q];
+    L.f.p[s] = pf;
+    L.f.t[s] = tf;
+    L.f.ds[s] = dsf;
+    L.f.aux[s] = L.f.aux[q];
     const int i = R.lev[q];
     if (i != qc_level) {  // the walk's level values and slopes
       qc_level = i;
@@ -546,15 +555,14 @@ __device__ void copy_base_geometry(const CtlDev& c, const BatchDev& b, const Los
       }
     }
     const float dl = (float)(z - z0);
-    const float pf = (float)p, tf = (float)t, dsf = (float)ds;
     for (int ig = 0; ig < c.ng; ig++) {
       const float v = qk_at(qc[ig * kTraceThreads], qc[(nqk + ig) * kTraceThreads], dl);
-      if (ig == c.ig_h2o) L.qh2o[s] = v;
-      L.u[ig * L.cap + s] = col_density(v, pf, tf, dsf);
+      if (ig == c.ig_h2o) L.f.qh2o[s] = v;
+      L.f.u[ig * L.cap + s] = col_density(v, pf, tf, dsf);
     }
     for (int iw = 0; iw < c.nw; iw++)
-      L.kw[iw * L.cap + s] = qk_at(qc[(c.ng + iw) * kTraceThreads],
-                                   qc[(nqk + c.ng + iw) * kTraceThreads], dl);
+      L.f.kw[iw * L.cap + s] = qk_at(qc[(c.ng + iw) * kTraceThreads],
+                                     qc[(nqk + c.ng + iw) * kTraceThreads], dl);
   }
 }
 
@@ -589,6 +597,7 @@ __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, const int* order,
   gk.want_p1 = false;
   gk.imin = 0;
   gk.zmin_seen = 0;
+  gk.ds_clip = 0;
   for (int i = 0; i < 3; i++) gk.x_m1[i] = gk.x_p1[i] = gk.x_first[i] = gk.x_last[i] = 0;
   // mode 1: points [0, m) are the base's (final values); the walk goes on
   // from the base's state at m, its lon/lat bookkeeping restated from the
@@ -607,13 +616,13 @@ __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, const int* order,
     for (int ip = 0; ip < m; ip++) {
       const long long q = ob + ip, s = base + ip;
       L.z[s] = L.z[q];
-      L.p[s] = L.p[q];
-      L.t[s] = L.t[q];
-      L.ds[s] = L.ds[q];
-      L.aux[s] = L.aux[q];
-      if (c.ig_h2o >= 0) L.qh2o[s] = L.qh2o[q];
-      for (int ig = 0; ig < c.ng; ig++) L.u[ig * L.cap + s] = L.u[ig * L.cap + q];
-      for (int iw = 0; iw < c.nw; iw++) L.kw[iw * L.cap + s] = L.kw[iw * L.cap + q];
+      L.f.p[s] = L.f.p[q];
+      L.f.t[s] = L.f.t[q];
+      L.f.ds[s] = L.f.ds[q];
+      L.f.aux[s] = L.f.aux[q];
+      if (c.ig_h2o >= 0) L.f.qh2o[s] = L.f.qh2o[q];
+      for (int ig = 0; ig < c.ng; ig++) L.f.u[ig * L.cap + s] = L.f.u[ig * L.cap + q];
+      for (int iw = 0; iw < c.nw; iw++) L.f.kw[iw * L.cap + s] = L.f.kw[iw * L.cap + q];
     }
     wf.n = m;
     for (int i = 0; i < 3; i++) {
@@ -656,11 +665,15 @@ __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, const int* order,
     return;
   }
   const double* z = L.z + base;
-  double* ds = L.ds + base;
+  float* ds = L.f.ds + base;
   if (ROLE == 1)  // raw segment lengths, for the perturbations walking on
     for (int ip = 0; ip < n; ip++) R.dsr[base + ip] = ds[ip];
-  // raw segment length of point ip (the base's before m)
-  auto ds_raw = [&](int ip) { return ip < m ? R.dsr[ob + ip] : ds[ip]; };
+  // raw segment length of point ip (the base's before m; the clipped last
+  // segment in FP64)
+  auto ds_raw = [&](int ip) -> double {
+    if (ip == n - 2) return gk.ds_clip;
+    return ip < m ? (double)R.dsr[ob + ip] : (double)ds[ip];
+  };
   double dummy, lon0, lat0, lonl, latl;
   to_geo(gk.x_first, &dummy, &lon0, &lat0);
   to_geo(gk.x_last, &dummy, &lonl, &latl);
@@ -696,28 +709,28 @@ __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, const int* order,
   // trapezoid segment lengths (points before m hold the base's)
   float prev;
   if (m > 0) {
-    prev = (float)R.dsr[ob + m - 1];
+    prev = R.dsr[ob + m - 1];
   } else {
-    prev = (float)ds[0];
+    prev = ds[0];
     ds[0] = 0.5f * prev;
   }
   for (int ip = m > 0 ? m : 1; ip < n; ip++) {
-    const float cur = (float)ds[ip];
+    const float cur = ds[ip];
     ds[ip] = 0.5f * (prev + cur);
     prev = cur;
   }
   // column densities (q stored in the u plane) and Curtis-Godson means
-  const double* p = L.p + base;
-  const double* t = L.t + base;
+  const float* p = L.f.p + base;
+  const float* t = L.f.t + base;
   for (int ig = 0; ig < c.ng; ig++) {
-    double* u = L.u + ig * L.cap + base;
-    double* cgu = L.cga ? L.cgu + ig * L.cap + base : nullptr;
-    double* cgp = L.cga ? L.cgp + ig * L.cap + base : nullptr;
-    double* cgt = L.cga ? L.cgt + ig * L.cap + base : nullptr;
+    float* u = L.f.u + ig * L.cap + base;
+    float* cgu = L.cga ? L.f.cgu + ig * L.cap + base : nullptr;
+    float* cgp = L.cga ? L.f.cgp + ig * L.cap + base : nullptr;
+    float* cgt = L.cga ? L.f.cgt + ig * L.cap + base : nullptr;
     float su = 0.f, sp = 0.f, st = 0.f, cu = 0.f, cp = 0.f, ct = 0.f;
     for (int ip = m; ip < n; ip++) {
-      const float pf = (float)p[ip], tf = (float)t[ip];
-      const float uu = col_density((float)u[ip], pf, tf, (float)ds[ip]);
+      const float pf = p[ip], tf = t[ip];
+      const float uu = col_density(u[ip], pf, tf, ds[ip]);
       u[ip] = uu;
       if (cgu) {
         // compensated running sums
