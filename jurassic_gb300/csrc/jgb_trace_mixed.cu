@@ -151,7 +151,8 @@ __device__ inline float dz_of(const float* xh, float r, const float* d) {
 struct GeoKeep {
   double x_first[3], x_m1[3], x_p1[3], x_last[3];
   double zmin_seen;
-  double ds_clip;  // the clipped last segment (point n - 2) in FP64
+  double ds_clip;     // the clipped last segment (point n - 2) in FP64
+  float ds_m, ds_p1;  // raw segment lengths of the lowest point and the next
   int imin;
   bool want_p1;
 };
@@ -164,6 +165,7 @@ struct WalkFrom {
   double x[3], e[3], z;
   double x_last[3], z_last;
   int lev_last;
+  float raw_last;  // raw segment length of the previous point
 };
 
 // Mixing ratio or extinction at offset dl in a level interval, from the
@@ -183,10 +185,22 @@ __device__ __forceinline__ float col_density(float q, float p, float t, float ds
 // level caches in shared memory with this stride).
 constexpr int kTraceThreads = 64;
 
-// qc: the fill pass's cache of the current level's emitter and window values
-// and slopes (qc[k * kTraceThreads], qc[(ng + nw + k) * kTraceThreads]).
-// ROLE 1 keeps every point's position, direction and level interval in sv;
-// ROLE 2 with wf walks on from the state wf (a base ray's walk).
+// Per-thread shared memory of the fill pass, stride kTraceThreads: the
+// current level's emitter and window values and slopes (qc[k], qc[nqk + k],
+// nqk = ng + nw), the mixing ratios of the point waiting for its trapezoid
+// length (pq[ig]) and, in CGA, the running compensated sums (cg[6 ig + j]).
+__host__ __device__ inline int trace_smem_floats(const CtlDev& c) {
+  return 2 * (c.ng + c.nw) + c.ng + (c.formod == 0 ? 6 * c.ng : 0);
+}
+
+// STORE places every point with its final values: its trapezoid length
+// 0.5 (ds_(i-1) + ds_i), column densities 10 / k_B q p / T ds and CGA sums
+// are written when the next point is placed (the clip of the last segment
+// changes the previous point's raw length), so the walk keeps the raw
+// lengths of the last two points.
+// ROLE 1 keeps every point's position, direction, raw length and level
+// interval in sv; ROLE 2 with wf walks on from the state wf (a base ray's
+// walk).
 template <bool STORE, int ROLE = 0>
 __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long nray, int r,
                       const LosDev& L, long long base, int cap, double* sft_out, GeoKeep* gk,
@@ -260,6 +274,49 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
   const float rayds = (float)c.rayds, raydz = (float)c.raydz;
   // the direction in FP32 (carried from the previous step's conversion)
   float ef[3] = {(float)ex0[0], (float)ex0[1], (float)ex0[2]};
+  // the point waiting for its final values (STORE): raw lengths of it and
+  // of the point before, its p and T; its mixing ratios in pq
+  float* pq = STORE ? qc + 2 * nqk * kTraceThreads : nullptr;
+  float* cg = STORE ? pq + c.ng * kTraceThreads : nullptr;
+  float raw_before = 0.f, raw_pend = 0.f, pend_p = 0.f, pend_t = 0.f;
+  const int n0 = n;
+  if (ROLE == 2 && wf) raw_pend = wf->raw_last;
+  if (STORE && L.cga)
+    for (int k = 0; k < 6 * c.ng; k++) cg[k * kTraceThreads] = 0.f;
+  auto finalize = [&](int k) {
+    const long long sk = base + k;
+    const float dsT = k == 0 ? 0.5f * raw_pend : 0.5f * (raw_before + raw_pend);
+    L.f.ds[sk] = dsT;
+    for (int ig = 0; ig < c.ng; ig++) {
+      const float uu = col_density(pq[ig * kTraceThreads], pend_p, pend_t, dsT);
+      L.f.u[ig * L.cap + sk] = uu;
+      if (L.cga) {  // compensated running sums
+        float* q = cg + 6 * ig * kTraceThreads;
+        float su = q[0], sp = q[kTraceThreads], st = q[2 * kTraceThreads];
+        float cu = q[3 * kTraceThreads], cp = q[4 * kTraceThreads], ct = q[5 * kTraceThreads];
+        float y = uu - cu, s2 = su + y;
+        cu = (s2 - su) - y;
+        su = s2;
+        y = uu * pend_p - cp;
+        s2 = sp + y;
+        cp = (s2 - sp) - y;
+        sp = s2;
+        y = uu * pend_t - ct;
+        s2 = st + y;
+        ct = (s2 - st) - y;
+        st = s2;
+        q[0] = su;
+        q[kTraceThreads] = sp;
+        q[2 * kTraceThreads] = st;
+        q[3 * kTraceThreads] = cu;
+        q[4 * kTraceThreads] = cp;
+        q[5 * kTraceThreads] = ct;
+        L.f.cgu[ig * L.cap + sk] = su;
+        L.f.cgp[ig * L.cap + sk] = sp / su;
+        L.f.cgt[ig * L.cap + sk] = st / su;
+      }
+    }
+  };
   for (;;) {
     // radial unit vector and radius at x
     const double rr = z + kRE;
@@ -286,7 +343,8 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
       for (int i = 0; i < 3; i++) x[i] = x_last[i] + frac * (x[i] - x_last[i]);
       z = last_z + frac * (z - last_z);
       const double dsc = (double)step * frac;
-      L.f.ds[base + n - 1] = (float)dsc;
+      raw_pend = (float)dsc;
+      if (ROLE == 1) sv->dsr[base + n - 1] = raw_pend;
       gk->ds_clip = dsc;
       step = 0.f;
     }
@@ -298,11 +356,15 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
     float p, t;
     lev_pt(lv, dl, &p, &t);
     if (STORE) {
+      if (n > n0) finalize(n - 1);
       const long long s = base + n;
       L.z[s] = z;
       L.f.p[s] = p;
       L.f.t[s] = t;
-      L.f.ds[s] = step;
+      raw_before = raw_pend;
+      raw_pend = step;
+      pend_p = p;
+      pend_t = t;
       const int i = lv.i;
       if (i != qc_level) {  // a new level: its values and slopes q0 + (q1 - q0) / dz * dl
         qc_level = i;
@@ -315,7 +377,7 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
       }
       for (int ig = 0; ig < c.ng; ig++) {
         const float v = qk_at(qc[ig * kTraceThreads], qc[(nqk + ig) * kTraceThreads], dl);
-        L.f.u[ig * L.cap + s] = v;
+        pq[ig * kTraceThreads] = v;
         if (ig == c.ig_h2o) L.f.qh2o[s] = v;
       }
       for (int iw = 0; iw < c.nw; iw++)
@@ -328,6 +390,7 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
           sv->es[i2 * bp + s] = ex0[i2];
         }
         sv->lev[s] = i;
+        sv->dsr[s] = step;
       }
       if (c.ncl > 0 && a.cldz > 0) {
         const float v = (float)((z - a.clz) / a.cldz);
@@ -340,11 +403,13 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
         for (int i2 = 0; i2 < 3; i2++) gk->x_first[i2] = x[i2];
       if (gk->want_p1) {
         for (int i2 = 0; i2 < 3; i2++) gk->x_p1[i2] = x[i2];
+        gk->ds_p1 = step;
         gk->want_p1 = false;
       }
       if (n == 0 || z < gk->zmin_seen) {
         gk->zmin_seen = z;
         gk->imin = n;
+        gk->ds_m = step;
         for (int i2 = 0; i2 < 3; i2++) gk->x_m1[i2] = x_last[i2];   // the previous point
         gk->want_p1 = true;
       }
@@ -355,8 +420,10 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
     if (stop) {
       if (c.nsf > 0 && a.sft > 0) t = (float)a.sft;
       *sft_out = (stop == 2 ? (c.nsf > 0 && a.sft > 0 ? a.sft : (double)t) : -999);
-      if (STORE)
+      if (STORE) {
         for (int i2 = 0; i2 < 3; i2++) gk->x_last[i2] = x[i2];
+        finalize(n - 1);
+      }
       break;
     }
     // refraction (jurassic.c:4388-4415): ex1 = (n ex0 + ds grad N) / |...|
@@ -585,7 +652,7 @@ __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, const int* order,
   const AtmM a = atm_m(b, c, b.ray_obs[r]);
   const long long base = L.off[r];
   const int cap = L.count[r];
-  __shared__ float qcache[2 * (kMaxG + kMaxW) * kTraceThreads];
+  extern __shared__ float qcache[];  // trace_smem_floats(c) per thread
   int4 pl = make_int4(-1, 0, 0, 0);
   if (ROLE == 2) pl = R.plan[r];
   if (ROLE == 2 && pl.z == 2) {
@@ -598,6 +665,7 @@ __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, const int* order,
   gk.imin = 0;
   gk.zmin_seen = 0;
   gk.ds_clip = 0;
+  gk.ds_m = gk.ds_p1 = 0.f;
   for (int i = 0; i < 3; i++) gk.x_m1[i] = gk.x_p1[i] = gk.x_first[i] = gk.x_last[i] = 0;
   // mode 1: points [0, m) are the base's (final values); the walk goes on
   // from the base's state at m, its lon/lat bookkeeping restated from the
@@ -634,6 +702,7 @@ __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, const int* order,
     wf.z = L.z[ob + m];
     wf.z_last = L.z[ob + m - 1];
     wf.lev_last = R.lev[ob + m - 1];
+    wf.raw_last = R.dsr[ob + m - 1];
     // the first lowest point so far and its neighbours
     int imin = 0;
     double zmin = L.z[ob];
@@ -645,6 +714,8 @@ __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, const int* order,
     gk.imin = imin;
     gk.zmin_seen = zmin;
     gk.want_p1 = imin == m - 1;
+    gk.ds_m = R.dsr[ob + imin];
+    if (imin + 1 < m) gk.ds_p1 = R.dsr[ob + imin + 1];
     for (int i = 0; i < 3; i++) {
       gk.x_m1[i] = imin > 0 ? R.xs[i * bp + ob + imin - 1] : 0.0;
       gk.x_p1[i] = imin + 1 < m ? R.xs[i * bp + ob + imin + 1] : 0.0;
@@ -665,19 +736,10 @@ __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, const int* order,
     return;
   }
   const double* z = L.z + base;
-  float* ds = L.f.ds + base;
-  if (ROLE == 1)  // raw segment lengths, for the perturbations walking on
-    for (int ip = 0; ip < n; ip++) R.dsr[base + ip] = ds[ip];
-  // raw segment length of point ip (the base's before m; the clipped last
-  // segment in FP64)
-  auto ds_raw = [&](int ip) -> double {
-    if (ip == n - 2) return gk.ds_clip;
-    return ip < m ? (double)R.dsr[ob + ip] : (double)ds[ip];
-  };
   double dummy, lon0, lat0, lonl, latl;
   to_geo(gk.x_first, &dummy, &lon0, &lat0);
   to_geo(gk.x_last, &dummy, &lonl, &latl);
-  // tangent point (tangent_point, jurassic.c:5223-5263), before trapezoid
+  // tangent point (tangent_point, jurassic.c:5223-5263) from the raw lengths
   const int imin = gk.imin;
   if (imin <= 0 || imin >= n - 1) {
     tp[0 * nr + r] = z[n - 1];
@@ -685,7 +747,9 @@ __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, const int* order,
     tp[2 * nr + r] = latl;
   } else {
     const double y0 = z[imin - 1], y1 = z[imin], y2 = z[imin + 1];
-    const double d1 = ds_raw(imin), d2 = ds_raw(imin + 1);
+    // raw segment lengths (the clipped last one, of point n - 2, in FP64)
+    const double d1 = imin == n - 2 ? gk.ds_clip : (double)gk.ds_m;
+    const double d2 = imin + 1 == n - 2 ? gk.ds_clip : (double)gk.ds_p1;
     const double x1 = sqrt(d1 * d1 - (y1 - y0) * (y1 - y0));
     const double x2 = x1 + sqrt(d2 * d2 - (y2 - y1) * (y2 - y1));
     const double aa = 1 / (x1 - x2) * (-(y0 - y1) / x1 + (y0 - y2) / x2);
@@ -706,51 +770,6 @@ __global__ void k_trace_fill_m(CtlDev c, BatchDev b, LosDev L, const int* order,
   e[3] = z[n - 1];
   e[4] = lonl;
   e[5] = latl;
-  // trapezoid segment lengths (points before m hold the base's)
-  float prev;
-  if (m > 0) {
-    prev = R.dsr[ob + m - 1];
-  } else {
-    prev = ds[0];
-    ds[0] = 0.5f * prev;
-  }
-  for (int ip = m > 0 ? m : 1; ip < n; ip++) {
-    const float cur = ds[ip];
-    ds[ip] = 0.5f * (prev + cur);
-    prev = cur;
-  }
-  // column densities (q stored in the u plane) and Curtis-Godson means
-  const float* p = L.f.p + base;
-  const float* t = L.f.t + base;
-  for (int ig = 0; ig < c.ng; ig++) {
-    float* u = L.f.u + ig * L.cap + base;
-    float* cgu = L.cga ? L.f.cgu + ig * L.cap + base : nullptr;
-    float* cgp = L.cga ? L.f.cgp + ig * L.cap + base : nullptr;
-    float* cgt = L.cga ? L.f.cgt + ig * L.cap + base : nullptr;
-    float su = 0.f, sp = 0.f, st = 0.f, cu = 0.f, cp = 0.f, ct = 0.f;
-    for (int ip = m; ip < n; ip++) {
-      const float pf = p[ip], tf = t[ip];
-      const float uu = col_density(u[ip], pf, tf, ds[ip]);
-      u[ip] = uu;
-      if (cgu) {
-        // compensated running sums
-        float y = uu - cu, s2 = su + y;
-        cu = (s2 - su) - y;
-        su = s2;
-        y = uu * pf - cp;
-        s2 = sp + y;
-        cp = (s2 - sp) - y;
-        sp = s2;
-        y = uu * tf - ct;
-        s2 = st + y;
-        ct = (s2 - st) - y;
-        st = s2;
-        cgu[ip] = su;
-        cgp[ip] = sp / su;
-        cgt[ip] = st / su;
-      }
-    }
-  }
 }
 
 }  // namespace
@@ -770,8 +789,9 @@ void launch_los_bound_mixed(const CtlDev& c, const BatchDev& b, double scale, in
 void launch_trace_fill_mixed(const CtlDev& c, const BatchDev& b, const LosDev& L, const int* order,
                              unsigned* err, cudaStream_t s) {
   const int bs = kTraceThreads;
-  k_trace_fill_m<0><<<(b.nray + bs - 1) / bs, bs, 0, s>>>(c, b, L, order, 0, b.nray,
-                                                           TraceResume{}, err);
+  const size_t smem = sizeof(float) * trace_smem_floats(c) * kTraceThreads;
+  k_trace_fill_m<0><<<(b.nray + bs - 1) / bs, bs, smem, s>>>(c, b, L, order, 0, b.nray,
+                                                              TraceResume{}, err);
 }
 
 int trace_fill_resident(int sms) {
@@ -792,10 +812,11 @@ void launch_trace_fill_resumed(const CtlDev& c, const BatchDev& b, const LosDev&
                                unsigned* err, cudaStream_t s) {
   const int bs = kTraceThreads;
   if (nr <= 0) return;
+  const size_t smem = sizeof(float) * trace_smem_floats(c) * kTraceThreads;
   if (role == 1)
-    k_trace_fill_m<1><<<(nr + bs - 1) / bs, bs, 0, s>>>(c, b, L, order, r0, nr, R, err);
+    k_trace_fill_m<1><<<(nr + bs - 1) / bs, bs, smem, s>>>(c, b, L, order, r0, nr, R, err);
   else
-    k_trace_fill_m<2><<<(nr + bs - 1) / bs, bs, 0, s>>>(c, b, L, order, r0, nr, R, err);
+    k_trace_fill_m<2><<<(nr + bs - 1) / bs, bs, smem, s>>>(c, b, L, order, r0, nr, R, err);
 }
 
 }  // namespace jgb
