@@ -144,13 +144,14 @@ def peaks():
 # channels, 5 emitters), from one capture of the 4000-observation launch
 # with the same channels, emitters and tables (the nadir observations are
 # alike, so the counters scale with the LOS points):
-#   ncu --set full --clock-control none -k regex:k_path_mixed -s 14 -c 1 -o path \
-#       python bench.py --nobs 4000 --steps 2 --warmup 1 --fp64-steps 0 --no-cpu \
-#       --serve-requests 0 --no-extra
-#   smsp__inst_executed.sum 3.2978e10, dram__bytes_read.sum + write.sum 769.9 MB,
+#   JGB_PATH_VARIANT=14 ncu --set full --clock-control none -k regex:k_path_mixed \
+#       -s 1 -c 1 -o path python bench.py --nobs 4000 --steps 2 --warmup 1 \
+#       --fp64-steps 0 --no-cpu --serve-requests 0 --no-extra
+#   (variant 14: the one the autotuner picks on the 1e5-observation launch)
+#   smsp__inst_executed.sum 3.2978e10, dram__bytes_read.sum + write.sum 862.5 MB,
 #   4,004,179 LOS points in the launch.
 PATH_NCU_NADIR = {"warp_inst_per_los_point": 32978257734 / 4004179,
-                  "dram_bytes_per_los_point": 769.919232e6 / 4004179}
+                  "dram_bytes_per_los_point": 862.547456e6 / 4004179}
 
 
 def sm_count(device=0):
