@@ -795,15 +795,16 @@ void launch_trace_fill_mixed(const CtlDev& c, const BatchDev& b, const LosDev& L
 }
 
 int trace_fill_resident(int sms) {
-  static int per_sm = 0;
-  if (per_sm == 0) {
+  // blocks per SM are set by the registers (the shared memory of a few
+  // emitters does not bind); computed once, thread-safely
+  static const int per_sm = [] {
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_trace_fill_m<2>, kTraceThreads, 0) !=
             cudaSuccess ||
         nb < 1)
       nb = 1;
-    per_sm = nb * kTraceThreads;
-  }
+    return nb * kTraceThreads;
+  }();
   return per_sm * sms;
 }
 
