@@ -20,7 +20,10 @@
 //    (first, last and the neighbours of the lowest point, for the tangent
 //    point and the solar geometry);
 //  * trapezoid lengths, column densities and Curtis-Godson sums in FP32
-//    (compensated sums).
+//    (compensated sums), written by the walk itself when the next point is
+//    placed; the point data go to FP32 planes (z stays FP64);
+//  * finite-difference perturbations in large EGA batches take their base
+//    ray's geometry or walk on from the base's walk (TraceResume).
 // The count and fill passes share the walk, so they agree on the point count.
 #include "jgb_common.cuh"
 #include "jgb_internal.h"
