@@ -185,6 +185,10 @@ int jgb_set_path_split(jgb_ctx *ctx, int mode);
    chunks then take those emitters' segment emissivities from the base's
    walk and compute only the perturbed one, where at least 30 % of the
    perturbed lookups can be shared (mode 3: always resume and always share).
+   In EGA, modes 2 and 3 also trace the perturbed rays from their bases'
+   walks (a perturbed mixing ratio or extinction takes the base's geometry,
+   a perturbed temperature walks on from the base's state); mode 1 does so
+   only for chunks of at least four waves of the trace kernel.
    The results do not depend on it. */
 int jgb_set_fd_resume(jgb_ctx *ctx, int mode);
 
