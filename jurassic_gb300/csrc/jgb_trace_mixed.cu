@@ -188,6 +188,20 @@ __device__ __forceinline__ float col_density(float q, float p, float t, float ds
 // level caches in shared memory with this stride).
 constexpr int kTraceThreads = 64;
 
+// The emitter and window values of level i and their slopes (v1 - v0) / dz
+// over interval i, into the per-thread cache qc (stride kTraceThreads):
+// qc[k] = v0, qc[nqk + k] = slope, nqk = ng + nw.
+__device__ __forceinline__ void level_values(const CtlDev& c, const AtmM& a, int i, float dz,
+                                             float* qc) {
+  const int nqk = c.ng + c.nw;
+  for (int k = 0; k < nqk; k++) {
+    const double* src = k < c.ng ? a.q + k * a.stride : a.k + (k - c.ng) * a.stride;
+    const float v0 = (float)src[i], v1 = (float)src[i + 1];
+    qc[k * kTraceThreads] = v0;
+    qc[(nqk + k) * kTraceThreads] = (v1 - v0) / dz;
+  }
+}
+
 // Per-thread shared memory of the fill pass, stride kTraceThreads: the
 // current level's emitter and window values and slopes (qc[k], qc[nqk + k],
 // nqk = ng + nw), the mixing ratios of the point waiting for its trapezoid
@@ -371,12 +385,7 @@ __device__ int walk_m(const CtlDev& c, const AtmM& a, const double* g, long long
       const int i = lv.i;
       if (i != qc_level) {  // a new level: its values and slopes q0 + (q1 - q0) / dz * dl
         qc_level = i;
-        for (int k = 0; k < nqk; k++) {
-          const double* src = k < c.ng ? a.q + k * a.stride : a.k + (k - c.ng) * a.stride;
-          const float v0 = (float)src[i], v1 = (float)src[i + 1];
-          qc[k * kTraceThreads] = v0;
-          qc[(nqk + k) * kTraceThreads] = (v1 - v0) / lv.dz;
-        }
+        level_values(c, a, i, lv.dz, qc);
       }
       for (int ig = 0; ig < c.ng; ig++) {
         const float v = qk_at(qc[ig * kTraceThreads], qc[(nqk + ig) * kTraceThreads], dl);
@@ -616,13 +625,7 @@ __device__ void copy_base_geometry(const CtlDev& c, const BatchDev& b, const Los
     if (i != qc_level) {  // the walk's level values and slopes
       qc_level = i;
       z0 = a.z[i];
-      const float dz = (float)(a.z[i + 1] - a.z[i]);
-      for (int k = 0; k < nqk; k++) {
-        const double* src = k < c.ng ? a.q + k * a.stride : a.k + (k - c.ng) * a.stride;
-        const float v0 = (float)src[i], v1 = (float)src[i + 1];
-        qc[k * kTraceThreads] = v0;
-        qc[(nqk + k) * kTraceThreads] = (v1 - v0) / dz;
-      }
+      level_values(c, a, i, (float)(a.z[i + 1] - a.z[i]), qc);
     }
     const float dl = (float)(z - z0);
     for (int ig = 0; ig < c.ng; ig++) {
