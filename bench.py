@@ -522,6 +522,14 @@ def run_serving(args, device):
     closed = serving.serve(engine(native.MIXED), ctl, reqs, np.inf)
     rate = args.serve_load * closed["retrievals_per_s"]
     pois = serving.serve(engine(native.MIXED), ctl, reqs, rate, seed=7)
+    # latency against offered load (the same requests, the same arrival seed)
+    sweep = []
+    for load in sorted({float(v) for v in args.serve_sweep.split(",") if v.strip()} | {args.serve_load}):
+        r = pois if load == args.serve_load else serving.serve(
+            engine(native.MIXED), ctl, reqs, load * closed["retrievals_per_s"], seed=7)
+        sweep.append({"load": load, "rate_hz": r["rate_hz"], "retrievals_per_s": r["retrievals_per_s"],
+                      "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"], "mean_ms": r["mean_ms"],
+                      "steps": r["steps"]})
     m = min(m, n)
     sub_mixed = closed if m == n else serving.serve(engine(native.MIXED), ctl, reqs[:m], np.inf)
     sub_fp64 = serving.serve(engine(native.FP64), ctl, reqs[:m], np.inf)
@@ -532,6 +540,7 @@ def run_serving(args, device):
     out.update({
         "mixed_closed_loop": strip(closed),
         "mixed_poisson": dict(strip(pois), load=args.serve_load),
+        "mixed_poisson_sweep": sweep,
         "fp64_closed_loop": dict(strip(sub_fp64), requests=m),
         "mixed_closed_loop_same_requests": dict(strip(sub_mixed), requests=m),
         "retrievals_per_s_mixed_over_fp64": sub_mixed["retrievals_per_s"] / sub_fp64["retrievals_per_s"],
@@ -702,6 +711,9 @@ def main():
                          "the mixed/FP64 retrievals/s ratio and the accuracy")
     ap.add_argument("--serve-load", type=float, default=0.7,
                     help="Poisson arrival rate as a fraction of the closed-loop capacity")
+    ap.add_argument("--serve-sweep", default="0.3,0.5",
+                    help="further Poisson loads (fractions of the closed-loop capacity) for the "
+                         "latency-load curve; empty: none")
     ap.add_argument("--serve-budget-gb", type=float, default=64.0)
     args = ap.parse_args()
 
