@@ -365,11 +365,12 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
   // or in FP64, the rays are counted first (count, scan, fill).
   const long long slab = c.nlos_max;
   // resumed perturbations (EGA; the Curtis-Godson sums run from the first
-  // point) are traced from their base rays' walks (TraceResume).  The base
-  // rays are then traced before the others, which adds a whole walk to the
-  // critical path: in the automatic mode this pays only where the perturbed
-  // rays take several waves of the fill kernel (a batch within one wave
-  // takes as long as its longest walk).
+  // point) can be traced from their base rays' walks (TraceResume).  The
+  // base rays are then traced before the others, which adds a whole walk to
+  // the critical path (a batch within one wave takes as long as its longest
+  // walk): measured, it gains nothing on a 1.3-wave Jacobian chunk and loses
+  // on serving batches, so the automatic mode keeps it for batches of at
+  // least four waves of the fill kernel; modes 2 and 3 force it.
   bool tres = x->resume && precision == JGB_MIXED && c.formod != 0;
   if (tres && x->fd_resume == 1) {
     const int nbr = x->resume->h_ray_off[x->resume->nbase];
@@ -472,7 +473,7 @@ int jgb::run_core(jgb_ctx* x, BatchDev& b, int precision, bool timed_h2d) {
       bpts = std::max(bpts, 1LL);
       auto a16 = [](size_t v) { return (v + 15) & ~size_t(15); };
       const size_t o_es = a16(sizeof(double) * 3 * (size_t)bpts);
-      const size_t o_ds = o_es + o_es, o_lev = o_ds + a16(sizeof(double) * (size_t)bpts);
+      const size_t o_ds = o_es + o_es, o_lev = o_ds + a16(sizeof(float) * (size_t)bpts);
       const size_t o_plan = o_lev + a16(sizeof(int) * (size_t)bpts);
       const size_t o_key = o_plan + a16(sizeof(int4) * (size_t)nray);
       const size_t nk = (size_t)std::max(npr, 1);
