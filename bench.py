@@ -430,6 +430,47 @@ def run_jacobian(args, rank, world, local, pg):
         print(json.dumps(line), flush=True)
 
 
+def invert_measure(ctx, L, nmat, n, steps, warmup):
+    """FP64 inverse of nmat symmetric positive-definite n x n matrices
+    (matrix_invert, retrieval.c:373-399: Cholesky factor and inverse) through
+    jgb_matrix_invert_dev: a-priori covariances with exponential
+    correlation (seeded heights, sigmas and correlation lengths) like the
+    retrieval's S_a.  Algorithmic flops n^3 per matrix (factor n^3/3,
+    inverse from the factor 2 n^3/3); the FP64 peak is GB300's nominal
+    1.25 TFLOP/s (no FP64 figure is measured for the pool)."""
+    import ctypes as C
+    rng = np.random.default_rng(12)
+    z = np.sort(rng.uniform(0, 60, (nmat, n)), axis=1)
+    sig = rng.uniform(1, 3, (nmat, n))
+    cz = rng.uniform(1, 5, (nmat, 1, 1))
+    mats = np.ascontiguousarray(sig[:, :, None] * sig[:, None, :] *
+                                np.exp(-np.abs(z[:, :, None] - z[:, None, :]) / cz))
+    dA = L.jgb_dev_alloc(mats.nbytes)
+    ni = np.full(nmat, n, np.int32)
+    st = np.zeros(nmat, np.int32)
+    times = []
+    for _ in range(warmup + steps):
+        L.jgb_memcpy_h2d(dA, mats.ctypes.data, mats.nbytes)
+        kms = C.c_float(0)
+        ctx._check(L.jgb_matrix_invert_dev(ctx.h, nmat, ni.ctypes.data_as(C.POINTER(C.c_int)), dA,
+                                           st.ctypes.data_as(C.POINTER(C.c_int)), C.byref(kms)))
+        times.append(kms.value)
+    out = np.zeros_like(mats)
+    L.jgb_memcpy_d2h(out.ctypes.data, dA, out.nbytes)
+    L.jgb_dev_free(dA)
+    t = statistics.mean(times[warmup:])
+    flops = float(n) ** 3 * nmat
+    dev = max(float(np.max(np.abs(out[k] - np.linalg.inv(mats[k]))) /
+                    np.max(np.abs(np.linalg.inv(mats[k])))) for k in range(4))
+    peak = 1250.0
+    return {"matrices": nmat, "n": n, "kernel_ms": t, "gflops": flops / (t / 1e3) / 1e9,
+            "flops_per_matrix": float(n) ** 3, "not_positive_definite": int(np.sum(st)),
+            "max_rel_vs_numpy_first4": dev,
+            "roofline": {"bound": "fp64", "achieved": flops / (t / 1e3) / 1e9, "peak": peak,
+                         "unit": "GFLOP/s", "frac": flops / (t / 1e3) / 1e9 / peak,
+                         "peak_kind": "nominal"}}
+
+
 def run_normal(args, rank, world, local, pg):
     """Normal-equation products alone (matrix_product, retrieval.c:403-444):
     nobs problems with m = 150 measurements and n = 405 state elements
@@ -482,6 +523,7 @@ def run_normal(args, rank, world, local, pg):
         bf16, kind = 1900.0, "fallback"
     peak = bf16 / 2 / 3
     rel = float(np.max(np.abs(A["mixed_3xtf32"] - A["fp64"])) / np.max(np.abs(A["fp64"])))
+    inv = invert_measure(ctx, L, min(nobs, 512), n_, args.steps, args.warmup)
     if rank == 0:
         v = res["mixed_3xtf32"]["tflops"]
         print(json.dumps({
@@ -493,6 +535,7 @@ def run_normal(args, rank, world, local, pg):
             "config": {"workload": "normal_equations_%dx(150x405)" % nobs,
                        "l2_policy": "K (%.0f MB) larger than L2; no flush" % (K.nbytes / 1e6)},
             "fp64": res["fp64"], "mixed_vs_fp64_max_rel": rel, "flops_per_step": flops,
+            "matrix_invert": inv,
             "roofline": {"bound": "tensor", "achieved": v, "peak": peak, "unit": "TFLOP/s",
                          "frac": v / peak, "traffic": None, "peak_kind": kind,
                          "peak_note": "bf16 dense / 2 (TF32) / 3 (3xTF32)"}}), flush=True)

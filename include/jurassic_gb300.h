@@ -244,6 +244,20 @@ int jgb_normal_equations_dev(jgb_ctx *ctx, int nret, const int *m, const int *n,
                              const double *K, const double *w, const double *dy, double *A,
                              double *b, int precision, float *kernel_ms);
 
+/* Inverse of nret symmetric positive-definite matrices in place
+   (matrix_invert, retrieval.c:373-399), FP64: a matrix with every element
+   right of the diagonal equal to 0 by its reciprocal diagonal, any other by
+   Cholesky decomposition and inverse (gsl_linalg_cholesky_decomp /
+   gsl_linalg_cholesky_invert), symmetrised.  A holds the concatenated
+   n[i] x n[i] row-major matrices.  status (host, nret entries, may be NULL)
+   gets 1 for a matrix that is not positive definite, which is then left as
+   it was (the reference aborts there), else 0.  At most 65535 matrices. */
+int jgb_matrix_invert(jgb_ctx *ctx, int nret, const int *n, double *A, int *status);
+/* The same on a device buffer A; with kernel_ms != NULL, *kernel_ms is the
+   CUDA-event time of the kernels (descriptor upload excluded). */
+int jgb_matrix_invert_dev(jgb_ctx *ctx, int nret, const int *n, double *A, int *status,
+                          float *kernel_ms);
+
 /* Emitter contributions (TASK c, formod.c:200-249) of every observation of a
    host batch: continua off; variant g < ng keeps only emitter g (all other
    mixing ratios and all extinction zero), variant ng ("EXTINCT") has all

@@ -264,12 +264,15 @@ __global__ void k_chol_factor(int nret, const RetDesc* d, const int* active, dou
   }
 }
 
-__device__ void chol_solve_serial(const double* L, int n, const double* b, double* xs,
-                                  long long stride) {
-  for (int r = 0; r < n; r++) xs[r * stride] = b[r * stride];
-  for (int r = 0; r < n; r++) {
+// L L^T x = e_c (column c of the identity) in place in xs (stride apart).
+// The forward sweep's entries above c are exactly +0 (1 or 0 minus products
+// with zeros), so the sweep starts at row c and its sums at column c: the
+// same values as the full sweep, a third of its work.
+__device__ void chol_solve_unit(const double* L, int n, int c, double* xs, long long stride) {
+  for (int r = 0; r < n; r++) xs[r * stride] = r == c ? 1.0 : 0.0;
+  for (int r = c; r < n; r++) {
     double s = xs[r * stride];
-    for (int k = 0; k < r; k++) s -= L[(long long)r * n + k] * xs[k * stride];
+    for (int k = c; k < r; k++) s -= L[(long long)r * n + k] * xs[k * stride];
     xs[r * stride] = s / L[(long long)r * n + r];
   }
   for (int r = n - 1; r >= 0; r--) {
@@ -328,9 +331,7 @@ __global__ void k_chol_inverse_cols(int nret, const RetDesc* d, const int* activ
   const int n = d[i].n;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= n) return;
-  double* W = work + d[i].so;
-  for (int r = 0; r < n; r++) W[(long long)r * n + c] = (r == c) ? 1.0 : 0.0;
-  chol_solve_serial(L + d[i].so, n, W + c, W + c, n);
+  chol_solve_unit(L + d[i].so, n, c, work + d[i].so + c, n);
 }
 
 __global__ void k_sym_half(int nret, const RetDesc* d, const int* active, const double* work,
@@ -353,6 +354,35 @@ __global__ void k_diag_inverse(int nret, const RetDesc* d, const int* active, do
     double* v = S + d[i].so + (long long)j * d[i].n + j;
     *v = 1 / *v;
   }
+}
+
+// The diagonal test of matrix_invert (retrieval.c:379-385: any element right
+// of the diagonal other than 0, NaN included, makes the matrix full):
+// diag[i] / full[i] select the two branches, status[i] starts at 0.
+__global__ void k_invert_flags(int nret, const RetDesc* d, const double* A, int* diag, int* full,
+                               int* status) {
+  const int i = blockIdx.x;
+  if (i >= nret) return;
+  const int n = d[i].n;
+  const double* M = A + d[i].so;
+  int nz = 0;
+  for (long long e = threadIdx.x; e < (long long)n * n; e += blockDim.x) {
+    const int r = (int)(e / n), c = (int)(e % n);
+    if (c > r && M[e] != 0) nz = 1;
+  }
+  nz = __syncthreads_or(nz);
+  if (threadIdx.x == 0) {
+    diag[i] = !nz;
+    full[i] = nz;
+    status[i] = 0;
+  }
+}
+
+// Matrices whose factor failed (status 1) take no inverse: they keep their
+// input.
+__global__ void k_drop_failed(int nret, const int* status, int* full) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nret && status[i]) full[i] = 0;
 }
 
 // a-priori covariance (set_cov_apr, retrieval.c:808-920): per element
@@ -1817,4 +1847,95 @@ extern "C" int jgb_retrieve_batch(jgb_ctx* x, const jgb_ret* ret, const jgb_batc
   jgb_engine_destroy(E);
   if (first_err == JGB_ERR_NUMERIC) return ctx_error(x, first_err, "normal matrix is not positive definite");
   return first_err;
+}
+
+// Batched matrix_invert (retrieval.c:373-399) on the device: the diagonal
+// test, reciprocal diagonals, and for the other matrices the engine's
+// Cholesky factor and column-solve inverse, symmetrised.
+extern "C" int jgb_matrix_invert_dev(jgb_ctx* x, int nret, const int* n, double* A, int* status,
+                                     float* kernel_ms) {
+  jgb::CtxLock lock(x);
+  if (!x || nret <= 0 || !n || !A) return ctx_error(x, JGB_ERR_ARG, "bad arguments");
+  if (nret > 65535) return ctx_error(x, JGB_ERR_ARG, "at most 65535 matrices per call");
+  CtxView v;
+  int rc = ctx_view(x, &v);  // only the device and the stream are needed
+  if (rc != JGB_OK && rc != JGB_ERR_STATE) return rc;
+  rc = JGB_OK;  // tables are not needed: a context without them is fine
+  cudaSetDevice(v.device);
+  (void)cudaGetLastError();  // launch errors below are this call's
+  std::vector<RetDesc> desc(nret);
+  long long so = 0;
+  int nmax = 1;
+  for (int i = 0; i < nret; i++) {
+    if (n[i] <= 0) return ctx_error(x, JGB_ERR_ARG, "empty matrix");
+    desc[i] = RetDesc{n[i], 0, 0, 0, so, 0};
+    so += (long long)n[i] * n[i];
+    nmax = std::max(nmax, n[i]);
+  }
+  // scratch: descriptors, flags and status, the factors, the column solves
+  const size_t b_desc = (sizeof(RetDesc) * (size_t)nret + 255) & ~size_t(255);
+  const size_t b_flags = (sizeof(int) * 3 * (size_t)nret + 255) & ~size_t(255);
+  void* buf = nullptr;
+  if (cudaMalloc(&buf, b_desc + b_flags + sizeof(double) * 2 * (size_t)so) != cudaSuccess)
+    return ctx_error(x, JGB_ERR_CUDA, "cudaMalloc failed");
+  char* p = static_cast<char*>(buf);
+  RetDesc* d = reinterpret_cast<RetDesc*>(p);
+  int* diag = reinterpret_cast<int*>(p + b_desc);
+  int* full = diag + nret;
+  int* st = full + nret;
+  double* L = reinterpret_cast<double*>(p + b_desc + b_flags);
+  double* W = L + so;
+  cudaStream_t s = v.stream;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaMemcpyAsync(d, desc.data(), sizeof(RetDesc) * nret, cudaMemcpyHostToDevice, s);
+  cudaEventRecord(e0, s);
+  k_invert_flags<<<nret, 256, 0, s>>>(nret, d, A, diag, full, st);
+  k_diag_inverse<<<nret, 128, 0, s>>>(nret, d, diag, A);
+  k_select_nn<<<dim3(16, nret), 256, 0, s>>>(nret, d, full, A, L);
+  k_chol_factor<<<nret, 1024, 0, s>>>(nret, d, full, L, st);
+  k_drop_failed<<<(nret + 255) / 256, 256, 0, s>>>(nret, st, full);
+  k_chol_inverse_cols<<<dim3((nmax + 63) / 64, nret), 64, 0, s>>>(nret, d, full, L, W);
+  k_sym_half<<<dim3(16, nret), 256, 0, s>>>(nret, d, full, W, A);
+  cudaEventRecord(e1, s);
+  cudaError_t err = cudaGetLastError();
+  std::vector<int> hst(nret);
+  if (err == cudaSuccess)
+    err = cudaMemcpyAsync(hst.data(), st, sizeof(int) * nret, cudaMemcpyDeviceToHost, s);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+  if (err == cudaSuccess && kernel_ms) cudaEventElapsedTime(kernel_ms, e0, e1);
+  if (err == cudaSuccess && status) std::memcpy(status, hst.data(), sizeof(int) * nret);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(buf);
+  if (err != cudaSuccess)
+    return ctx_error(x, JGB_ERR_CUDA,
+                     std::string("matrix inversion kernels: ") + cudaGetErrorString(err));
+  return JGB_OK;
+}
+
+extern "C" int jgb_matrix_invert(jgb_ctx* x, int nret, const int* n, double* A, int* status) {
+  jgb::CtxLock lock(x);
+  if (!x || nret <= 0 || !n || !A) return ctx_error(x, JGB_ERR_ARG, "bad arguments");
+  long long so = 0;
+  for (int i = 0; i < nret; i++) {
+    if (n[i] <= 0) return ctx_error(x, JGB_ERR_ARG, "empty matrix");
+    so += (long long)n[i] * n[i];
+  }
+  CtxView v;
+  int rc = ctx_view(x, &v);
+  if (rc != JGB_OK && rc != JGB_ERR_STATE) return rc;
+  cudaSetDevice(v.device);
+  jgb::DevBuf dA;
+  if (dA.reserve(sizeof(double) * (size_t)so) != cudaSuccess)
+    return ctx_error(x, JGB_ERR_CUDA, "cudaMalloc failed");
+  if (cudaMemcpyAsync(dA.p, A, sizeof(double) * so, cudaMemcpyHostToDevice, v.stream) != cudaSuccess)
+    return ctx_error(x, JGB_ERR_CUDA, "copy to the device failed");
+  rc = jgb_matrix_invert_dev(x, nret, n, dA.as<double>(), status, nullptr);
+  if (rc) return rc;
+  if (cudaMemcpyAsync(A, dA.p, sizeof(double) * so, cudaMemcpyDeviceToHost, v.stream) != cudaSuccess ||
+      cudaStreamSynchronize(v.stream) != cudaSuccess)
+    return ctx_error(x, JGB_ERR_CUDA, "copy to the host failed");
+  return JGB_OK;
 }

@@ -137,6 +137,9 @@ SIGNATURES = {
     "jgb_normal_equations_dev": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, C.c_void_p, C.c_void_p,
                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                            C.POINTER(C.c_float)]),
+    "jgb_matrix_invert": (C.c_int, [C.c_void_p, C.c_int, _ip, _dp, _ip]),
+    "jgb_matrix_invert_dev": (C.c_int, [C.c_void_p, C.c_int, _ip, C.c_void_p, _ip,
+                                        C.POINTER(C.c_float)]),
     "jgb_retrieve_batch": (C.c_int, [C.c_void_p, C.POINTER(_Ret), C.POINTER(_Batch), _dp, _dp,
                                      _dp, _ip, C.c_int]),
     "jgb_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
@@ -416,6 +419,21 @@ class Context:
             oa += ni * ni
             ob += ni
         return outA, outb
+
+    def matrix_invert(self, As):
+        """Inverses of a list of symmetric positive-definite matrices
+        (matrix_invert, retrieval.c:373-399), FP64 on the device.  Returns
+        (inverses, status); status[i] = 1 where A_i is not positive definite
+        (its entry is then A_i unchanged)."""
+        n = np.array([a.shape[0] for a in As], np.int32)
+        A = _d(np.concatenate([np.ravel(a) for a in As]))
+        st = np.zeros(len(As), np.int32)
+        self._check(load().jgb_matrix_invert(self.h, len(As), _p(n, _ip), _p(A), _p(st, _ip)))
+        out, o = [], 0
+        for ni in n:
+            out.append(A[o:o + ni * ni].reshape(ni, ni))
+            o += ni * ni
+        return out, st
 
     def contributions(self, batch, precision: int = FP64):
         """Emitter contributions (TASK c, src/formod.c:200-249): continua off,

@@ -1543,6 +1543,10 @@ static int sym_invert(double *a, int n) {
   return 0;
 }
 
+int jrc_matrix_invert(double *a, int n) {
+  return n > 0 && a ? sym_invert(a, n) : -1;
+}
+
 /* K^T diag(w)^2 K (matrix_product, retrieval.c:403-444, transpose == 1). */
 static void ktwk(const double *kmat, const double *w, int m, int n, double *out) {
   double *aux = malloc((size_t) m * (size_t) n * sizeof(double));

@@ -151,6 +151,12 @@ int jrc_retrieval_ex(jrc_ctx *c, const jrc_ret *ret, const jrc_atm *atm_apr,
                      double *cov, double *costs, int maxcost, int *info,
                      int nthreads, jrc_ana *ana);
 
+/* matrix_invert (retrieval.c:373-399) of one n x n row-major matrix in
+   place: the reciprocal diagonal if every element right of the diagonal is
+   zero, else the Cholesky inverse (symmetrised).  Returns -1 when a is not
+   positive definite (a is then partly factored), else 0. */
+int jrc_matrix_invert(double *a, int n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -115,8 +115,17 @@ def lib():
         L.jrc_retrieval_ex.argtypes = [C.c_void_p, C.POINTER(_Ret), C.POINTER(_Atm),
                                        C.POINTER(_Obs), _dp, _dp, _dp, _dp, C.c_int, _ip, C.c_int,
                                        C.POINTER(_Ana)]
+        L.jrc_matrix_invert.argtypes = [_dp, C.c_int]
         _lib = L
     return _lib
+
+
+def matrix_invert(a):
+    """matrix_invert (retrieval.c:373-399) of one square matrix: returns
+    (inverse, ok); ok is False where the matrix is not positive definite."""
+    a = np.array(a, dtype=np.float64, order="C")
+    rc = lib().jrc_matrix_invert(_ptr(a), a.shape[0])
+    return a, rc == 0
 
 
 def continua_blob():
